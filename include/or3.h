@@ -1,0 +1,239 @@
+/*
+ * or3.h -- C ABI of the GB300 path-tracing hot path (libor3.so).
+ *
+ * This is the drop-in boundary for omochi-renderer3's render call.  The
+ * reference renders through the abstract `Renderer` interface
+ * (src/renderer/Renderer.h:10-23), implemented by `PathTracer`
+ * (src/renderer/PathTracer.h:18-88).  A C++ host class mirrors that interface
+ * on top of the functions below (omochi-renderer3_gb300/host/GpuPathTracer.hpp),
+ * so the reference's `main` changes by one line.
+ *
+ * Conventions
+ *   - Every function returns an int status: OR3_OK (0) or a negative OR3_ERR_*
+ *     code.  No exception or abort crosses the ABI; or3_last_error() gives the
+ *     message of the last failure on a context.
+ *   - Scene data enters in the reference's own precision (double) and layout
+ *     conventions; the library flattens and converts it (FP32 on the device).
+ *   - Pointers named *_host are host memory, *_dev are device memory of the
+ *     context's GPU.
+ *   - A context is used from one host thread at a time, except or3_stop() and
+ *     or3_get_frame(), which may be called from other threads while
+ *     or3_render() runs (the reference's timer and saver threads do this:
+ *     src/tools/StopRendererWithTimer.cpp:38-40,
+ *     src/tools/FileSaverCallerWithTimer.cpp:59-66).
+ */
+#ifndef OR3_H_
+#define OR3_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OR3_API_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define OR3_OK 0
+#define OR3_ERR_INVALID_ARGUMENT (-1)
+#define OR3_ERR_CUDA (-2)
+#define OR3_ERR_OUT_OF_MEMORY (-3)
+#define OR3_ERR_NO_DEVICE (-4)
+#define OR3_ERR_NOT_FOUND (-5)
+/* A kernel reported an internal limit (traversal stack, queue capacity,
+   bounded wait); the context stays usable. */
+#define OR3_ERR_DEVICE_REPORTED (-6)
+#define OR3_ERR_BUSY (-7)
+
+/* ---- materials (src/renderer/Material.h:9-36) --------------------------- */
+#define OR3_LAMBERT 0    /* REFLECTION_TYPE_LAMBERT */
+#define OR3_SPECULAR 1   /* REFLECTION_TYPE_SPECULAR */
+#define OR3_REFRACTION 2 /* REFLECTION_TYPE_REFRACTION */
+#define OR3_PHONG 3      /* glossy lobe; no counterpart in the reference */
+
+typedef struct or3_material {
+  int32_t type;          /* OR3_LAMBERT .. OR3_PHONG */
+  int32_t texture;       /* index into or3_scene_desc textures, -1 = none */
+  double emission[3];    /* Material::emission */
+  double color[3];       /* Material::color */
+  double ior;            /* Material::refraction_rate */
+  double phong_exponent; /* OR3_PHONG only */
+} or3_material;
+
+/* ---- flattened scene ---------------------------------------------------
+ * One record per reference SceneObject.  `id` fields give the object's
+ * insertion index in the reference Scene (AddObject order,
+ * src/scenes/Scene.h:48-59); closest-hit queries return these ids, so they
+ * compare one-to-one with the reference's `IntersectionInformation::object`.
+ * If an id array is NULL the ids are 0..n-1 per primitive class, offset by
+ * the counts of the classes before it (triangles, spheres, planes).
+ *
+ * Each object has a list of material layers chosen by roulette with the
+ * given rates (SceneObject::MultiMaterialElem, src/renderer/SceneObject.h:17-67);
+ * `*_layers` holds [begin, count] into layer_material/layer_rate.
+ */
+#define OR3_SPHERE_LIGHT 1u   /* sphere_flags bit: a SphereLight (src/renderer/SphereLight.h:8) */
+
+#define OR3_PLANE_AXIS_ALIGNED 0 /* AxisAlignedPlane (src/renderer/AxisAlignedPlane.h:9-70) */
+#define OR3_PLANE_INFINITE_FLOOR 1 /* InfiniteFloor (src/renderer/InfiniteFloor.h:11-42) */
+
+typedef struct or3_scene_desc {
+  uint32_t num_materials;
+  const or3_material *materials;
+  uint32_t num_layers;
+  const uint32_t *layer_material; /* [num_layers] */
+  const double *layer_rate;       /* [num_layers], normalised per object */
+
+  /* Polygon (src/renderer/Polygon.h:11-136), in BVH */
+  uint32_t num_triangles;
+  const double *tri_vertices; /* [n][3][3] world positions (pos_i + position_) */
+  const double *tri_normals;  /* [n][3][3] per-vertex normals, NULL = face normal */
+  const double *tri_uvs;      /* [n][3][2], NULL = zero */
+  const uint32_t *tri_layers; /* [n][2] */
+  const uint32_t *tri_ids;    /* [n] or NULL */
+
+  /* Sphere / SphereLight (src/renderer/Sphere.h:11-82), in BVH */
+  uint32_t num_spheres;
+  const double *spheres;         /* [n][4] center xyz, radius */
+  const uint32_t *sphere_layers; /* [n][2] */
+  const uint32_t *sphere_flags;  /* [n] OR3_SPHERE_LIGHT, or NULL */
+  const uint32_t *sphere_ids;    /* [n] or NULL */
+
+  /* objects kept out of the BVH (Scene::m_notInBVHObjects) */
+  uint32_t num_planes;
+  const double *planes;         /* [n][4] kind, axis(0=XY,1=XZ,2=YZ), offset, flip */
+  const uint32_t *plane_layers; /* [n][2] */
+  const uint32_t *plane_ids;    /* [n] or NULL */
+
+  /* IBL equirect image (src/renderer/IBL.h:30-45), row-major RGB float */
+  uint32_t env_width, env_height;
+  const float *env_rgb;  /* NULL = no IBL: misses return `background` */
+  double background[3];  /* Scene::Background() (src/scenes/Scene.h:40) */
+
+  /* textures (src/tools/Image.h:20-31): RGB float, linear */
+  uint32_t num_textures;
+  const uint32_t *texture_dims;    /* [n][2] width, height */
+  const uint64_t *texture_offsets; /* [n] float offset into texture_rgb */
+  const float *texture_rgb;
+} or3_scene_desc;
+
+/* ---- camera (src/renderer/Camera.h:12-43, :65-93; Aperture.h:23-35) ---- */
+typedef struct or3_camera {
+  uint32_t width, height;
+  double position[3];
+  double direction[3];
+  double up[3];
+  double screen_height_world; /* Camera::m_nearScreenHeight */
+  double distance_to_screen;  /* Camera::m_distToScreen */
+  double focal_distance;      /* Camera::m_focalDistance */
+  double aperture_radius;     /* CircleAperture radius, 0 = pinhole (no aperture) */
+} or3_camera;
+
+/* ---- render parameters (PathTracer ctor, src/renderer/PathTracer.h:25-37) */
+#define OR3_LAYOUT_REFERENCE 0 /* 2W x H doubles, image in the left viewport, rows top-down
+                                  (ScreenPixels with 2x1 viewports, src/renderer/ScreenPixels.cpp:37-65) */
+#define OR3_LAYOUT_COMPACT 1   /* W x H doubles, rows top-down */
+
+#define OR3_FLAG_KEEP_PATHS 1u   /* keep per-path radiance of the last wave (testing) */
+#define OR3_FLAG_UNSORTED 2u     /* shade without partitioning rays by material */
+#define OR3_FLAG_NO_GRAPH 4u     /* launch the bounce loop without a CUDA graph */
+#define OR3_FLAG_NO_TAIL 8u      /* no single-launch tail for the last few rays */
+
+typedef struct or3_render_params {
+  int32_t min_samples;   /* PathTracer m_min_samples */
+  int32_t max_samples;   /* m_max_samples */
+  int32_t step_samples;  /* m_step_samples */
+  int32_t supersamples;  /* m_supersamples (ss x ss fixed grid per pixel) */
+  int32_t next_event_estimation; /* 0 = off (the reference default);
+                                    1 = light sampling with shadow rays (not in the reference) */
+  int32_t rr_min_depth;  /* Russian roulette for depth > this; reference MinDepth = 5 */
+  int32_t max_depth;     /* rays at depth >= max_depth are not traced; 0 = unbounded (reference) */
+  int32_t output_layout; /* OR3_LAYOUT_* */
+  uint64_t seed;         /* counter-based RNG key */
+  uint64_t wave_paths;   /* camera paths per wave, 0 = automatic */
+  uint32_t flags;        /* OR3_FLAG_* */
+  uint32_t reserved;
+} or3_render_params;
+
+/* Called after each pass, like PathTracer's RenderingFinishCallbackFunction
+   (src/renderer/PathTracer.h:21): samples so far, the frame in the requested
+   layout, its width/height in doubles-per-row / rows, accumulated minutes. */
+typedef void (*or3_frame_callback)(void *user, int32_t samples, const double *rgb,
+                                   size_t width, size_t height, double minutes);
+
+typedef struct or3_render_stats {
+  uint64_t camera_paths;   /* W*H*ss*ss*samples rendered */
+  uint64_t extension_rays; /* closest-hit queries */
+  uint64_t shadow_rays;    /* any-hit queries */
+  uint64_t bounces;        /* bounce iterations launched */
+  uint64_t waves;
+  double render_ms;        /* device time of the passes (CUDA events) */
+  double upload_ms;        /* scene upload + BVH build of the rendered scene */
+  int32_t samples;         /* samples per subpixel accumulated */
+  int32_t passes;
+} or3_render_stats;
+
+typedef struct or3_scene_info {
+  uint64_t num_primitives;
+  uint64_t num_nodes;      /* 64-byte wide nodes */
+  uint64_t device_bytes;
+  double build_ms;         /* host BVH build */
+  double upload_ms;        /* H2D copies */
+  int32_t tree_depth;
+  int32_t reserved;
+} or3_scene_info;
+
+typedef struct or3_context or3_context;
+
+/* ---- context ----------------------------------------------------------- */
+int or3_context_create(int device, or3_context **out);
+int or3_context_destroy(or3_context *ctx);
+const char *or3_last_error(const or3_context *ctx);
+int or3_api_version(void);
+
+/* ---- scenes (replaces Scene::ConstructBVH/ConstructQBVH,
+        src/scenes/Scene.cpp:27-49, and the data Scene::CheckIntersection walks) */
+int or3_scene_upload(or3_context *ctx, const or3_scene_desc *desc, int32_t *scene_out);
+int or3_scene_release(or3_context *ctx, int32_t scene);
+int or3_scene_get_info(or3_context *ctx, int32_t scene, or3_scene_info *out);
+
+/* ---- render (replaces PathTracer::RenderScene, src/renderer/PathTracer.cpp:55-85)
+   Blocking.  Calls `cb` (may be NULL) after every pass. */
+int or3_render(or3_context *ctx, int32_t scene, const or3_camera *camera,
+               const or3_render_params *params, or3_frame_callback cb, void *user);
+/* Renderer::StopRendering (src/renderer/Renderer.h:22); safe from any thread. */
+int or3_stop(or3_context *ctx);
+/* Clears the stop request so the next or3_render runs. */
+int or3_reset_stop(or3_context *ctx);
+/* Last completed frame (Renderer::GetResult): `capacity` doubles. */
+int or3_get_frame(or3_context *ctx, double *rgb_host, size_t capacity, int32_t *samples_out);
+int or3_get_stats(or3_context *ctx, or3_render_stats *out);
+/* Per-pixel sums of path radiance and of its square, rows top-down, W*H*3
+   doubles each (either may be NULL); count = paths per pixel. */
+int or3_get_moments(or3_context *ctx, double *sum_host, double *sumsq_host, size_t capacity,
+                    uint64_t *count_out);
+/* Per-path radiance of the last wave when OR3_FLAG_KEEP_PATHS was set:
+   3 floats per path, in camera-path order
+   g = ((s * H + y) * W + x) * ss*ss + sy*ss + sx, counted from the wave's first
+   path (s = sample index from 0, y = camera row with 0 at the bottom as in
+   PathTracer::scanPixelsOnYAndCastRays, src/renderer/PathTracer.cpp:143-175). */
+int or3_get_path_radiance(or3_context *ctx, float *rgb_host, size_t capacity, uint64_t *paths_out);
+
+/* ---- ray queries (replaces Scene::CheckIntersection, src/scenes/Scene.cpp:51-85)
+   Closest hit of n rays: prim id (object id, -1 = miss), distance t, and the
+   shading normal as the reference reports it (interpolated for triangles). */
+int or3_trace_closest(or3_context *ctx, int32_t scene, size_t n, const float *origins_host,
+                      const float *dirs_host, int32_t *prim_host, float *t_host,
+                      float *normal_host);
+int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const float *origins_dev,
+                             const float *dirs_dev, int32_t *prim_dev, float *t_dev,
+                             float *normal_dev, void *stream);
+/* Any hit in (EPS, tmax) for shadow rays: 1 = occluded. */
+int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *origins_host,
+                       const float *dirs_host, const float *tmax_host, uint8_t *occluded_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OR3_H_ */

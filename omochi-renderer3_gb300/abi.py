@@ -1,0 +1,140 @@
+"""ctypes mirror of include/or3.h and the loader for libor3.so.
+
+The loader never falls back to anything: if the CUDA library is missing or was
+built for another ABI version, it raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+c_double3 = ctypes.c_double * 3
+
+OR3_OK = 0
+OR3_ERR_INVALID_ARGUMENT = -1
+OR3_ERR_CUDA = -2
+OR3_ERR_OUT_OF_MEMORY = -3
+OR3_ERR_NO_DEVICE = -4
+OR3_ERR_NOT_FOUND = -5
+OR3_ERR_DEVICE_REPORTED = -6
+OR3_ERR_BUSY = -7
+
+OR3_LAMBERT, OR3_SPECULAR, OR3_REFRACTION, OR3_PHONG = 0, 1, 2, 3
+OR3_SPHERE_LIGHT = 1
+OR3_PLANE_AXIS_ALIGNED, OR3_PLANE_INFINITE_FLOOR = 0, 1
+OR3_LAYOUT_REFERENCE, OR3_LAYOUT_COMPACT = 0, 1
+OR3_FLAG_KEEP_PATHS = 1
+OR3_FLAG_UNSORTED = 2
+OR3_FLAG_NO_GRAPH = 4
+OR3_FLAG_NO_TAIL = 8
+
+API_VERSION = 1
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("texture", ctypes.c_int32), ("emission", c_double3),
+                ("color", c_double3), ("ior", ctypes.c_double), ("phong_exponent", ctypes.c_double)]
+
+
+P = ctypes.POINTER
+u32p = P(ctypes.c_uint32)
+f64p = P(ctypes.c_double)
+f32p = P(ctypes.c_float)
+
+
+class SceneDescC(ctypes.Structure):
+    _fields_ = [
+        ("num_materials", ctypes.c_uint32), ("materials", P(Material)),
+        ("num_layers", ctypes.c_uint32), ("layer_material", u32p), ("layer_rate", f64p),
+        ("num_triangles", ctypes.c_uint32), ("tri_vertices", f64p), ("tri_normals", f64p), ("tri_uvs", f64p),
+        ("tri_layers", u32p), ("tri_ids", u32p),
+        ("num_spheres", ctypes.c_uint32), ("spheres", f64p), ("sphere_layers", u32p), ("sphere_flags", u32p),
+        ("sphere_ids", u32p),
+        ("num_planes", ctypes.c_uint32), ("planes", f64p), ("plane_layers", u32p), ("plane_ids", u32p),
+        ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32), ("env_rgb", f32p),
+        ("background", c_double3),
+        ("num_textures", ctypes.c_uint32), ("texture_dims", u32p), ("texture_offsets", P(ctypes.c_uint64)),
+        ("texture_rgb", f32p),
+    ]
+
+
+class CameraC(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("position", c_double3),
+                ("direction", c_double3), ("up", c_double3), ("screen_height_world", ctypes.c_double),
+                ("distance_to_screen", ctypes.c_double), ("focal_distance", ctypes.c_double),
+                ("aperture_radius", ctypes.c_double)]
+
+
+class RenderParamsC(ctypes.Structure):
+    _fields_ = [("min_samples", ctypes.c_int32), ("max_samples", ctypes.c_int32),
+                ("step_samples", ctypes.c_int32), ("supersamples", ctypes.c_int32),
+                ("next_event_estimation", ctypes.c_int32), ("rr_min_depth", ctypes.c_int32),
+                ("max_depth", ctypes.c_int32), ("output_layout", ctypes.c_int32),
+                ("seed", ctypes.c_uint64), ("wave_paths", ctypes.c_uint64),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class RenderStatsC(ctypes.Structure):
+    _fields_ = [("camera_paths", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64), ("bounces", ctypes.c_uint64), ("waves", ctypes.c_uint64),
+                ("render_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
+                ("samples", ctypes.c_int32), ("passes", ctypes.c_int32)]
+
+
+class SceneInfoC(ctypes.Structure):
+    _fields_ = [("num_primitives", ctypes.c_uint64), ("num_nodes", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_uint64), ("build_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
+                ("tree_depth", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, f64p, ctypes.c_size_t, ctypes.c_size_t,
+                            ctypes.c_double)
+
+# name -> (restype, argtypes); every function declared in include/or3.h
+PROTOTYPES = {
+    "or3_api_version": (ctypes.c_int, []),
+    "or3_context_create": (ctypes.c_int, [ctypes.c_int, P(ctypes.c_void_p)]),
+    "or3_context_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "or3_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "or3_scene_upload": (ctypes.c_int, [ctypes.c_void_p, P(SceneDescC), P(ctypes.c_int32)]),
+    "or3_scene_release": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "or3_scene_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(SceneInfoC)]),
+    "or3_render": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(CameraC), P(RenderParamsC), FRAME_CB,
+                                  ctypes.c_void_p]),
+    "or3_stop": (ctypes.c_int, [ctypes.c_void_p]),
+    "or3_reset_stop": (ctypes.c_int, [ctypes.c_void_p]),
+    "or3_get_frame": (ctypes.c_int, [ctypes.c_void_p, f64p, ctypes.c_size_t, P(ctypes.c_int32)]),
+    "or3_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(RenderStatsC)]),
+    "or3_get_moments": (ctypes.c_int, [ctypes.c_void_p, f64p, f64p, ctypes.c_size_t, P(ctypes.c_uint64)]),
+    "or3_get_path_radiance": (ctypes.c_int, [ctypes.c_void_p, f32p, ctypes.c_size_t, P(ctypes.c_uint64)]),
+    "or3_trace_closest": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, f32p, f32p,
+                                         P(ctypes.c_int32), f32p, f32p]),
+    "or3_trace_closest_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
+    "or3_trace_occluded": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, f32p, f32p, f32p,
+                                          P(ctypes.c_uint8)]),
+}
+
+_LIB = None
+
+
+def load_library(build_if_missing=True):
+    """Loads the in-tree libor3.so (building it first if asked and needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if build_if_missing and _build.needs_build():
+        _build.build_library()
+    if not os.path.exists(path):
+        raise RuntimeError("libor3.so is not built (%s); run __graft_entry__.build()" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.or3_api_version() != API_VERSION:
+        raise RuntimeError("libor3.so ABI version %d != %d" % (lib.or3_api_version(), API_VERSION))
+    _LIB = lib
+    return lib

@@ -1,0 +1,827 @@
+// or3_api.cu -- the C ABI (include/or3.h): contexts, scene upload, render loop,
+// ray-set queries.  Host side of the GB300 path-tracing hot path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "or3.h"
+#include "or3_kernels.cuh"
+
+using namespace or3;
+
+namespace {
+
+struct SceneGPU {
+  DevScene view{};
+  std::vector<void *> allocs;
+  or3_scene_info info{};
+  bool has_split = false;  // a refractive layer exists: paths can split at depth <= 2
+};
+
+}  // namespace
+
+struct or3_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<int32_t, SceneGPU *> scenes;
+  int32_t next_scene = 1;
+  int num_sms = 0;
+  int occ_extend = 1, occ_shade = 1;
+
+  // queues
+  size_t cap_rays = 0, cap_paths = 0;
+  float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
+  float4 *hits = nullptr, *pathL = nullptr;
+  uint32_t *counters = nullptr;
+  unsigned long long *dstats = nullptr;
+  uint32_t *host_counters = nullptr;  // pinned
+
+  // accumulation + frames
+  size_t cap_pixels = 0;
+  double *pix_sum = nullptr, *pix_sumsq = nullptr;
+  size_t cap_frame = 0;
+  double *frame_dev = nullptr, *frame_pinned = nullptr;
+  std::vector<double> frame_host;  // last completed frame (Renderer::GetResult)
+  std::mutex frame_mu;
+  int32_t frame_samples = 0;
+
+  std::atomic<bool> stop{false};
+  or3_render_stats last{};
+  uint32_t last_W = 0, last_H = 0;
+  uint64_t last_count = 0;  // paths per pixel in the moments
+  bool moments_valid = false;
+  uint64_t last_wave_paths = 0;
+  bool last_kept_paths = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int fail(or3_context *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return code;
+}
+
+#define OR3_CUDA(ctx, call)                                                                      \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) {                                                                     \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? OR3_ERR_OUT_OF_MEMORY : OR3_ERR_CUDA,   \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);  \
+    }                                                                                            \
+  } while (0)
+
+template <class T>
+int dev_upload(or3_context *ctx, SceneGPU *sg, const std::vector<T> &v, const T **out) {
+  *out = nullptr;
+  if (v.empty()) return OR3_OK;
+  void *p = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&p, v.size() * sizeof(T)));
+  sg->allocs.push_back(p);
+  OR3_CUDA(ctx, cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  sg->info.device_bytes += v.size() * sizeof(T);
+  *out = static_cast<const T *>(p);
+  return OR3_OK;
+}
+
+void free_scene(SceneGPU *sg) {
+  for (void *p : sg->allocs) cudaFree(p);
+  delete sg;
+}
+
+float down(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+float up(double x) {
+  float f = (float)x;
+  if ((double)f < x) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+int check_layers(or3_context *ctx, const or3_scene_desc *d, const uint32_t *lay, const char *what, uint32_t i) {
+  if (lay[1] == 0 || (uint64_t)lay[0] + lay[1] > d->num_layers)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s %u: layer range [%u,+%u) outside %u layers", what, i, lay[0],
+                lay[1], d->num_layers);
+  return OR3_OK;
+}
+
+uint32_t layer_flags(const or3_scene_desc *d, const uint32_t *lay) {
+  uint32_t f = 0;
+  for (uint32_t k = 0; k < lay[1]; k++) {
+    const or3_material &m = d->materials[d->layer_material[lay[0] + k]];
+    if (m.texture >= 0) f |= kFlagTexturedUV;
+    if (m.emission[0] * m.emission[0] + m.emission[1] * m.emission[1] + m.emission[2] * m.emission[2] != 0)
+      f |= kFlagEmissive;
+  }
+  return f;
+}
+
+int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
+  if (paths <= ctx->cap_paths && rays <= ctx->cap_rays) return OR3_OK;
+  for (int k = 0; k < 2; k++) {
+    cudaFree(ctx->qorig[k]);
+    cudaFree(ctx->qdir[k]);
+    cudaFree(ctx->qbeta[k]);
+    ctx->qorig[k] = ctx->qdir[k] = ctx->qbeta[k] = nullptr;
+  }
+  cudaFree(ctx->hits);
+  cudaFree(ctx->pathL);
+  ctx->hits = ctx->pathL = nullptr;
+  ctx->cap_paths = ctx->cap_rays = 0;
+  for (int k = 0; k < 2; k++) {
+    OR3_CUDA(ctx, cudaMalloc(&ctx->qorig[k], rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&ctx->qdir[k], rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&ctx->qbeta[k], rays * sizeof(float4)));
+  }
+  OR3_CUDA(ctx, cudaMalloc(&ctx->hits, rays * sizeof(float4)));
+  OR3_CUDA(ctx, cudaMalloc(&ctx->pathL, paths * sizeof(float4)));
+  ctx->cap_paths = paths;
+  ctx->cap_rays = rays;
+  return OR3_OK;
+}
+
+int ensure_pixels(or3_context *ctx, size_t pixels, size_t frame_doubles) {
+  if (pixels > ctx->cap_pixels) {
+    cudaFree(ctx->pix_sum);
+    cudaFree(ctx->pix_sumsq);
+    ctx->pix_sum = ctx->pix_sumsq = nullptr;
+    ctx->cap_pixels = 0;
+    OR3_CUDA(ctx, cudaMalloc(&ctx->pix_sum, pixels * 3 * sizeof(double)));
+    OR3_CUDA(ctx, cudaMalloc(&ctx->pix_sumsq, pixels * 3 * sizeof(double)));
+    ctx->cap_pixels = pixels;
+  }
+  if (frame_doubles > ctx->cap_frame) {
+    cudaFree(ctx->frame_dev);
+    cudaFreeHost(ctx->frame_pinned);
+    ctx->frame_dev = nullptr;
+    ctx->frame_pinned = nullptr;
+    ctx->cap_frame = 0;
+    OR3_CUDA(ctx, cudaMalloc(&ctx->frame_dev, frame_doubles * sizeof(double)));
+    OR3_CUDA(ctx, cudaMallocHost(&ctx->frame_pinned, frame_doubles * sizeof(double)));
+    ctx->cap_frame = frame_doubles;
+  }
+  return OR3_OK;
+}
+
+Queues make_queues(or3_context *ctx) {
+  Queues q{};
+  for (int k = 0; k < 2; k++) {
+    q.orig[k] = ctx->qorig[k];
+    q.dir[k] = ctx->qdir[k];
+    q.beta[k] = ctx->qbeta[k];
+  }
+  q.hits = ctx->hits;
+  q.pathL = ctx->pathL;
+  q.counters = ctx->counters;
+  q.stats = ctx->dstats;
+  q.capacity = (uint32_t)ctx->cap_rays;
+  return q;
+}
+
+// Camera::Camera (src/renderer/Camera.h:12-43) in double.
+void camera_basis(const or3_camera *c, Camera32 &out) {
+  double dir[3] = {c->direction[0], c->direction[1], c->direction[2]};
+  double upv[3] = {c->up[0], c->up[1], c->up[2]};
+  auto nrm = [](double *v) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= l; v[1] /= l; v[2] /= l;
+  };
+  auto crs = [](const double *a, const double *b, double *r) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  nrm(dir);
+  nrm(upv);
+  const double sh = c->screen_height_world;
+  const double sw = c->screen_height_world * (double)c->width / (double)c->height;
+  double X[3], Y[3];
+  crs(dir, upv, X);
+  nrm(X);
+  crs(X, dir, Y);
+  nrm(Y);
+  for (int a = 0; a < 3; a++) {
+    out.pos[a] = (float)c->position[a];
+    out.center[a] = (float)(c->position[a] + dir[a] * c->distance_to_screen);
+    out.xaxis[a] = (float)(X[a] * sw);
+    out.yaxis[a] = (float)(Y[a] * sh);
+  }
+  out.focal = (float)c->focal_distance;
+  out.aperture = (float)c->aperture_radius;
+}
+
+}  // namespace
+
+extern "C" {
+
+int or3_api_version(void) { return OR3_API_VERSION; }
+
+const char *or3_last_error(const or3_context *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int or3_context_create(int device, or3_context **out) {
+  if (!out) return OR3_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return OR3_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return OR3_ERR_INVALID_ARGUMENT;
+  or3_context *ctx = new or3_context();
+  ctx->device = device;
+  auto bail = [&](int code) {
+    delete ctx;
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(OR3_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(OR3_ERR_CUDA);
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_extend, kernel_extend_ptr(), 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_shade, kernel_shade_ptr(), 256, 0);
+  ctx->occ_extend = std::max(ctx->occ_extend, 1);
+  ctx->occ_shade = std::max(ctx->occ_shade, 1);
+  if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
+  if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
+  if (cudaMallocHost(&ctx->host_counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
+  cudaMemset(ctx->counters, 0, 16 * sizeof(uint32_t));
+  cudaMemset(ctx->dstats, 0, 8 * sizeof(unsigned long long));
+  cudaEventCreate(&ctx->ev0);
+  cudaEventCreate(&ctx->ev1);
+  if (cudaDeviceSynchronize() != cudaSuccess) return bail(OR3_ERR_CUDA);
+  *out = ctx;
+  return OR3_OK;
+}
+
+int or3_context_destroy(or3_context *ctx) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->scenes) free_scene(kv.second);
+  for (int k = 0; k < 2; k++) {
+    cudaFree(ctx->qorig[k]);
+    cudaFree(ctx->qdir[k]);
+    cudaFree(ctx->qbeta[k]);
+  }
+  cudaFree(ctx->hits);
+  cudaFree(ctx->pathL);
+  cudaFree(ctx->counters);
+  cudaFree(ctx->dstats);
+  cudaFreeHost(ctx->host_counters);
+  cudaFree(ctx->pix_sum);
+  cudaFree(ctx->pix_sumsq);
+  cudaFree(ctx->frame_dev);
+  cudaFreeHost(ctx->frame_pinned);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return OR3_OK;
+}
+
+int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_out) {
+  if (!ctx || !d || !scene_out) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  cudaSetDevice(ctx->device);
+  *scene_out = -1;
+  // ---- validation
+  if (d->num_materials == 0 || !d->materials) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "no materials");
+  if (d->num_layers == 0 || !d->layer_material || !d->layer_rate)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "no material layers");
+  for (uint32_t i = 0; i < d->num_layers; i++)
+    if (d->layer_material[i] >= d->num_materials)
+      return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "layer %u: material %u out of range", i, d->layer_material[i]);
+  for (uint32_t i = 0; i < d->num_materials; i++) {
+    const or3_material &m = d->materials[i];
+    if (m.type < OR3_LAMBERT || m.type > OR3_PHONG)
+      return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "material %u: unknown type %d", i, m.type);
+    if (m.texture >= (int32_t)d->num_textures)
+      return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "material %u: texture %d out of range", i, m.texture);
+  }
+  if (d->num_triangles && (!d->tri_vertices || !d->tri_layers))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "triangles without vertices or layers");
+  if (d->num_spheres && (!d->spheres || !d->sphere_layers))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "spheres without data or layers");
+  if (d->num_planes && (!d->planes || !d->plane_layers))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "planes without data or layers");
+  if ((uint64_t)d->num_triangles + d->num_spheres >= (uint64_t)kPlaneBit)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "too many primitives");
+  if (d->env_rgb && (d->env_width == 0 || d->env_height == 0))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "environment map with zero size");
+
+  auto t0 = std::chrono::steady_clock::now();
+  SceneGPU *sg = new SceneGPU();
+  const uint32_t nt = d->num_triangles, nsph = d->num_spheres, np = nt + nsph;
+
+  // ---- primitives and their bounds (in the FP32 geometry the kernels test)
+  std::vector<float> geom(12 * (size_t)np, 0.f);
+  std::vector<BuildPrim> bp(np);
+  std::vector<PrimInfo> pinfo(np);
+  std::vector<TriShade> tshade(np);
+  for (uint32_t i = 0; i < nt; i++) {
+    int rc = check_layers(ctx, d, d->tri_layers + 2 * i, "triangle", i);
+    if (rc) { free_scene(sg); return rc; }
+    const double *v = d->tri_vertices + 9 * (size_t)i;
+    float *g = &geom[12 * (size_t)i];
+    for (int a = 0; a < 3; a++) {
+      g[a] = (float)v[a];                 // v0
+      g[3 + a] = (float)(v[3 + a] - v[a]);  // e1 = p1 - p0
+      g[6 + a] = (float)(v[6 + a] - v[a]);  // e2 = p2 - p0
+    }
+    for (int a = 0; a < 3; a++) {
+      const double p0 = g[a], p1 = (double)g[a] + g[3 + a], p2 = (double)g[a] + g[6 + a];
+      bp[i].lo[a] = down(std::min(p0, std::min(p1, p2)));
+      bp[i].hi[a] = up(std::max(p0, std::max(p1, p2)));
+    }
+    bp[i].kind = kPrimTriangle;
+    const uint32_t *lay = d->tri_layers + 2 * i;
+    pinfo[i] = PrimInfo{d->tri_ids ? d->tri_ids[i] : i, lay[0], lay[1], kPrimTriangle | (layer_flags(d, lay) << 8)};
+    TriShade &ts = tshade[i];
+    std::memset(&ts, 0, sizeof(ts));
+    double n0[3], n1[3], n2[3];
+    if (d->tri_normals) {
+      const double *n = d->tri_normals + 9 * (size_t)i;
+      for (int a = 0; a < 3; a++) { n0[a] = n[a]; n1[a] = n[3 + a]; n2[a] = n[6 + a]; }
+    } else {
+      const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+      const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+      double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+      const double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      for (int a = 0; a < 3; a++) n0[a] = n1[a] = n2[a] = l > 0 ? c[a] / l : 0.0;
+    }
+    for (int a = 0; a < 3; a++) {
+      ts.n0[a] = (float)n0[a];
+      ts.dn1[a] = (float)(n1[a] - n0[a]);
+      ts.dn2[a] = (float)(n2[a] - n0[a]);
+    }
+    if (d->tri_uvs) {
+      const double *u = d->tri_uvs + 6 * (size_t)i;
+      for (int a = 0; a < 2; a++) {
+        ts.uv0[a] = (float)u[a];
+        ts.duv1[a] = (float)(u[2 + a] - u[a]);
+        ts.duv2[a] = (float)(u[4 + a] - u[a]);
+      }
+    }
+  }
+  for (uint32_t j = 0; j < nsph; j++) {
+    const uint32_t i = nt + j;
+    int rc = check_layers(ctx, d, d->sphere_layers + 2 * j, "sphere", j);
+    if (rc) { free_scene(sg); return rc; }
+    const double *s = d->spheres + 4 * (size_t)j;
+    if (!(s[3] > 0)) { free_scene(sg); return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sphere %u: radius <= 0", j); }
+    float *g = &geom[12 * (size_t)i];
+    g[0] = (float)s[0]; g[1] = (float)s[1]; g[2] = (float)s[2]; g[3] = (float)s[3];
+    for (int a = 0; a < 3; a++) {
+      bp[i].lo[a] = down((double)g[a] - (double)g[3]);
+      bp[i].hi[a] = up((double)g[a] + (double)g[3]);
+    }
+    bp[i].kind = kPrimSphere;
+    const uint32_t *lay = d->sphere_layers + 2 * j;
+    uint32_t fl = layer_flags(d, lay);
+    if (d->sphere_flags && (d->sphere_flags[j] & OR3_SPHERE_LIGHT)) fl |= kFlagSphereLight;
+    pinfo[i] = PrimInfo{d->sphere_ids ? d->sphere_ids[j] : nt + j, lay[0], lay[1], kPrimSphere | (fl << 8)};
+  }
+
+  WideBVH bvh;
+  std::string berr;
+  if (!build_wide_bvh(bp, 16, 4, bvh, &berr)) {
+    free_scene(sg);
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s", berr.c_str());
+  }
+  auto t1 = std::chrono::steady_clock::now();
+
+  // ---- records in leaf order
+  std::vector<float4> prims(3 * (size_t)np);
+  std::vector<PrimInfo> info(np);
+  std::vector<TriShade> shade(np);
+  for (uint32_t r = 0; r < np; r++) {
+    const uint32_t src = bvh.order[r];
+    const float *g = &geom[12 * (size_t)src];
+    if (src < nt) {
+      prims[3 * r + 0] = make_float4(g[0], g[1], g[2], g[3]);
+      prims[3 * r + 1] = make_float4(g[4], g[5], g[6], g[7]);
+      prims[3 * r + 2] = make_float4(g[8], 0.f, 0.f, 0.f);
+    } else {
+      prims[3 * r + 0] = make_float4(g[0], g[1], g[2], g[3]);
+      prims[3 * r + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      prims[3 * r + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    info[r] = pinfo[src];
+    shade[r] = tshade[src];
+  }
+  std::vector<PlaneRec> planes(d->num_planes);
+  for (uint32_t i = 0; i < d->num_planes; i++) {
+    int rc = check_layers(ctx, d, d->plane_layers + 2 * i, "plane", i);
+    if (rc) { free_scene(sg); return rc; }
+    const double *p = d->planes + 4 * (size_t)i;
+    PlaneRec &pr = planes[i];
+    pr.kind = (int)p[0] == OR3_PLANE_INFINITE_FLOOR ? kPrimFloor : kPrimPlane;
+    pr.axis = (uint32_t)p[1];
+    if (pr.axis > 2) { free_scene(sg); return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "plane %u: axis %u", i, pr.axis); }
+    pr.offset = (float)p[2];
+    pr.normal_sign = p[3] != 0.0 ? -1.f : 1.f;
+    pr.object_id = d->plane_ids ? d->plane_ids[i] : np + i;
+    pr.layer_begin = d->plane_layers[2 * i];
+    pr.layer_count = d->plane_layers[2 * i + 1];
+    pr.flags = layer_flags(d, d->plane_layers + 2 * i);
+  }
+  std::vector<MaterialDev> mats(d->num_materials);
+  bool split = false;
+  for (uint32_t i = 0; i < d->num_materials; i++) {
+    const or3_material &m = d->materials[i];
+    MaterialDev &o = mats[i];
+    std::memset(&o, 0, sizeof(o));
+    for (int a = 0; a < 3; a++) {
+      o.emission[a] = (float)m.emission[a];
+      o.color[a] = (float)m.color[a];
+    }
+    o.ior = (float)m.ior;
+    o.phong_exponent = (float)m.phong_exponent;
+    o.type = m.type;
+    o.texture = m.texture;
+    o.emissive = (m.emission[0] * m.emission[0] + m.emission[1] * m.emission[1] + m.emission[2] * m.emission[2]) != 0;
+  }
+  std::vector<LayerDev> layers(d->num_layers);
+  for (uint32_t i = 0; i < d->num_layers; i++) {
+    layers[i].material = d->layer_material[i];
+    layers[i].rate = (float)d->layer_rate[i];
+    if (d->materials[d->layer_material[i]].type == OR3_REFRACTION) split = true;
+  }
+  sg->has_split = split;
+
+  DevScene &S = sg->view;
+  S.num_nodes = (uint32_t)bvh.nodes.size();
+  S.num_prims = np;
+  S.num_planes = d->num_planes;
+  S.bg[0] = (float)d->background[0];
+  S.bg[1] = (float)d->background[1];
+  S.bg[2] = (float)d->background[2];
+  int rc = OR3_OK;
+  const WideNode *nodes_dev = nullptr;
+  if ((rc = dev_upload(ctx, sg, bvh.nodes, &nodes_dev))) { free_scene(sg); return rc; }
+  S.nodes = reinterpret_cast<const uint4 *>(nodes_dev);
+  if ((rc = dev_upload(ctx, sg, prims, &S.prims))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, info, &S.info))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, shade, &S.tri_shade))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, planes, &S.planes))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, mats, &S.materials))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, layers, &S.layers))) { free_scene(sg); return rc; }
+  if (d->env_rgb) {
+    std::vector<float> env(d->env_rgb, d->env_rgb + 3 * (size_t)d->env_width * d->env_height);
+    if ((rc = dev_upload(ctx, sg, env, &S.env))) { free_scene(sg); return rc; }
+    S.env_w = d->env_width;
+    S.env_h = d->env_height;
+  }
+  if (d->num_textures) {
+    std::vector<TextureDev> tex(d->num_textures);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < d->num_textures; i++) {
+      tex[i].offset = d->texture_offsets[i];
+      tex[i].width = d->texture_dims[2 * i];
+      tex[i].height = d->texture_dims[2 * i + 1];
+      total = std::max<uint64_t>(total, tex[i].offset + 3ull * tex[i].width * tex[i].height);
+    }
+    std::vector<float> texels(d->texture_rgb, d->texture_rgb + total);
+    if ((rc = dev_upload(ctx, sg, tex, &S.textures))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, texels, &S.texels))) { free_scene(sg); return rc; }
+    S.num_textures = d->num_textures;
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    free_scene(sg);
+    return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(e));
+  }
+  auto t2 = std::chrono::steady_clock::now();
+  sg->info.num_primitives = np + d->num_planes;
+  sg->info.num_nodes = bvh.nodes.size();
+  sg->info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  sg->info.upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  sg->info.tree_depth = bvh.wide_depth;
+  const int32_t id = ctx->next_scene++;
+  ctx->scenes[id] = sg;
+  *scene_out = id;
+  return OR3_OK;
+}
+
+int or3_scene_release(or3_context *ctx, int32_t scene) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_scene(it->second);
+  ctx->scenes.erase(it);
+  return OR3_OK;
+}
+
+int or3_scene_get_info(or3_context *ctx, int32_t scene, or3_scene_info *out) {
+  if (!ctx || !out) return OR3_ERR_INVALID_ARGUMENT;
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  *out = it->second->info;
+  return OR3_OK;
+}
+
+int or3_stop(or3_context *ctx) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  ctx->stop.store(true);
+  return OR3_OK;
+}
+
+int or3_reset_stop(or3_context *ctx) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  ctx->stop.store(false);
+  return OR3_OK;
+}
+
+int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3_render_params *prm,
+               or3_frame_callback cb, void *user) {
+  if (!ctx || !cam || !prm) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  SceneGPU *sg = it->second;
+  if (cam->width == 0 || cam->height == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "empty image");
+  if ((uint64_t)cam->width * cam->height > (1ull << 28))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "image too large");
+  if (prm->supersamples < 1 || prm->supersamples > 256)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "supersamples must be in [1,256]");
+  if (prm->min_samples < 1 || prm->max_samples < prm->min_samples || prm->step_samples < 1)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sample schedule must satisfy 1 <= min <= max, step >= 1");
+  if (prm->output_layout != OR3_LAYOUT_REFERENCE && prm->output_layout != OR3_LAYOUT_COMPACT)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "unknown output layout");
+  cudaSetDevice(ctx->device);
+
+  const uint32_t W = cam->width, H = cam->height, ss = (uint32_t)prm->supersamples, ss2 = ss * ss;
+  const uint64_t npix = (uint64_t)W * H;
+  const uint64_t paths_per_sample = npix * ss2;
+  uint64_t wave = prm->wave_paths ? prm->wave_paths : (1ull << 22);
+  wave = std::max<uint64_t>(wave, ss2);
+  wave = std::min<uint64_t>(wave, 1ull << 30);
+  // Waves: whole samples of the full image when one fits, else row chunks of one sample.
+  uint64_t ns_per_wave = 1, npix_per_wave = npix;
+  if (paths_per_sample <= wave) {
+    ns_per_wave = wave / paths_per_sample;
+  } else {
+    npix_per_wave = std::max<uint64_t>(1, wave / ss2);
+  }
+  const uint64_t max_wave_paths = ns_per_wave * npix_per_wave * ss2;
+  const uint64_t rays = max_wave_paths * (sg->has_split ? 8 : 1);
+  int rc = ensure_queues(ctx, max_wave_paths, rays);
+  if (rc) return rc;
+  const size_t frame_doubles = (prm->output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * npix * 3;
+  if ((rc = ensure_pixels(ctx, npix, frame_doubles))) return rc;
+
+  RenderConst rcst{};
+  camera_basis(cam, rcst.cam);
+  rcst.W = W;
+  rcst.H = H;
+  rcst.ss = ss;
+  rcst.ss2 = ss2;
+  rcst.nee = prm->next_event_estimation;
+  rcst.rr_min_depth = prm->rr_min_depth;
+  rcst.max_depth = prm->max_depth;
+  rcst.seed_lo = (uint32_t)prm->seed;
+  rcst.seed_hi = (uint32_t)(prm->seed >> 32);
+
+  cudaStream_t st = ctx->stream;
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->pix_sum, 0, npix * 3 * sizeof(double), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->pix_sumsq, 0, npix * 3 * sizeof(double), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->frame_dev, 0, frame_doubles * sizeof(double), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->dstats, 0, 8 * sizeof(unsigned long long), st));
+
+  const Queues q = make_queues(ctx);
+  const int block = 256;
+  const int grid_ext = ctx->num_sms * ctx->occ_extend;
+  const int grid_sh = ctx->num_sms * ctx->occ_shade;
+  const int smem_nodes = (int)std::min<uint64_t>(256, sg->view.num_nodes);
+
+  or3_render_stats stats{};
+  ctx->moments_valid = false;
+  ctx->last_kept_paths = (prm->flags & OR3_FLAG_KEEP_PATHS) != 0;
+  auto wall0 = std::chrono::steady_clock::now();
+  int32_t prev = 0;
+  int passes = 0;
+  bool stopped = false;
+  for (int32_t next = prm->min_samples; next <= prm->max_samples; next += prm->step_samples) {
+    if (ctx->stop.load()) { stopped = true; break; }
+    OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+    // waves over [prev, next) samples
+    for (uint32_t s = (uint32_t)prev; s < (uint32_t)next && !stopped;) {
+      const uint32_t ns = (uint32_t)std::min<uint64_t>(ns_per_wave, (uint64_t)next - s);
+      for (uint64_t p0 = 0; p0 < npix && !stopped; p0 += npix_per_wave) {
+        const uint64_t np = std::min<uint64_t>(npix_per_wave, npix - p0);
+        Wave w{};
+        w.g_first = ((uint64_t)s * npix + p0) * ss2;
+        w.num_paths = (uint32_t)(ns * np * ss2);
+        w.pass_first = (uint32_t)prev;
+        w.pix0 = (uint32_t)p0;
+        w.npix = (uint32_t)np;
+        w.ns = ns;
+        launch_raygen(rcst, w, q, 0, 0, block, st);
+        int in = 0;
+        uint32_t count = w.num_paths;
+        for (int bounce = 0; count > 0; bounce++) {
+          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, st);
+          launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
+          launch_reset_count(q, in, st);
+          in ^= 1;
+          OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost, st));
+          OR3_CUDA(ctx, cudaStreamSynchronize(st));
+          count = ctx->host_counters[in];
+          if (ctx->host_counters[2]) break;
+          if (bounce > 100000) break;
+        }
+        launch_accumulate(q, w, ss2, ctx->pix_sum, ctx->pix_sumsq,
+                          (int)std::min<uint64_t>((np + 7) / 8, 152 * 64), block, st);
+        stats.waves++;
+        stats.camera_paths += w.num_paths;
+        ctx->last_wave_paths = w.num_paths;
+        if (ctx->host_counters[2]) break;
+      }
+      s += ns;
+      if (ctx->host_counters[2]) break;
+      if (ctx->stop.load() && s < (uint32_t)next) stopped = true;
+    }
+    OR3_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+    OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    if (ctx->host_counters[2]) {
+      const uint32_t bits = ctx->host_counters[2];
+      cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
+      cudaStreamSynchronize(st);
+      return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x (%s)", bits,
+                  (bits & kErrQueue) ? "ray queue capacity" : "traversal stack");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats.render_ms += ms;
+    if (stopped) break;
+    passes++;
+    // frame = running mean over `next` samples (PathTracer.cpp:169-170)
+    const double scale = 1.0 / ((double)next * ss2);
+    launch_frame(ctx->pix_sum, W, H, prm->output_layout, scale, ctx->frame_dev, st);
+    OR3_CUDA(ctx, cudaMemcpyAsync(ctx->frame_pinned, ctx->frame_dev, frame_doubles * sizeof(double),
+                                  cudaMemcpyDeviceToHost, st));
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    {
+      std::lock_guard<std::mutex> lk(ctx->frame_mu);
+      ctx->frame_host.assign(ctx->frame_pinned, ctx->frame_pinned + frame_doubles);
+      ctx->frame_samples = next;
+    }
+    ctx->last_count = (uint64_t)next * ss2;
+    prev = next;
+    if (cb) {
+      const double minutes =
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count() / 60.0;
+      cb(user, next, ctx->frame_pinned, (prm->output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * (size_t)W,
+         (size_t)H, minutes);
+    }
+  }
+  unsigned long long hs[8];
+  OR3_CUDA(ctx, cudaMemcpy(hs, ctx->dstats, sizeof(hs), cudaMemcpyDeviceToHost));
+  stats.extension_rays = hs[0];
+  stats.shadow_rays = hs[1];
+  stats.bounces = hs[2];
+  stats.samples = prev;
+  stats.passes = passes;
+  stats.upload_ms = sg->info.build_ms + sg->info.upload_ms;
+  ctx->last = stats;
+  ctx->last_W = W;
+  ctx->last_H = H;
+  ctx->moments_valid = !stopped;
+  return OR3_OK;
+}
+
+int or3_get_frame(or3_context *ctx, double *rgb, size_t capacity, int32_t *samples_out) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(ctx->frame_mu);
+  if (samples_out) *samples_out = ctx->frame_samples;
+  if (ctx->frame_host.empty()) return fail(ctx, OR3_ERR_NOT_FOUND, "no frame rendered yet");
+  if (!rgb || capacity < ctx->frame_host.size())
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "frame needs %zu doubles", ctx->frame_host.size());
+  std::memcpy(rgb, ctx->frame_host.data(), ctx->frame_host.size() * sizeof(double));
+  return OR3_OK;
+}
+
+int or3_get_stats(or3_context *ctx, or3_render_stats *out) {
+  if (!ctx || !out) return OR3_ERR_INVALID_ARGUMENT;
+  *out = ctx->last;
+  return OR3_OK;
+}
+
+int or3_get_moments(or3_context *ctx, double *sum, double *sumsq, size_t capacity, uint64_t *count_out) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  if (!ctx->moments_valid) return fail(ctx, OR3_ERR_NOT_FOUND, "no completed render");
+  const size_t n = (size_t)ctx->last_W * ctx->last_H * 3;
+  if (capacity < n) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "moments need %zu doubles", n);
+  cudaSetDevice(ctx->device);
+  double *tmp = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&tmp, 2 * n * sizeof(double)));
+  launch_moments(ctx->pix_sum, ctx->pix_sumsq, ctx->last_W, ctx->last_H, tmp, tmp + n, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && sum) e = cudaMemcpy(sum, tmp, n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && sumsq) e = cudaMemcpy(sumsq, tmp + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "moments: %s", cudaGetErrorString(e));
+  if (count_out) *count_out = ctx->last_count;
+  return OR3_OK;
+}
+
+int or3_get_path_radiance(or3_context *ctx, float *rgb, size_t capacity, uint64_t *paths_out) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  if (!ctx->last_kept_paths || ctx->last_wave_paths == 0)
+    return fail(ctx, OR3_ERR_NOT_FOUND, "render with OR3_FLAG_KEEP_PATHS first");
+  const size_t n = ctx->last_wave_paths;
+  if (paths_out) *paths_out = n;
+  if (!rgb) return OR3_OK;
+  if (capacity < 3 * n) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "path radiance needs %zu floats", 3 * n);
+  std::vector<float4> tmp(n);
+  OR3_CUDA(ctx, cudaMemcpy(tmp.data(), ctx->pathL, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; i++) {
+    rgb[3 * i] = tmp[i].x;
+    rgb[3 * i + 1] = tmp[i].y;
+    rgb[3 * i + 2] = tmp[i].z;
+  }
+  return OR3_OK;
+}
+
+int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const float *o, const float *d,
+                             int32_t *prim, float *t, float *normal, void *stream) {
+  if (!ctx || (n && (!o || !d || !prim || !t))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  if (n == 0) return OR3_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  launch_trace_closest(it->second->view, n, o, d, prim, t, normal, ctx->counters + 2, st);
+  OR3_CUDA(ctx, cudaGetLastError());
+  return OR3_OK;
+}
+
+int or3_trace_closest(or3_context *ctx, int32_t scene, size_t n, const float *o, const float *d, int32_t *prim,
+                      float *t, float *normal) {
+  if (!ctx || (n && (!o || !d || !prim || !t))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  if (ctx->scenes.find(scene) == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  if (n == 0) return OR3_OK;
+  cudaSetDevice(ctx->device);
+  char *buf = nullptr;
+  const size_t bytes = n * (3 + 3 + 1 + 1 + 3) * 4;
+  OR3_CUDA(ctx, cudaMalloc(&buf, bytes));
+  float *od = (float *)buf, *dd = od + 3 * n, *td = dd + 3 * n, *nd = td + n;
+  int32_t *pd = (int32_t *)(nd + 3 * n);
+  cudaStream_t st = ctx->stream;
+  cudaMemcpyAsync(od, o, 3 * n * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dd, d, 3 * n * 4, cudaMemcpyHostToDevice, st);
+  int rc = or3_trace_closest_device(ctx, scene, n, od, dd, pd, td, nd, st);
+  if (rc == OR3_OK) {
+    cudaMemcpyAsync(prim, pd, n * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(t, td, n * 4, cudaMemcpyDeviceToHost, st);
+    if (normal) cudaMemcpyAsync(normal, nd, 3 * n * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(ctx, OR3_ERR_CUDA, "trace: %s", cudaGetErrorString(e));
+    else if (ctx->host_counters[2]) rc = fail(ctx, OR3_ERR_DEVICE_REPORTED, "traversal stack overflow");
+  }
+  cudaFree(buf);
+  return rc;
+}
+
+int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *o, const float *d,
+                       const float *tmax, uint8_t *occ) {
+  if (!ctx || (n && (!o || !d || !tmax || !occ))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  if (n == 0) return OR3_OK;
+  cudaSetDevice(ctx->device);
+  char *buf = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&buf, n * 7 * 4 + n));
+  float *od = (float *)buf, *dd = od + 3 * n, *tm = dd + 3 * n;
+  uint8_t *oc = (uint8_t *)(tm + n);
+  cudaStream_t st = ctx->stream;
+  cudaMemcpyAsync(od, o, 3 * n * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dd, d, 3 * n * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(tm, tmax, n * 4, cudaMemcpyHostToDevice, st);
+  launch_trace_occluded(it->second->view, n, od, dd, tm, oc, ctx->counters + 2, st);
+  cudaMemcpyAsync(occ, oc, n, cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "occluded: %s", cudaGetErrorString(e));
+  return OR3_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,415 @@
+// or3_device.cuh -- device-side scene view, RNG, intersection and traversal.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "or3.h"
+#include "or3_common.h"
+
+namespace or3 {
+
+// Device view of one uploaded scene.
+struct DevScene {
+  const uint4 *nodes;          // WideNode[num_nodes] as 4 x uint4
+  const float4 *prims;         // 3 x float4 per record
+  const PrimInfo *info;        // per record
+  const TriShade *tri_shade;   // per record (triangles)
+  const PlaneRec *planes;      // not-in-BVH objects
+  const MaterialDev *materials;
+  const LayerDev *layers;
+  const float *env;            // RGB, env_w * env_h
+  const TextureDev *textures;
+  const float *texels;
+  // NEE light list (emissive triangles and spheres), CDF over power
+  const uint32_t *light_rec;   // record index per light
+  const float *light_cdf;      // inclusive CDF, last = 1
+  const float *light_pdf;      // selection probability per light
+  const uint32_t *rec_light;   // record -> light index (0xffffffff = none)
+  const float *env_marg_cdf;   // [env_h] inclusive marginal CDF over rows
+  const float *env_cond_cdf;   // [env_h * env_w] inclusive conditional CDF per row
+  const float *env_row_sum;    // [env_h] (for pdf)
+  uint32_t num_nodes, num_prims, num_planes, num_lights;
+  uint32_t env_w, env_h, num_textures, pad0;
+  float env_total;             // sum of luminance*sin(theta) weights (0 = none)
+  float env_select_prob;       // probability of sampling the environment in NEE
+  float bg[3];
+};
+
+// ---------------------------------------------------------------- math
+struct V3 {
+  float x, y, z;
+};
+OR3_HD V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+OR3_HD V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+OR3_HD V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+OR3_HD V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+OR3_HD V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+OR3_HD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+OR3_HD V3 cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ V3 normalize(V3 a) {
+  const float l = sqrtf(dot(a, a));
+  return v3(a.x / l, a.y / l, a.z / l);
+}
+
+// ---------------------------------------------------------------- RNG
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11), counter-based so a path's random numbers depend
+// only on (path, leaf, depth, call) and not on execution order.  Replaces the
+// reference's per-row xorshift stream (src/tools/Random.h:7-30), which cannot
+// be replayed in wavefront order.
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+// 24-bit uniform in [0, 1)
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// counter for bounce randoms of a path leaf
+__device__ __forceinline__ uint4 path_counter(uint64_t g, uint32_t leaf, uint32_t depth, uint32_t call) {
+  return make_uint4((uint32_t)g, (uint32_t)(g >> 32), (depth & 0xFFFFu) | (leaf << 16) | (call << 24), 0u);
+}
+
+// ---------------------------------------------------------------- hits
+constexpr uint32_t kMissRec = 0xFFFFFFFFu;
+constexpr uint32_t kPlaneBit = 0x80000000u;
+
+struct Hit {
+  float t;
+  uint32_t rec;  // record index, kPlaneBit|plane, or kMissRec
+  float u, v;    // barycentric rates (triangles)
+};
+
+// Reference triangle test, single-sided with det > EPS
+// (Polygon::CheckIntersection, src/renderer/Polygon.h:63-106), in FP32.
+__device__ __forceinline__ bool isect_triangle(const float4 a, const float4 b, const float4 c, V3 o, V3 d,
+                                               float tbest, float &t, float &ur, float &vr) {
+  const V3 v0 = v3(a.x, a.y, a.z);
+  const V3 e1 = v3(a.w, b.x, b.y);
+  const V3 e2 = v3(b.z, b.w, c.x);
+  const V3 P = cross(d, e2);
+  const float det = dot(P, e1);
+  if (!(det > kEps)) return false;
+  const V3 T = o - v0;
+  const float u = dot(P, T);
+  if (!(u >= 0.f && u <= det)) return false;
+  const V3 Q = cross(T, e1);
+  const float v = dot(Q, d);
+  if (!(v >= 0.f && u + v <= det)) return false;
+  const float tt = dot(Q, e2) / det;
+  if (!(tt >= kEps) || !(tt < tbest)) return false;
+  t = tt;
+  ur = u / det;
+  vr = v / det;
+  return true;
+}
+
+// Sphere test with the reference's root choice (Sphere::CheckIntersection,
+// src/renderer/Sphere.h:21-78): nearest root > EPS.  The discriminant is
+// formed from the ray-to-centre perpendicular and the near root from the
+// product of roots (Haines, Guenther, Akenine-Moller, "Precision Improvements
+// for Ray/Sphere Intersection", Ray Tracing Gems ch. 7), which keeps FP32
+// close to the reference's FP64 values.
+__device__ __forceinline__ bool isect_sphere(const float4 s, V3 o, V3 d, float tbest, float &t) {
+  const V3 cx = v3(s.x - o.x, s.y - o.y, s.z - o.z);
+  const float a = dot(d, d);
+  const float b = dot(d, cx);  // = v.(c - x)
+  const V3 l = cx - d * (b / a);
+  const float r2 = s.w * s.w;
+  const float D = r2 - dot(l, l);  // discriminant / a
+  if (D < 0.f) return false;
+  const float sq = sqrtf(a * D);
+  const float q = b + copysignf(sq, b);
+  const float cc = dot(cx, cx) - r2;
+  float t1, t2;  // far, near (reference t1 = b + sqrtD, t2 = b - sqrtD, scaled by 1/a)
+  if (q == 0.f) {
+    t1 = t2 = 0.f;
+  } else {
+    const float ra = q / a, rb = cc / q;
+    t1 = fmaxf(ra, rb);
+    t2 = fminf(ra, rb);
+  }
+  if (t1 <= kEps && t2 <= kEps) return false;
+  const float tt = t2 > kEps ? t2 : t1;
+  if (!(tt < tbest)) return false;
+  t = tt;
+  return true;
+}
+
+// AxisAlignedPlane (src/renderer/AxisAlignedPlane.h:38-64) and InfiniteFloor
+// (src/renderer/InfiniteFloor.h:19-37).
+__device__ __forceinline__ bool isect_plane(const PlaneRec &p, V3 o, V3 d, float tbest, float &t) {
+  float tt;
+  if (p.kind == kPrimFloor) {
+    if (fabsf(d.y) < kEps) return false;
+    tt = (p.offset - o.y) / d.y;
+  } else {
+    const float dd = p.axis == 0 ? d.z : p.axis == 1 ? d.y : d.x;
+    const float oo = p.axis == 0 ? o.z : p.axis == 1 ? o.y : o.x;
+    if (dd == 0.f) return false;
+    tt = (p.offset - oo) / dd;
+  }
+  if (!(tt >= kEps) || !(tt < tbest)) return false;
+  t = tt;
+  return true;
+}
+
+// byte i of w as an exact float (PRMT into a 2^23 mantissa + FADD)
+__device__ __forceinline__ float qbyte(uint32_t w, uint32_t i) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + i)) - 8388608.0f;
+}
+
+__device__ __forceinline__ float safe_inv(float x) {
+  return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x));
+}
+
+// Closest hit (ANY = false) or first hit (ANY = true) against the wide BVH
+// and the not-in-BVH list.  Replaces Scene::CheckIntersection
+// (src/scenes/Scene.cpp:51-85), BVH::CheckIntersection (src/renderer/BVH.cpp:19-88)
+// and QBVH::CheckIntersection (src/renderer/QBVH.cpp:30-144):
+//   * boxes are tested 4 at a time from one 64-byte node;
+//   * leaf children are intersected as soon as their box is hit;
+//   * internal children are visited nearest first, the others pushed with
+//     their entry distance and pruned on pop against the best hit;
+//   * a primitive replaces the best hit only if strictly closer, BVH first,
+//     then the not-in-BVH objects, as in the reference.
+// `nodes_smem`/`smem_nodes`: the first smem_nodes nodes may be read from
+// shared memory instead of global.
+template <bool ANY>
+__device__ __forceinline__ Hit trace(const DevScene &S, V3 o, V3 d, float tmax, uint32_t *err,
+                                     const uint4 *nodes_smem = nullptr, uint32_t smem_nodes = 0) {
+  Hit h;
+  h.t = tmax;
+  h.rec = kMissRec;
+  h.u = h.v = 0.f;
+  if (S.num_nodes > 0) {
+    const V3 inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    const V3 oi = v3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
+    // per axis: which byte word is the near plane
+    const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
+    uint32_t stack_node[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+      uint4 n0, n1, n2, n3;
+      if (node < smem_nodes) {
+        n0 = nodes_smem[4 * node + 0];
+        n1 = nodes_smem[4 * node + 1];
+        n2 = nodes_smem[4 * node + 2];
+        n3 = nodes_smem[4 * node + 3];
+      } else {
+        const uint4 *np = S.nodes + 4 * (size_t)node;
+        n0 = __ldg(np + 0);
+        n1 = __ldg(np + 1);
+        n2 = __ldg(np + 2);
+        n3 = __ldg(np + 3);
+      }
+      const uint32_t ew = n0.w;
+      const float sx = __uint_as_float((ew & 0xFFu) << 23);
+      const float sy = __uint_as_float(((ew >> 8) & 0xFFu) << 23);
+      const float sz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
+      const uint32_t imask = ew >> 24;
+      const float ax = sx * inv.x, ay = sy * inv.y, az = sz * inv.z;
+      const float bx = fmaf(__uint_as_float(n0.x), inv.x, oi.x);
+      const float by = fmaf(__uint_as_float(n0.y), inv.y, oi.y);
+      const float bz = fmaf(__uint_as_float(n0.z), inv.z, oi.z);
+      // byte words: lo x,y,z = n1.x,n1.y,n1.z ; hi x,y,z = n1.w,n2.x,n2.y
+      const uint32_t wnx = nx ? n1.w : n1.x, wfx = nx ? n1.x : n1.w;
+      const uint32_t wny = ny ? n2.x : n1.y, wfy = ny ? n1.y : n2.x;
+      const uint32_t wnz = nz ? n2.y : n1.z, wfz = nz ? n1.z : n2.y;
+      const uint32_t counts = n3.z;
+      const float tlimit = h.t * 1.0000010f;
+      float key[4];
+      uint32_t kid[4];
+      uint32_t leafmask = 0;
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const float tnx = fmaf(qbyte(wnx, i), ax, bx), tfx = fmaf(qbyte(wfx, i), ax, bx);
+        const float tny = fmaf(qbyte(wny, i), ay, by), tfy = fmaf(qbyte(wfy, i), ay, by);
+        const float tnz = fmaf(qbyte(wnz, i), az, bz), tfz = fmaf(qbyte(wfz, i), az, bz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+        const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
+        const bool internal = (imask >> i) & 1u;
+        const uint32_t cnt = (counts >> (8 * i)) & 0xFFu;
+        const bool hitbox = tn <= tf && tn <= tlimit;
+        const uint32_t ch = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
+        key[i] = (hitbox && internal) ? tn : kInf * 2.f;
+        kid[i] = ch;
+        if (hitbox && !internal && cnt != 0u) leafmask |= 1u << i;
+      }
+      // leaf children: triangles then spheres
+      while (leafmask) {
+        const uint32_t i = __ffs(leafmask) - 1;
+        leafmask &= leafmask - 1;
+        const uint32_t first = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
+        const uint32_t cnt = (counts >> (8 * i)) & 0xFFu;
+        const uint32_t ntri = cnt & 15u, nsph = cnt >> 4;
+        for (uint32_t k = 0; k < ntri; k++) {
+          const float4 *pr = S.prims + 3 * (size_t)(first + k);
+          const float4 a = __ldg(pr), b = __ldg(pr + 1), c = __ldg(pr + 2);
+          float t, u, v;
+          if (isect_triangle(a, b, c, o, d, h.t, t, u, v)) {
+            h.t = t;
+            h.rec = first + k;
+            h.u = u;
+            h.v = v;
+          }
+        }
+        for (uint32_t k = ntri; k < ntri + nsph; k++) {
+          const float4 a = __ldg(S.prims + 3 * (size_t)(first + k));
+          float t;
+          if (isect_sphere(a, o, d, h.t, t)) {
+            h.t = t;
+            h.rec = first + k;
+            h.u = h.v = 0.f;
+          }
+        }
+        if (ANY && h.rec != kMissRec) return h;
+      }
+      // nearest-first order of the internal children hit (sorting network)
+#define OR3_CSWAP(a, b)                                   \
+  if (key[b] < key[a]) {                                  \
+    const float tk = key[a]; key[a] = key[b]; key[b] = tk; \
+    const uint32_t tc = kid[a]; kid[a] = kid[b]; kid[b] = tc; \
+  }
+      OR3_CSWAP(0, 1) OR3_CSWAP(2, 3) OR3_CSWAP(0, 2) OR3_CSWAP(1, 3) OR3_CSWAP(1, 2)
+#undef OR3_CSWAP
+      const float inf2 = kInf * 2.f;
+      const float tl2 = h.t * 1.0000010f;
+      bool advanced = false;
+      if (key[0] < inf2 && key[0] <= tl2) {
+#pragma unroll
+        for (int j = 3; j >= 1; j--) {
+          if (key[j] < inf2 && key[j] <= tl2) {
+            if (sp < kStackSize) {
+              stack_node[sp] = kid[j];
+              stack_t[sp] = key[j];
+              sp++;
+            } else {
+              atomicOr(err, 1u);  // cannot happen with builder depth bound
+            }
+          }
+        }
+        node = kid[0];
+        advanced = true;
+      }
+      if (!advanced) {
+        bool found = false;
+        while (sp > 0) {
+          sp--;
+          if (stack_t[sp] <= h.t * 1.0000010f) {
+            node = stack_node[sp];
+            found = true;
+            break;
+          }
+        }
+        if (!found) break;
+      }
+    }
+  }
+  for (uint32_t p = 0; p < S.num_planes; p++) {
+    float t;
+    if (isect_plane(S.planes[p], o, d, h.t, t)) {
+      h.t = t;
+      h.rec = kPlaneBit | p;
+      h.u = h.v = 0.f;
+      if (ANY) return h;
+    }
+  }
+  return h;
+}
+
+// Surface data at a hit, as HitInformation reports it (normal not yet
+// oriented toward the ray, uv when a layer is textured).
+struct Surface {
+  V3 p;          // hit position orig + dir * t
+  V3 n;          // hit.normal
+  float uvx, uvy;
+  uint32_t layer_begin, layer_count, object_id, flags, kind;
+};
+
+__device__ __forceinline__ Surface surface_at(const DevScene &S, const Hit &h, V3 o, V3 d) {
+  Surface s;
+  s.p = o + d * h.t;
+  s.uvx = s.uvy = 0.f;
+  if (h.rec & kPlaneBit) {
+    const PlaneRec &pl = S.planes[h.rec & ~kPlaneBit];
+    s.layer_begin = pl.layer_begin;
+    s.layer_count = pl.layer_count;
+    s.object_id = pl.object_id;
+    s.flags = pl.flags;
+    s.kind = pl.kind;
+    if (pl.kind == kPrimFloor) {
+      s.n = v3(0.f, d.y < 0.f ? 1.f : -1.f, 0.f);
+    } else {
+      s.n = pl.axis == 0 ? v3(0, 0, pl.normal_sign) : pl.axis == 1 ? v3(0, pl.normal_sign, 0) : v3(pl.normal_sign, 0, 0);
+    }
+    return s;
+  }
+  const PrimInfo inf = S.info[h.rec];
+  s.layer_begin = inf.layer_begin;
+  s.layer_count = inf.layer_count;
+  s.object_id = inf.object_id;
+  s.kind = inf.kind_flags & 0xFFu;
+  s.flags = inf.kind_flags >> 8;
+  if (s.kind == kPrimTriangle) {
+    const float4 *ts = reinterpret_cast<const float4 *>(S.tri_shade + h.rec);
+    const float4 a = __ldg(ts), b = __ldg(ts + 1), c = __ldg(ts + 2), e = __ldg(ts + 3);
+    // n0=(a.xyz) dn1=(a.w,b.xy) dn2=(b.zw,c.x) uv0=(c.yz) duv1=(c.w,e.x) duv2=(e.yz)
+    s.n = normalize(v3(fmaf(a.w, h.u, fmaf(b.z, h.v, a.x)), fmaf(b.x, h.u, fmaf(b.w, h.v, a.y)),
+                       fmaf(b.y, h.u, fmaf(c.x, h.v, a.z))));
+    if (s.flags & kFlagTexturedUV) {
+      s.uvx = fmaf(c.w, h.u, fmaf(e.y, h.v, c.y));
+      s.uvy = fmaf(e.x, h.u, fmaf(e.z, h.v, c.z));
+    }
+  } else {
+    const float4 sp = __ldg(S.prims + 3 * (size_t)h.rec);
+    s.n = normalize(v3(s.p.x - sp.x, s.p.y - sp.y, s.p.z - sp.z));
+    if (s.flags & kFlagTexturedUV) {
+      // lat-long uv (src/renderer/Sphere.h:61-75)
+      float v = (asinf(fminf(fmaxf(s.n.y, -1.f), 1.f)) + kPi * 0.5f) / kPi;
+      while (v > 1.f) v -= 1.f;
+      while (v < 0.f) v += 1.f;
+      float u = (atan2f(s.n.z, s.n.x) + kPi) / (2.f * kPi);
+      while (u > 1.f) u -= 1.f;
+      while (u < 0.f) u += 1.f;
+      s.uvx = u;
+      s.uvy = 1.f - v;
+    }
+  }
+  return s;
+}
+
+// Image::GetPixelByUV (src/tools/Image.h:21-31): clamp, *0.99999, nearest.
+__device__ __forceinline__ V3 texel(const DevScene &S, int tex, float u, float v) {
+  const TextureDev td = S.textures[tex];
+  u = fminf(fmaxf(u, 0.f), 1.f) * 0.99999f;
+  v = fminf(fmaxf(v, 0.f), 1.f) * 0.99999f;
+  const uint32_t x = (uint32_t)(u * (float)td.width), y = (uint32_t)(v * (float)td.height);
+  const float *p = S.texels + td.offset + 3 * ((size_t)y * td.width + x);
+  return v3(p[0], p[1], p[2]);
+}
+
+// IBL::Sample(dir) (src/renderer/IBL.h:30-45): nearest texel of the equirect map.
+__device__ __forceinline__ V3 env_lookup(const DevScene &S, V3 d) {
+  if (S.env == nullptr) return v3(S.bg[0], S.bg[1], S.bg[2]);
+  const float theta = acosf(fminf(fmaxf(d.y, -1.f), 1.f));
+  const float rxz = sqrtf(d.x * d.x + d.z * d.z);
+  float phi = rxz > 0.f ? acosf(fminf(fmaxf(d.x / rxz, -1.f), 1.f)) : 0.f;
+  if (d.z < 0.f) phi = 2.f * kPi - phi;
+  const float u = phi / (2.f * kPi), v = theta / kPi;
+  const uint32_t x = (uint32_t)(u * (float)S.env_w) % S.env_w;
+  const uint32_t y = (uint32_t)(v * (float)S.env_h) % S.env_h;
+  const float *p = S.env + 3 * ((size_t)y * S.env_w + x);
+  return v3(p[0], p[1], p[2]);
+}
+
+}  // namespace or3

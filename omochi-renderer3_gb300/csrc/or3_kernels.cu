@@ -1,0 +1,446 @@
+// or3_kernels.cu -- the wavefront path-tracing kernels.
+//
+// One bounce of the reference's recursive estimator (PathTracer::Radiance ->
+// Radiance_internal -> Radiance_Lambert/Specular/Refraction,
+// src/renderer/PathTracer.cpp:180-591) becomes
+//     extend (closest hit for every queued ray)  ->  shade (one vertex of every path)
+// over structure-of-arrays queues in HBM; the recursion's return values become
+// a per-ray throughput and per-path radiance sums:
+//   Radiance(r, d) = E_d + w_d * Radiance(r', d+1)  ==>  L += beta * E_d;  beta *= w_d
+// The glass split at depth <= 2 (PathTracer.cpp:581-588) emits two child rays,
+// each with its own share of the throughput.
+#include <cuda_runtime.h>
+
+#include "or3_kernels.cuh"
+
+namespace or3 {
+
+namespace {
+
+__device__ __forceinline__ void add_radiance(float4 *L, V3 v) {
+  if (v.x != 0.f) atomicAdd(&L->x, v.x);
+  if (v.y != 0.f) atomicAdd(&L->y, v.y);
+  if (v.z != 0.f) atomicAdd(&L->z, v.z);
+}
+
+__device__ __forceinline__ V3 ld3(const float4 &f) { return v3(f.x, f.y, f.z); }
+
+// Camera::SampleRayForPixel (src/renderer/Camera.h:65-93) for sub-pixel
+// position (x + rx, y + ry), rx = (2 sx + 1) / (2 ss)
+// (PathTracer::scanPixelsOnYAndCastRays, src/renderer/PathTracer.cpp:156-161).
+__device__ __forceinline__ void camera_ray(const RenderConst &rc, uint32_t x, uint32_t y, uint32_t sx,
+                                           uint32_t sy, uint32_t lens_key, uint32_t pass_first, V3 &o,
+                                           V3 &d) {
+  const Camera32 &c = rc.cam;
+  const float inv2ss = 1.0f / (2.0f * (float)rc.ss);
+  const float rx = (2.0f * (float)sx + 1.0f) * inv2ss;
+  const float ry = (2.0f * (float)sy + 1.0f) * inv2ss;
+  const float fx = ((float)x + rx) / (float)rc.W - 0.5f;
+  const float fy = ((float)y + ry) / (float)rc.H - 0.5f;
+  const V3 target = v3(c.center[0] + c.xaxis[0] * fx + c.yaxis[0] * fy,
+                       c.center[1] + c.xaxis[1] * fx + c.yaxis[1] * fy,
+                       c.center[2] + c.xaxis[2] * fx + c.yaxis[2] * fy);
+  const V3 pos = v3(c.pos[0], c.pos[1], c.pos[2]);
+  d = normalize(target - pos);
+  o = pos;
+  if (c.aperture > 0.f) {
+    // CircleAperture::SampleOnePoint (src/renderer/Aperture.h:23-35): one lens
+    // sample per sub-pixel per pass, as the reference reuses its camera ray
+    // for every sample of a pass (PathTracer.cpp:161-167).
+    const uint4 r = philox(make_uint4(lens_key, pass_first, 0u, 1u), rc.seed_lo, rc.seed_hi);
+    float sn, cs;
+    sincospif(2.0f * u01(r.x), &sn, &cs);
+    const float rr = c.aperture * sqrtf(u01(r.y));
+    const float tf = c.focal / fabsf(d.z);
+    const V3 focus = pos + d * tf;
+    o = v3(pos.x + rr * cs, pos.y + rr * sn, pos.z);
+    d = normalize(focus - o);
+  }
+}
+
+__global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) q.counters[out] = w.num_paths;
+  if (i >= w.num_paths) return;
+  const uint64_t g = w.g_first + i;
+  const uint32_t sub = (uint32_t)(g % rc.ss2);
+  const uint64_t pg = g / rc.ss2;
+  const uint32_t pix = (uint32_t)(pg % ((uint64_t)rc.W * rc.H));
+  const uint32_t x = pix % rc.W, y = pix / rc.W;
+  V3 o, d;
+  camera_ray(rc, x, y, sub % rc.ss, sub / rc.ss, pix * rc.ss2 + sub, w.pass_first, o, d);
+  q.orig[out][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
+  q.dir[out][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+  q.beta[out][i] = make_float4(1.f, 1.f, 1.f, 0.f);
+  q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
+
+__global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
+  __shared__ uint4 snodes[kSmemNodes * 4];
+  const uint32_t n = q.counters[in];
+  const uint32_t ns = min((uint32_t)smem_nodes, S.num_nodes);
+  if (ns > 0) {
+    for (uint32_t k = threadIdx.x; k < ns * 4; k += blockDim.x) snodes[k] = S.nodes[k];
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+    if (n) atomicAdd(&q.stats[2], 1ull);
+  }
+  const float4 *qo = q.orig[in];
+  const float4 *qd = q.dir[in];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 ro = qo[i], rd = qd[i];
+    const Hit h = trace<false>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns);
+    q.hits[i] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+  }
+}
+
+struct NewRay {
+  V3 o, d, beta;
+  uint32_t meta;
+};
+
+// One path vertex: PathTracer::Radiance_internal (src/renderer/PathTracer.cpp:349-442)
+// and the three BSDFs (:445-591).  Writes 0, 1 or 2 continuation rays.
+__device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &rc, const Wave &w,
+                                         const Queues &q, int in, uint32_t i, NewRay &r0, NewRay &r1) {
+  const float4 ro = q.orig[in][i], rd = q.dir[in][i], rb = q.beta[in][i], hh = q.hits[i];
+  const V3 o = ld3(ro), d = ld3(rd);
+  V3 beta = ld3(rb);
+  const uint32_t path = __float_as_uint(ro.w);
+  const uint32_t meta = __float_as_uint(rd.w);
+  const uint32_t depth = meta & 0xFFFFu;
+  const uint32_t leaf = (meta >> 16) & 0xFFu;
+  float4 *L = q.pathL + path;
+  Hit h;
+  h.t = hh.x;
+  h.rec = __float_as_uint(hh.y);
+  h.u = hh.z;
+  h.v = hh.w;
+  if (h.rec == kMissRec) {
+    // miss: IBL::Sample(ray.dir) or Scene::Background() (PathTracer.cpp:357-364)
+    add_radiance(L, beta * env_lookup(S, d));
+    return 0;
+  }
+  const Surface s = surface_at(S, h, o, d);
+  // normal oriented toward the incoming ray (PathTracer.cpp:188-190)
+  const V3 nl = dot(s.n, d) < 0.f ? s.n : s.n * -1.f;
+  const uint4 rn = philox(path_counter(w.g_first + path, leaf, depth, 0u), rc.seed_lo, rc.seed_hi);
+
+  // material layer roulette (PathTracer.cpp:370-382)
+  float val = u01(rn.x);
+  uint32_t sel = s.layer_count - 1;
+  for (uint32_t k = 0; k < s.layer_count; k++) {
+    const float rate = S.layers[s.layer_begin + k].rate;
+    if (val <= rate) {
+      sel = k;
+      break;
+    }
+    val -= rate;
+  }
+  const MaterialDev &m = S.materials[S.layers[s.layer_begin + sel].material];
+  V3 col = v3(m.color[0], m.color[1], m.color[2]);
+  if (m.texture >= 0) col = col * texel(S, m.texture, s.uvx, s.uvy);  // GetTexturedColor (:327-346)
+
+  // emission is counted at every vertex when NEE is off, at the eye vertex
+  // only when NEE is on (PathTracer.cpp:404-411, :433-439)
+  if (m.emissive && (depth == 0 || !rc.nee))
+    add_radiance(L, beta * v3(m.emission[0], m.emission[1], m.emission[2]));
+
+  // Russian roulette (PathTracer.cpp:398-416)
+  float prr = fmaxf(col.x, fmaxf(col.y, col.z));
+  if (depth > 64u) prr *= exp2f(-(float)(depth - 64u));
+  if ((int)depth > rc.rr_min_depth) {
+    if (u01(rn.y) >= prr) return 0;
+  } else {
+    prr = 1.0f;
+  }
+  // hard depth cut (not in the reference): rays at depth >= max_depth are not traced
+  if (rc.max_depth > 0 && (int)depth + 1 >= rc.max_depth) return 0;
+
+  const uint32_t nmeta = (depth + 1u) | (leaf << 16);
+  r0.o = s.p;
+  r0.meta = nmeta;
+  switch (m.type) {
+    case OR3_LAMBERT: {
+      // Radiance_Lambert (PathTracer.cpp:445-500).  An emitter does not
+      // continue.  The tangent vectors are the reference's unnormalised
+      // cross products (:461-469), so the sampled density matches its
+      // estimator exactly, including for normals off the coordinate axes.
+      if (m.emissive) return 0;
+      const V3 ww = nl;
+      const V3 uu = fabsf(ww.x) > kEps ? cross(v3(0.f, 1.f, 0.f), ww) : cross(v3(1.f, 0.f, 0.f), ww);
+      const V3 vv = cross(ww, uu);
+      float sn, cs;
+      sincospif(2.0f * u01(rn.z), &sn, &cs);
+      const float u2 = u01(rn.w);
+      const float r2 = sqrtf(u2), r3 = sqrtf(1.0f - u2);
+      r0.d = normalize(uu * (r3 * cs) + vv * (r3 * sn) + ww * r2);
+      r0.beta = beta * col * (1.0f / prr);
+      return 1;
+    }
+    case OR3_SPECULAR: {
+      // Radiance_Specular (PathTracer.cpp:503-520)
+      r0.d = normalize(d - nl * (2.0f * dot(d, nl)));
+      r0.beta = beta * col * (1.0f / prr);
+      return 1;
+    }
+    case OR3_REFRACTION: {
+      // Radiance_Refraction (PathTracer.cpp:523-591)
+      const bool into = dot(s.n, nl) > 0.f;
+      const V3 refl = normalize(d - nl * (2.0f * dot(d, nl)));
+      const float nobj = m.ior;
+      const float nratio = into ? 1.0f / nobj : nobj;
+      const float dd = dot(d, nl);
+      const float cos2t = 1.0f - nratio * nratio * (1.0f - dd * dd);
+      if (cos2t < 0.f) {
+        // total internal reflection: weight uses material.color (:543-548)
+        r0.d = refl;
+        r0.beta = beta * v3(m.color[0], m.color[1], m.color[2]) * (1.0f / prr);
+        return 1;
+      }
+      const V3 refr = normalize(d * nratio - nl * (dd * nratio + sqrtf(cos2t)));
+      const float F0 = (nobj - 1.0f) * (nobj - 1.0f) / ((nobj + 1.0f) * (nobj + 1.0f));
+      const float c = 1.0f - (into ? -dd : -dot(refr, nl));
+      const float c2 = c * c;
+      const float Fr = F0 + (1.0f - F0) * c2 * c2 * c;
+      const float Tr = (1.0f - Fr) * nratio * nratio;
+      if (depth > 2u) {
+        const uint4 rn2 = philox(path_counter(w.g_first + path, leaf, depth, 1u), rc.seed_lo, rc.seed_hi);
+        const float pr = 0.1f + 0.8f * Fr;
+        if (u01(rn2.x) < pr) {
+          r0.d = refl;
+          r0.beta = beta * col * (Fr / (prr * pr));
+        } else {
+          r0.d = refr;
+          r0.beta = beta * col * (Tr / (prr * (1.0f - pr)));
+        }
+        return 1;
+      }
+      // depth <= 2: trace both, each child with its own leaf bit
+      r0.d = refl;
+      r0.beta = beta * col * (Fr / prr);
+      r1.o = s.p;
+      r1.d = refr;
+      r1.beta = beta * col * (Tr / prr);
+      r1.meta = (depth + 1u) | ((leaf | (1u << depth)) << 16);
+      return 2;
+    }
+    default: {
+      // Phong lobe about the mirror direction (not in the reference):
+      // pdf = (n+1)/(2 pi) cos^n(a), brdf = rho (n+2)/(2 pi) cos^n(a),
+      // weight = rho (n+2)/(n+1) cos(theta).
+      const V3 r = normalize(d - nl * (2.0f * dot(d, nl)));
+      const float e = m.phong_exponent;
+      const float ca = powf(u01(rn.z), 1.0f / (e + 1.0f));
+      const float sa = sqrtf(fmaxf(0.f, 1.0f - ca * ca));
+      float sn, cs;
+      sincospif(2.0f * u01(rn.w), &sn, &cs);
+      // orthonormal basis about r (Duff et al., "Building an Orthonormal Basis, Revisited", JCGT 2017)
+      const float sg = copysignf(1.0f, r.z);
+      const float aa = -1.0f / (sg + r.z);
+      const float bb = r.x * r.y * aa;
+      const V3 t1 = v3(1.0f + sg * r.x * r.x * aa, sg * bb, -sg * r.x);
+      const V3 t2 = v3(bb, sg + r.y * r.y * aa, -r.y);
+      const V3 wi = normalize(t1 * (sa * cs) + t2 * (sa * sn) + r * ca);
+      const float cosn = dot(wi, nl);
+      if (cosn <= 0.f) return 0;
+      r0.d = wi;
+      r0.beta = beta * col * ((e + 2.0f) / (e + 1.0f) * cosn / prr);
+      return 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_shade(DevScene S, RenderConst rc, Wave w, Queues q, int in) {
+  const uint32_t n = q.counters[in];
+  const int out = in ^ 1;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    NewRay r0, r1;
+    int cnt = 0;
+    if (i < n) cnt = shade_one(S, rc, w, q, in, i, r0, r1);
+    // warp-aggregated append to the output queue
+    int incl = cnt;
+#pragma unroll
+    for (int ofs = 1; ofs < 32; ofs <<= 1) {
+      const int v = __shfl_up_sync(0xFFFFFFFFu, incl, ofs);
+      if ((int)lane >= ofs) incl += v;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t wbase = 0;
+    if (lane == 31 && total > 0) wbase = atomicAdd(&q.counters[out], (uint32_t)total);
+    wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+    uint32_t pos = wbase + (uint32_t)(incl - cnt);
+    const uint32_t pathbits = cnt ? __float_as_uint(q.orig[in][i].w) : 0u;
+    for (int k = 0; k < cnt; k++, pos++) {
+      const NewRay &r = k == 0 ? r0 : r1;
+      if (pos >= q.capacity) {
+        atomicOr(&q.counters[2], kErrQueue);
+        continue;
+      }
+      q.orig[out][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
+      q.dir[out][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
+      q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, 0.f);
+    }
+  }
+}
+
+__global__ void k_reset_count(uint32_t *counters, int which) { counters[which] = 0; }
+
+// Per-pixel sums of the wave's path radiance: one warp per pixel, lanes over
+// the pixel's samples (coalesced), FP32 partials added into FP64 sums.
+__global__ void k_accumulate(Queues q, Wave w, uint32_t ss2, double *sum, double *sumsq) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t per = w.ns * ss2;
+  for (uint32_t p = warp; p < w.npix; p += nwarps) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f;
+    for (uint32_t j = lane; j < per; j += 32u) {
+      const uint32_t sl = j / ss2, k = j - sl * ss2;
+      const float4 L = q.pathL[((size_t)sl * w.npix + p) * ss2 + k];
+      s0 += L.x; s1 += L.y; s2 += L.z;
+      q0 += L.x * L.x; q1 += L.y * L.y; q2 += L.z * L.z;
+    }
+#pragma unroll
+    for (int ofs = 16; ofs > 0; ofs >>= 1) {
+      s0 += __shfl_xor_sync(0xFFFFFFFFu, s0, ofs);
+      s1 += __shfl_xor_sync(0xFFFFFFFFu, s1, ofs);
+      s2 += __shfl_xor_sync(0xFFFFFFFFu, s2, ofs);
+      q0 += __shfl_xor_sync(0xFFFFFFFFu, q0, ofs);
+      q1 += __shfl_xor_sync(0xFFFFFFFFu, q1, ofs);
+      q2 += __shfl_xor_sync(0xFFFFFFFFu, q2, ofs);
+    }
+    if (lane == 0) {
+      const size_t px = (size_t)(w.pix0 + p);
+      sum[3 * px] += s0; sum[3 * px + 1] += s1; sum[3 * px + 2] += s2;
+      sumsq[3 * px] += q0; sumsq[3 * px + 1] += q1; sumsq[3 * px + 2] += q2;
+    }
+  }
+}
+
+// Frame in the reference's layout: ScreenPixels::ScreenViewport::calcIndex
+// (src/renderer/ScreenPixels.cpp:50-65) flips y, the image is viewport 0 of a
+// 2 x 1 grid (PathTracer.cpp:63).  The right viewport is cleared by the host.
+__global__ void k_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= W * H) return;
+  const uint32_t x = p % W, y = p / W;
+  const uint32_t rowW = layout == 0 ? 2 * W : W;
+  const size_t o = ((size_t)(H - 1 - y) * rowW + x) * 3;
+  out[o] = sum[3 * (size_t)p] * scale;
+  out[o + 1] = sum[3 * (size_t)p + 1] * scale;
+  out[o + 2] = sum[3 * (size_t)p + 2] * scale;
+}
+
+__global__ void k_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t H, double *so,
+                          double *qo) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= W * H) return;
+  const uint32_t x = p % W, y = p / W;
+  const size_t o = ((size_t)(H - 1 - y) * W + x) * 3;
+  for (int c = 0; c < 3; c++) {
+    if (so) so[o + c] = sum[3 * (size_t)p + c];
+    if (qo) qo[o + c] = sumsq[3 * (size_t)p + c];
+  }
+}
+
+__global__ void k_trace_closest(DevScene S, size_t n, const float *orig, const float *dir, int32_t *prim,
+                                float *tout, float *nout, uint32_t *err) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const V3 o = v3(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
+    const V3 d = v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+    const Hit h = trace<false>(S, o, d, kInf, err);
+    if (h.rec == kMissRec) {
+      prim[i] = -1;
+      tout[i] = kInf;
+      if (nout) nout[3 * i] = nout[3 * i + 1] = nout[3 * i + 2] = 0.f;
+    } else {
+      const Surface s = surface_at(S, h, o, d);
+      prim[i] = (int32_t)s.object_id;
+      tout[i] = h.t;
+      if (nout) {
+        nout[3 * i] = s.n.x;
+        nout[3 * i + 1] = s.n.y;
+        nout[3 * i + 2] = s.n.z;
+      }
+    }
+  }
+}
+
+__global__ void k_trace_occluded(DevScene S, size_t n, const float *orig, const float *dir, const float *tmax,
+                                 uint8_t *occ, uint32_t *err) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const V3 o = v3(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
+    const V3 d = v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+    const Hit h = trace<true>(S, o, d, tmax[i], err);
+    occ[i] = h.rec != kMissRec ? 1 : 0;
+  }
+}
+
+int grid_for(size_t n, int block) {
+  size_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > 152 * 64) g = 152 * 64;
+  return (int)g;
+}
+
+}  // namespace
+
+void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int out, int grid, int block,
+                   cudaStream_t st) {
+  (void)grid;
+  const int g = (int)((w.num_paths + block - 1) / block);
+  k_raygen<<<g > 0 ? g : 1, block, 0, st>>>(rc, w, q, out);
+}
+
+void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes,
+                   cudaStream_t st) {
+  k_extend<<<grid, block, 0, st>>>(S, q, in, smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes);
+}
+
+void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
+                  int grid, int block, cudaStream_t st) {
+  k_shade<<<grid, block, 0, st>>>(S, rc, w, q, in);
+}
+
+void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
+  k_reset_count<<<1, 1, 0, st>>>(q.counters, which);
+}
+
+void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
+                       int block, cudaStream_t st) {
+  k_accumulate<<<grid, block, 0, st>>>(q, w, ss2, sum, sumsq);
+}
+
+void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,
+                  cudaStream_t st) {
+  const uint32_t n = W * H;
+  k_frame<<<(n + 255) / 256, 256, 0, st>>>(sum, W, H, layout, scale, out);
+}
+
+void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t H, double *so, double *qo,
+                    cudaStream_t st) {
+  const uint32_t n = W * H;
+  k_moments<<<(n + 255) / 256, 256, 0, st>>>(sum, sumsq, W, H, so, qo);
+}
+
+void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const float *dir, int32_t *prim,
+                          float *t, float *normal, uint32_t *err, cudaStream_t st) {
+  k_trace_closest<<<grid_for(n, 128), 128, 0, st>>>(S, n, orig, dir, prim, t, normal, err);
+}
+
+void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
+                           const float *tmax, uint8_t *occ, uint32_t *err, cudaStream_t st) {
+  k_trace_occluded<<<grid_for(n, 128), 128, 0, st>>>(S, n, orig, dir, tmax, occ, err);
+}
+
+const void *kernel_extend_ptr() { return (const void *)k_extend; }
+const void *kernel_shade_ptr() { return (const void *)k_shade; }
+
+}  // namespace or3

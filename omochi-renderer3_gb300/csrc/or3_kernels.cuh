@@ -1,0 +1,86 @@
+// or3_kernels.cuh -- launch interface between the host runtime and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "or3_device.cuh"
+
+namespace or3 {
+
+// Camera basis (Camera::Camera, src/renderer/Camera.h:12-43), built in double on
+// the host and used in FP32 on the device.
+struct Camera32 {
+  float pos[3];
+  float center[3];
+  float xaxis[3];  // scaled by the screen width in world units
+  float yaxis[3];  // scaled by the screen height in world units
+  float focal;
+  float aperture;  // 0 = pinhole
+};
+
+struct RenderConst {
+  Camera32 cam;
+  uint32_t W, H, ss, ss2;
+  int32_t nee, rr_min_depth, max_depth, pad;
+  uint32_t seed_lo, seed_hi;
+};
+
+// One wave = a contiguous range of camera paths g in [g_first, g_first + num_paths)
+// with g = ((s * H + y) * W + x) * ss2 + sub.  Waves never straddle passes.
+struct Wave {
+  uint64_t g_first;
+  uint32_t num_paths;
+  uint32_t pass_first;  // first sample index of the pass (lens sample key)
+  uint32_t pix0, npix;  // pixel range touched (camera order y*W+x)
+  uint32_t ns;          // samples per pixel in the wave
+  uint32_t pad;
+};
+
+// Ray queues in HBM (structure of arrays, ping-pong).
+//   orig: (o.xyz, path index in wave)   dir: (d.xyz, depth | leaf << 16)
+//   beta: (throughput.xyz, -)           hits: (t, record, u, v)
+struct Queues {
+  float4 *orig[2];
+  float4 *dir[2];
+  float4 *beta[2];
+  float4 *hits;
+  float4 *pathL;  // per camera path radiance of the wave
+  uint32_t *counters;         // [0],[1] queue lengths, [2] error bits
+  unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] bounces
+  uint32_t capacity;          // entries per queue
+  uint32_t pad;
+};
+
+constexpr uint32_t kErrStack = 1u;
+constexpr uint32_t kErrQueue = 2u;
+
+struct LaunchCfg {
+  int grid_extend, grid_shade, grid_raygen, grid_accum;
+  int block;
+};
+
+// host launchers (or3_kernels.cu)
+void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int out, int grid, int block,
+                   cudaStream_t st);
+void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes,
+                   cudaStream_t st);
+void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
+                  int grid, int block, cudaStream_t st);
+void launch_reset_count(const Queues &q, int which, cudaStream_t st);
+void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
+                       int block, cudaStream_t st);
+void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,
+                  cudaStream_t st);
+void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t H, double *sum_out,
+                    double *sumsq_out, cudaStream_t st);
+void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const float *dir, int32_t *prim,
+                          float *t, float *normal, uint32_t *err, cudaStream_t st);
+void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
+                           const float *tmax, uint8_t *occ, uint32_t *err, cudaStream_t st);
+
+// kernel handles for occupancy queries
+const void *kernel_extend_ptr();
+const void *kernel_shade_ptr();
+
+}  // namespace or3

@@ -1,0 +1,228 @@
+"""Python host mirror of the reference's render interface over the C ABI.
+
+`GpuPathTracer` has the reference PathTracer's constructor arguments and
+methods (src/renderer/PathTracer.h:18-88, src/renderer/Renderer.h:10-23):
+RenderScene, GetResult, GetCurrentSampleCount, GetCurrentRenderingInfo,
+StopRendering, EnableNextEventEstimation, SetMaxThreadCount.  `Context` is a
+thin owner of an or3_context; every call goes to libor3.so (CUDA) and errors
+surface as `Or3Error` with the library's message.
+"""
+import ctypes
+import threading
+
+import numpy as np
+
+from . import abi
+
+
+class Or3Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("or3 error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Context:
+    def __init__(self, device=0):
+        self.lib = abi.load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.or3_context_create(device, ctypes.byref(h))
+        if rc != abi.OR3_OK:
+            raise Or3Error(rc, "cannot create a context on CUDA device %d" % device)
+        self.h = h
+        self._keep = {}
+
+    def _check(self, rc):
+        if rc != abi.OR3_OK:
+            raise Or3Error(rc, self.lib.or3_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if self.h:
+            self.lib.or3_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- scenes
+    def upload(self, scene_desc):
+        d, keep = scene_desc.to_c()
+        sid = ctypes.c_int32()
+        self._check(self.lib.or3_scene_upload(self.h, ctypes.byref(d), ctypes.byref(sid)))
+        return sid.value
+
+    def release(self, scene):
+        self._check(self.lib.or3_scene_release(self.h, scene))
+
+    def scene_info(self, scene):
+        info = abi.SceneInfoC()
+        self._check(self.lib.or3_scene_get_info(self.h, scene, ctypes.byref(info)))
+        return {k: getattr(info, k) for k, _ in abi.SceneInfoC._fields_}
+
+    # ---- render
+    def render(self, scene, camera, *, supersamples=1, min_samples=1, max_samples=1, step_samples=1,
+               next_event_estimation=False, rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE,
+               seed=0, wave_paths=0, flags=0, callback=None):
+        cam = camera.to_c()
+        p = abi.RenderParamsC()
+        p.min_samples, p.max_samples, p.step_samples = min_samples, max_samples, step_samples
+        p.supersamples = supersamples
+        p.next_event_estimation = 1 if next_event_estimation else 0
+        p.rr_min_depth, p.max_depth = rr_min_depth, max_depth
+        p.output_layout = layout
+        p.seed, p.wave_paths, p.flags = seed, wave_paths, flags
+        if callback is not None:
+            def _cb(user, samples, rgb, w, h, minutes):
+                img = np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy()
+                callback(samples, img, w, h, minutes)
+            cb = abi.FRAME_CB(_cb)
+        else:
+            cb = abi.FRAME_CB()
+        self._check(self.lib.or3_render(self.h, scene, ctypes.byref(cam), ctypes.byref(p), cb, None))
+        return self.stats()
+
+    def stop(self):
+        self._check(self.lib.or3_stop(self.h))
+
+    def reset_stop(self):
+        self._check(self.lib.or3_reset_stop(self.h))
+
+    def stats(self):
+        s = abi.RenderStatsC()
+        self._check(self.lib.or3_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.RenderStatsC._fields_}
+
+    def frame(self, width, height, layout=abi.OR3_LAYOUT_REFERENCE):
+        w = width * (2 if layout == abi.OR3_LAYOUT_REFERENCE else 1)
+        out = np.zeros((height, w, 3), np.float64)
+        s = ctypes.c_int32()
+        self._check(self.lib.or3_get_frame(self.h, out.ctypes.data_as(abi.f64p), out.size, ctypes.byref(s)))
+        return out, s.value
+
+    def moments(self, width, height):
+        s = np.zeros((height, width, 3), np.float64)
+        q = np.zeros_like(s)
+        n = ctypes.c_uint64()
+        self._check(self.lib.or3_get_moments(self.h, s.ctypes.data_as(abi.f64p), q.ctypes.data_as(abi.f64p),
+                                             s.size, ctypes.byref(n)))
+        return s, q, n.value
+
+    def path_radiance(self):
+        n = ctypes.c_uint64()
+        self._check(self.lib.or3_get_path_radiance(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 3), np.float32)
+        self._check(self.lib.or3_get_path_radiance(self.h, out.ctypes.data_as(abi.f32p), out.size, ctypes.byref(n)))
+        return out
+
+    # ---- ray queries
+    def trace_closest(self, scene, origins, dirs):
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        n = o.shape[0]
+        prim = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        self._check(self.lib.or3_trace_closest(self.h, scene, n, o.ctypes.data_as(abi.f32p),
+                                               d.ctypes.data_as(abi.f32p),
+                                               prim.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                               t.ctypes.data_as(abi.f32p), nrm.ctypes.data_as(abi.f32p)))
+        return prim, t, nrm
+
+    def trace_occluded(self, scene, origins, dirs, tmax):
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        tm = np.ascontiguousarray(tmax, np.float32)
+        occ = np.zeros(o.shape[0], np.uint8)
+        self._check(self.lib.or3_trace_occluded(self.h, scene, o.shape[0], o.ctypes.data_as(abi.f32p),
+                                                d.ctypes.data_as(abi.f32p), tm.ctypes.data_as(abi.f32p),
+                                                occ.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return occ.astype(bool)
+
+
+class ScreenPixels:
+    """Result view with the reference ScreenPixels accessors (src/renderer/ScreenPixels.hpp:20-71)."""
+
+    def __init__(self, pixels):
+        self._px = pixels
+
+    def GetScreen(self):
+        return self._px
+
+    def CalcScreenWidth(self):
+        return self._px.shape[1]
+
+    def CalcScreenHeight(self):
+        return self._px.shape[0]
+
+
+class GpuPathTracer:
+    """Drop-in for PathTracer(camera, min, max, step, supersamples, callback)."""
+
+    def __init__(self, camera, min_samples, max_samples=None, step=1, supersamples=1, callback=None, device=0,
+                 context=None):
+        if max_samples is None:  # PathTracer(camera, samples, supersamples) form
+            max_samples = min_samples
+        self.camera = camera
+        self.min_samples, self.max_samples, self.step = min_samples, max_samples, step
+        self.supersamples = supersamples
+        self.callback = callback
+        self.ctx = context or Context(device)
+        self._nee = False
+        self._threads = 1
+        self._current = 0
+        self._result = None
+        self._lock = threading.Lock()
+        self.rr_min_depth = 5   # reference MinDepth (src/renderer/PathTracer.cpp:177)
+        self.max_depth = 0      # reference: no hard depth limit
+        self.seed = 0
+        self._scene_cache = {}
+
+    def EnableNextEventEstimation(self, enable=True):
+        self._nee = bool(enable)
+
+    def SetMaxThreadCount(self, count):
+        # host threads do not apply to the GPU path; kept for interface parity
+        self._threads = 1 if count == 0 else int(count)
+
+    def RenderScene(self, scene_desc):
+        key = id(scene_desc)
+        if key not in self._scene_cache:
+            self._scene_cache[key] = self.ctx.upload(scene_desc)
+        sid = self._scene_cache[key]
+
+        def on_frame(samples, img, w, h, minutes):
+            with self._lock:
+                self._current = samples
+                self._result = ScreenPixels(img)
+            if self.callback:
+                self.callback(samples, img, w, h, minutes)
+
+        self.ctx.render(sid, self.camera, supersamples=self.supersamples, min_samples=self.min_samples,
+                        max_samples=self.max_samples, step_samples=self.step,
+                        next_event_estimation=self._nee, rr_min_depth=self.rr_min_depth,
+                        max_depth=self.max_depth, seed=self.seed, callback=on_frame)
+
+    def GetResult(self):
+        with self._lock:
+            return self._result
+
+    def GetCurrentSampleCount(self):
+        return self._current
+
+    def GetCurrentRenderingInfo(self):
+        s = self.ctx.stats()
+        return ("(width, height) = (%d, %d)\nsamples / pixel = %dx(%dx%d)\npaths = %d, extension rays = %d\n"
+                % (self.camera.width, self.camera.height, s["samples"], self.supersamples, self.supersamples,
+                   s["camera_paths"], s["extension_rays"]))
+
+    def StopRendering(self):
+        self.ctx.stop()

@@ -1,0 +1,228 @@
+"""Seeded synthetic workloads (no public dataset is involved).
+
+  cornell_box()           10-triangle Cornell box, 20x20 area light (emission 12),
+                          mirror and glass spheres r=16.5; 256x256, ss=8 (64 spp)
+  icosphere_in_box()      level-6 displaced icosphere (81,920 triangles, radius 25,
+                          0.1 * fBm of 4 octaves), Lambert 0.8 with a Phong lobe of
+                          exponent 64 on half the faces, in the Cornell box;
+                          1024x768, ss=16 (256 spp), max depth 10
+  terrain_ibl()           1024x512-cell heightfield (1,048,576 triangles) with
+                          fBm heights in [0, 50], 64 glass spheres, 2048x1024
+                          float sky (gradient + 0.5 degree sun of 1e4 + log-normal
+                          background); 1920x1080, ss=32 (1024 spp), max depth 12
+  reference_cornell()     the reference's own built-in CornellBoxScene
+                          (src/scenes/CornellBoxScene.cpp:10-36): axis floors,
+                          a two-layer sphere, a SphereLight
+Each returns (SceneDesc, Camera, render settings dict).
+"""
+import math
+
+import numpy as np
+
+from . import abi
+from .scene import Camera, SceneDesc, fbm3, icosphere, quad, vertex_normals
+
+
+def _box_walls(sd, white, red, blue):
+    L = 100.0
+    walls = [
+        ([[0, 0, 0], [L, 0, 0], [L, 0, L], [0, 0, L]], (0, 1, 0), white),      # floor
+        ([[0, L, 0], [L, L, 0], [L, L, L], [0, L, L]], (0, -1, 0), white),     # ceiling
+        ([[0, 0, 0], [L, 0, 0], [L, L, 0], [0, L, 0]], (0, 0, 1), white),      # back
+        ([[0, 0, 0], [0, L, 0], [0, L, L], [0, 0, L]], (1, 0, 0), red),        # left
+        ([[L, 0, 0], [L, L, 0], [L, L, L], [L, 0, L]], (-1, 0, 0), blue),      # right
+    ]
+    for corners, facing, mat in walls:
+        sd.add_triangles(quad(corners, facing), sd.layers(mat))
+
+
+def _box_light(sd, light):
+    y = 99.9
+    sd.add_triangles(quad([[40, y, 40], [60, y, 40], [60, y, 60], [40, y, 60]], (0, -1, 0)), sd.layers(light))
+
+
+def cornell_camera(width, height):
+    # pinhole at (50, 50, 250) looking down -z with a 40 degree vertical field of view
+    return Camera(width, height, (50.0, 50.0, 250.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0),
+                  2.0 * 40.0 * math.tan(math.radians(20.0)), 40.0, 300.0, 0.0)
+
+
+def cornell_box(width=256, height=256):
+    sd = SceneDesc()
+    white = sd.material(abi.OR3_LAMBERT, (0.75, 0.75, 0.75))
+    red = sd.material(abi.OR3_LAMBERT, (0.75, 0.25, 0.25))
+    blue = sd.material(abi.OR3_LAMBERT, (0.25, 0.25, 0.75))
+    light = sd.material(abi.OR3_LAMBERT, (0.0, 0.0, 0.0), emission=(12.0, 12.0, 12.0))
+    mirror = sd.material(abi.OR3_SPECULAR, (0.99, 0.99, 0.99))
+    glass = sd.material(abi.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    _box_walls(sd, white, red, blue)
+    _box_light(sd, light)
+    sd.add_sphere((30.0, 16.5, 40.0), 16.5, sd.layers(mirror))
+    sd.add_sphere((70.0, 16.5, 60.0), 16.5, sd.layers(glass))
+    settings = dict(supersamples=8, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=3, max_depth=8)
+    return sd, cornell_camera(width, height), settings
+
+
+def icosphere_in_box(width=1024, height=768, level=6, seed=2):
+    rng = np.random.default_rng(seed)
+    sd = SceneDesc()
+    white = sd.material(abi.OR3_LAMBERT, (0.75, 0.75, 0.75))
+    red = sd.material(abi.OR3_LAMBERT, (0.75, 0.25, 0.25))
+    blue = sd.material(abi.OR3_LAMBERT, (0.25, 0.25, 0.75))
+    light = sd.material(abi.OR3_LAMBERT, (0.0, 0.0, 0.0), emission=(12.0, 12.0, 12.0))
+    diffuse = sd.material(abi.OR3_LAMBERT, (0.8, 0.8, 0.8))
+    gloss = sd.material(abi.OR3_PHONG, (0.8, 0.8, 0.8), phong_exponent=64.0)
+    _box_walls(sd, white, red, blue)
+    _box_light(sd, light)
+    v, f = icosphere(level)
+    disp = 1.0 + 0.1 * fbm3(v * 2.0, seed)
+    center = np.array([50.0, 45.0, 50.0])
+    pos = v * (25.0 * disp)[:, None] + center
+    vn = vertex_normals(pos, f)
+    lam = sd.layers(diffuse)
+    mix = sd.layers([(diffuse, 0.5), (gloss, 0.5)])
+    glossy = rng.random(len(f)) < 0.5
+    lay = np.where(glossy[:, None], np.array(mix, np.uint32), np.array(lam, np.uint32)).astype(np.uint32)
+    sd.add_triangles(pos[f], lay, normals=vn[f])
+    settings = dict(supersamples=16, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=10)
+    return sd, cornell_camera(width, height), settings
+
+
+def sky_image(width=2048, height=1024, seed=3, sun_dir=(0.5, 0.55, -0.3), sun_radiance=1.0e4,
+              sun_radius_deg=0.5, sigma=1.0):
+    """Equirect float sky in the reference IBL's mapping (src/renderer/IBL.h:30-45):
+    row = theta / pi (theta from +y), column = phi / 2pi (phi from +x toward +z)."""
+    rng = np.random.default_rng(seed)
+    th = (np.arange(height) + 0.5) / height * math.pi
+    ph = (np.arange(width) + 0.5) / width * 2.0 * math.pi
+    st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+    d = np.stack(np.broadcast_arrays(st * np.cos(ph)[None, :], ct, st * np.sin(ph)[None, :]), -1)
+    s = np.asarray(sun_dir, np.float64)
+    s /= np.linalg.norm(s)
+    cosg = np.clip((d * s).sum(-1), -1.0, 1.0)
+    gamma = np.arccos(cosg)
+    up = np.clip(d[..., 1], 0.0, 1.0)
+    # Preetham-like: zenith darkening + circumsolar brightening (Perez-style shape)
+    zen = 1.0 + 2.0 * np.exp(-3.0 / (up + 0.08))
+    circ = 1.0 + 8.0 * np.exp(-3.0 * gamma) + 0.45 * cosg ** 2
+    base = np.stack([0.25 * zen * circ, 0.35 * zen * circ, 0.65 * zen * circ], -1) * 0.5
+    base[d[..., 1] < 0] = 0.05
+    noise = np.exp(sigma * rng.standard_normal((height, width)) - 0.5 * sigma * sigma)
+    img = base * noise[..., None]
+    img[gamma < math.radians(sun_radius_deg)] = sun_radiance
+    return img.astype(np.float32), s
+
+
+def terrain_ibl(width=1920, height=1080, cells_x=1024, cells_z=512, seed=3, spheres=64):
+    rng = np.random.default_rng(seed)
+    sd = SceneDesc()
+    ground = sd.material(abi.OR3_LAMBERT, (0.45, 0.42, 0.38))
+    glass = sd.material(abi.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    ex, ez = 2000.0, 1000.0
+    xs = np.linspace(-ex / 2, ex / 2, cells_x + 1)
+    zs = np.linspace(-ez / 2, ez / 2, cells_z + 1)
+    X, Z = np.meshgrid(xs, zs)  # (cells_z+1, cells_x+1)
+    h = fbm3(np.stack([X / 250.0, np.zeros_like(X), Z / 250.0], -1), seed)
+    h = (h - h.min()) / (h.max() - h.min()) * 50.0
+    P = np.stack([X, h, Z], -1).reshape(-1, 3)
+    idx = np.arange((cells_z + 1) * (cells_x + 1)).reshape(cells_z + 1, cells_x + 1)
+    a, b = idx[:-1, :-1].ravel(), idx[:-1, 1:].ravel()
+    c, d = idx[1:, :-1].ravel(), idx[1:, 1:].ravel()
+    f = np.concatenate([np.stack([a, c, b], 1), np.stack([b, c, d], 1)])
+    nrm = np.cross(P[f[:, 1]] - P[f[:, 0]], P[f[:, 2]] - P[f[:, 0]])
+    flip = nrm[:, 1] < 0
+    f[flip] = f[flip][:, ::-1]
+    vn = vertex_normals(P, f)
+    sd.add_triangles(P[f], sd.layers(ground), normals=vn[f])
+    gl = sd.layers(glass)
+    for _ in range(spheres):
+        r = rng.uniform(3.0, 10.0)
+        x, z = rng.uniform(-300, 300), rng.uniform(-150, 250)
+        ix = int(round((x + ex / 2) / ex * cells_x))
+        iz = int(round((z + ez / 2) / ez * cells_z))
+        y = h[iz, ix] + r
+        sd.add_sphere((x, y, z), r, gl)
+    sky, _ = sky_image(seed=seed)
+    sd.set_env(sky)
+    cam = Camera.from_fov(width, height, (0.0, 140.0, 520.0), (0.0, 20.0, 0.0), 45.0)
+    settings = dict(supersamples=32, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=12)
+    return sd, cam, settings
+
+
+def reference_cornell(width=160, height=120):
+    """The reference's built-in CornellBoxScene, object for object
+    (src/scenes/CornellBoxScene.cpp:10-36, floors from src/scenes/Scene.cpp:88-200),
+    camera from settings.txt (position 50,55,230; direction ~(0,-0.15,-1))."""
+    sd = SceneDesc()
+    L = abi.OR3_LAMBERT
+
+    def floor(kind, sx, sy, pos, mat):
+        # Scene::AddFloor* vertex lists, translated by `pos`
+        hx, hy = sx / 2.0, sy / 2.0
+        p = np.asarray(pos, np.float64)
+        tbl = {
+            "YZ_xUp": ([(0, hx, -hy), (0, hx, hy), (0, -hx, hy)], [(0, -hx, -hy), (0, hx, -hy), (0, -hx, hy)],
+                       (1, 0, 0)),
+            "YZ_xDown": ([(0, -hx, hy), (0, hx, hy), (0, hx, -hy)], [(0, -hx, hy), (0, hx, -hy), (0, -hx, -hy)],
+                         (-1, 0, 0)),
+            "XY_zUp": ([(-hx, hy, 0), (-hx, -hy, 0), (hx, -hy, 0)], [(hx, hy, 0), (-hx, hy, 0), (hx, -hy, 0)],
+                       (0, 0, 1)),
+            "XY_zDown": ([(hx, -hy, 0), (-hx, -hy, 0), (-hx, hy, 0)], [(hx, -hy, 0), (-hx, hy, 0), (hx, hy, 0)],
+                         (0, 0, -1)),
+            "XZ_yUp": ([(-hx, 0, -hy), (-hx, 0, hy), (hx, 0, -hy)], [(hx, 0, -hy), (-hx, 0, hy), (hx, 0, hy)],
+                       (0, 1, 0)),
+            "XZ_yDown": ([(hx, 0, -hy), (-hx, 0, hy), (-hx, 0, -hy)], [(hx, 0, hy), (-hx, 0, hy), (hx, 0, -hy)],
+                         (0, -1, 0)),
+        }
+        t0, t1, n = tbl[kind]
+        tris = np.asarray([t0, t1], np.float64) + p
+        normals = np.broadcast_to(np.asarray(n, np.float64), (2, 3, 3))
+        sd.add_triangles(tris, sd.layers(mat), normals=normals)
+
+    red = sd.material(L, (0.75, 0.25, 0.25))
+    blue = sd.material(L, (0.25, 0.25, 0.75))
+    back = sd.material(L, (1, 1, 1))
+    front = sd.material(L, (0.75, 0.75, 0.75))
+    white = sd.material(L, (0.75, 0.75, 0.75))
+    floor("YZ_xUp", 200, 200, (1, 40.8, 81.6), red)
+    floor("YZ_xDown", 200, 200, (99, 40.8, 81.6), blue)
+    floor("XY_zUp", 150, 150 / 1.77777777777, (50, 40.8, 0), back)
+    floor("XY_zDown", 150, 150 / 1.77777777777, (50, 40.8, 250), front)
+    floor("XZ_yUp", 2000, 2000, (50, 0, 81.6), white)
+    floor("XZ_yDown", 200, 200, (50, 81.6, 81.6), white)
+    green = sd.material(L, (0.25, 0.75, 0.25))
+    spec = sd.material(abi.OR3_SPECULAR, (0.99, 0.99, 0.99))
+    glass = sd.material(abi.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    lightm = sd.material(L, (0, 0, 0), emission=(36, 36, 36))
+    # first layer rate 1.0, then AddMaterial(spec, 0.1) normalises to 1/1.1, 0.1/1.1
+    sd.add_sphere((50, 20, 50), 20, sd.layers([(green, 1.0 / 1.1), (spec, 0.1 / 1.1)]))
+    sd.add_sphere((19, 16.5, 25), 16.5, sd.layers(spec))
+    sd.add_sphere((77, 16.5, 78), 16.5, sd.layers(glass))
+    sd.add_sphere((50.0, 90, 81.6), 15, sd.layers(lightm), light=True)
+    cam = Camera(width, height, (50.0, 55.0, 230.0), (0.00001, -0.15, -1.0), (0.0, 1.0, 0.0), 30.0, 40.0, 300.0, 0.0)
+    settings = dict(supersamples=4, min_samples=1, max_samples=4, step_samples=1, rr_min_depth=5, max_depth=0)
+    return sd, cam, settings
+
+
+def random_triangles(n=2000, seed=7, extent=100.0, size=8.0):
+    """Triangle soup for closest-hit parity (random orientation, both windings)."""
+    rng = np.random.default_rng(seed)
+    sd = SceneDesc()
+    m = sd.material(abi.OR3_LAMBERT, (0.5, 0.5, 0.5))
+    c = rng.uniform(0, extent, (n, 1, 3))
+    v = c + rng.uniform(-size, size, (n, 3, 3))
+    sd.add_triangles(v, sd.layers(m))
+    cen = rng.uniform(0, extent, (max(1, n // 100), 3))
+    for p in cen:
+        sd.add_sphere(p, rng.uniform(1.0, 6.0), sd.layers(m))
+    return sd
+
+
+def random_rays(n, seed, lo=-20.0, hi=120.0, target_lo=0.0, target_hi=100.0):
+    """Seeded rays from a box around the scene toward random points inside it (FP64, unit)."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3))
+    t = rng.uniform(target_lo, target_hi, (n, 3))
+    d = t - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o, d

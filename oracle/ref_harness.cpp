@@ -1,0 +1,321 @@
+// ref_harness.cpp -- TEST INFRASTRUCTURE ONLY (the oracle's reference arm).
+//
+// Drives the reference's own, unmodified C++ classes (compiled from the
+// reference sources by oracle/Makefile into oracle/_ref/) so the test suite can
+// pin the oracle and the GPU path against the reference itself:
+//   * orref_scene_create  builds a reference `Scene` from the flattened
+//     or3_scene_desc through Scene::AddObject (src/scenes/Scene.h:48-59) and,
+//     on request, Scene::ConstructBVH (src/scenes/Scene.cpp:27-34);
+//   * orref_closest       calls Scene::CheckIntersection (src/scenes/Scene.cpp:51-85);
+//   * orref_render_moments calls PathTracer::Radiance (src/renderer/PathTracer.cpp:180-199)
+//     per camera sample with the reference's per-row RNG seeding
+//     (src/renderer/PathTracer.cpp:151) and records per-pixel sums and sums of
+//     squares so the tests have standard errors;
+//   * orref_render_scene  runs PathTracer::RenderScene itself
+//     (src/renderer/PathTracer.cpp:55-85) and returns its 2W x H buffer.
+// Nothing in the product links or loads this file.
+//
+// The reference keeps Scene's containers protected and PathTracer::Radiance
+// private; this one translation unit reaches them by compiling the reference
+// headers with `private`/`protected` redefined after all standard headers are
+// in, which leaves the class layouts unchanged (GCC lays members out in
+// declaration order whatever their access).
+
+#include <algorithm>
+#include <atomic>
+#include <cassert>
+#include <cfloat>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stack>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#define private public
+#define protected public
+#include "stdafx.h"
+#include "renderer/AxisAlignedPlane.h"
+#include "renderer/Camera.h"
+#include "renderer/IBL.h"
+#include "renderer/InfiniteFloor.h"
+#include "renderer/PathTracer.h"
+#include "renderer/Polygon.h"
+#include "renderer/Sphere.h"
+#include "renderer/SphereLight.h"
+#include "scenes/Scene.h"
+#include "tools/ImageHandler.h"
+#undef private
+#undef protected
+
+#include "or3.h"
+
+using namespace OmochiRenderer;
+
+#ifdef OR3REF_CFG
+// Depth limits of the patched copy of PathTracer.cpp (see oracle/Makefile).
+extern "C" {
+int or3ref_min_depth = 5;
+int or3ref_max_depth = 0;
+}
+#endif
+
+namespace {
+
+class HarnessScene : public Scene {
+ public:
+  HarnessScene() : Scene(), m_bg(0, 0, 0) {}
+  Color Background() const override { return m_bg; }
+  void add(SceneObject *obj, bool inBVH) { AddObject(obj, true, inBVH); }
+  Color m_bg;
+  std::vector<SceneObject *> byId;  // object id -> object
+  std::unordered_map<const SceneObject *, int32_t> idOf;
+};
+
+Vector3 V(const double *p) { return Vector3(p[0], p[1], p[2]); }
+
+Material makeMaterial(const or3_material &m, const std::vector<int> &texIds) {
+  Material::REFLECTION_TYPE t = Material::REFLECTION_TYPE_LAMBERT;
+  if (m.type == OR3_SPECULAR) t = Material::REFLECTION_TYPE_SPECULAR;
+  if (m.type == OR3_REFRACTION) t = Material::REFLECTION_TYPE_REFRACTION;
+  int tex = ImageHandler::INVALID_IMAGE_ID;
+  if (m.texture >= 0 && m.texture < (int)texIds.size()) tex = texIds[m.texture];
+  return Material(t, V(m.emission), V(m.color), m.ior, tex);
+}
+
+// Reproduces the object's layer list exactly (rates as given, no re-normalisation).
+void setLayers(SceneObject *obj, const or3_scene_desc *d, const uint32_t *lay,
+               const std::vector<int> &texIds) {
+  obj->materials_.clear();
+  for (uint32_t k = 0; k < lay[1]; k++) {
+    const uint32_t li = lay[0] + k;
+    obj->materials_.push_back(SceneObject::MultiMaterialElem(
+        makeMaterial(d->materials[d->layer_material[li]], texIds), d->layer_rate[li]));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void *orref_scene_create(const or3_scene_desc *d, int use_bvh) {
+  HarnessScene *s = new HarnessScene();
+  s->m_bg = V(d->background);
+
+  std::vector<int> texIds;
+  for (uint32_t i = 0; i < d->num_textures; i++) {
+    const uint32_t w = d->texture_dims[2 * i], h = d->texture_dims[2 * i + 1];
+    int id = ImageHandler::GetInstance().CreateImage(w, h);
+    Image *img = ImageHandler::GetInstance().GetImage(id);
+    const float *src = d->texture_rgb + d->texture_offsets[i];
+    for (size_t p = 0; p < (size_t)w * h; p++)
+      img->m_image[p] = Color(src[3 * p], src[3 * p + 1], src[3 * p + 2]);
+    texIds.push_back(id);
+  }
+
+  // (id, class, index) sorted by id = the reference's insertion order.
+  struct Rec { uint32_t id; int cls; uint32_t idx; };
+  std::vector<Rec> recs;
+  uint32_t base = 0;
+  for (uint32_t i = 0; i < d->num_triangles; i++)
+    recs.push_back({d->tri_ids ? d->tri_ids[i] : base + i, 0, i});
+  base += d->num_triangles;
+  for (uint32_t i = 0; i < d->num_spheres; i++)
+    recs.push_back({d->sphere_ids ? d->sphere_ids[i] : base + i, 1, i});
+  base += d->num_spheres;
+  for (uint32_t i = 0; i < d->num_planes; i++)
+    recs.push_back({d->plane_ids ? d->plane_ids[i] : base + i, 2, i});
+  std::sort(recs.begin(), recs.end(), [](const Rec &a, const Rec &b) { return a.id < b.id; });
+
+  const Material dummy;
+  for (const Rec &r : recs) {
+    SceneObject *obj = nullptr;
+    bool inBVH = true;
+    if (r.cls == 0) {
+      const double *v = d->tri_vertices + 9 * r.idx;
+      Vector3 p0 = V(v), p1 = V(v + 3), p2 = V(v + 6);
+      Vector3 n0, n1, n2;
+      if (d->tri_normals) {
+        const double *n = d->tri_normals + 9 * r.idx;
+        n0 = V(n); n1 = V(n + 3); n2 = V(n + 6);
+      } else {
+        n0 = n1 = n2 = Polygon::CalculateNormal(p0, p1, p2);
+      }
+      Vector3 uv0, uv1, uv2;
+      if (d->tri_uvs) {
+        const double *u = d->tri_uvs + 6 * r.idx;
+        uv0 = Vector3(u[0], u[1], 0); uv1 = Vector3(u[2], u[3], 0); uv2 = Vector3(u[4], u[5], 0);
+      }
+      obj = new Polygon(p0, p1, p2, uv0, uv1, uv2, n0, n1, n2, dummy, Vector3(0, 0, 0));
+      setLayers(obj, d, d->tri_layers + 2 * r.idx, texIds);
+    } else if (r.cls == 1) {
+      const double *sp = d->spheres + 4 * r.idx;
+      const bool light = d->sphere_flags && (d->sphere_flags[r.idx] & OR3_SPHERE_LIGHT);
+      if (light) obj = new SphereLight(sp[3], V(sp), dummy);
+      else obj = new Sphere(sp[3], V(sp), dummy);
+      setLayers(obj, d, d->sphere_layers + 2 * r.idx, texIds);
+    } else {
+      const double *pl = d->planes + 4 * r.idx;
+      if ((int)pl[0] == OR3_PLANE_INFINITE_FLOOR) {
+        obj = new InfiniteFloor(pl[2], dummy);
+      } else {
+        AxisAlignedPlane::PLANE_AXIS ax = AxisAlignedPlane::PLANE_XY;
+        if ((int)pl[1] == 1) ax = AxisAlignedPlane::PLANE_XZ;
+        if ((int)pl[1] == 2) ax = AxisAlignedPlane::PLANE_YZ;
+        obj = new AxisAlignedPlane(dummy, ax, pl[2], pl[3] != 0.0);
+      }
+      setLayers(obj, d, d->plane_layers + 2 * r.idx, texIds);
+      inBVH = false;
+    }
+    s->add(obj, inBVH);
+    if (s->byId.size() <= r.id) s->byId.resize(r.id + 1, nullptr);
+    s->byId[r.id] = obj;
+    s->idOf[obj] = (int32_t)r.id;
+  }
+
+  if (d->env_rgb && d->env_width && d->env_height) {
+    // The IBL constructor only reads a .hdr file; feed the float image instead
+    // (no RGBE quantisation).
+    std::streambuf *old = std::cerr.rdbuf(nullptr);
+    IBL *ibl = new IBL("");
+    std::cerr.rdbuf(old);
+    ibl->m_image.m_width = d->env_width;
+    ibl->m_image.m_height = d->env_height;
+    ibl->m_image.m_image.resize((size_t)d->env_width * d->env_height);
+    for (size_t p = 0; p < (size_t)d->env_width * d->env_height; p++)
+      ibl->m_image.m_image[p] = Color(d->env_rgb[3 * p], d->env_rgb[3 * p + 1], d->env_rgb[3 * p + 2]);
+    s->m_ibl.reset(ibl);
+  }
+  if (use_bvh && !s->m_inBVHObjects.empty()) s->ConstructBVH();
+  return s;
+}
+
+void orref_scene_destroy(void *p) { delete static_cast<HarnessScene *>(p); }
+
+// Closest hit of n rays through Scene::CheckIntersection.
+int orref_closest(void *p, size_t n, const double *orig, const double *dir, int32_t *id,
+                  double *t, double *normal, double *pos) {
+  HarnessScene *s = static_cast<HarnessScene *>(p);
+  for (size_t i = 0; i < n; i++) {
+    Ray ray(V(orig + 3 * i), V(dir + 3 * i));
+    Scene::IntersectionInformation info;
+    const bool hit = s->CheckIntersection(ray, info);
+    id[i] = hit ? s->idOf[info.object] : -1;
+    t[i] = hit ? info.hit.distance : INF;
+    for (int k = 0; k < 3; k++) {
+      const double nv = k == 0 ? info.hit.normal.x : k == 1 ? info.hit.normal.y : info.hit.normal.z;
+      const double pv = k == 0 ? info.hit.position.x : k == 1 ? info.hit.position.y : info.hit.position.z;
+      if (normal) normal[3 * i + k] = hit ? nv : 0.0;
+      if (pos) pos[3 * i + k] = hit ? pv : 0.0;
+    }
+  }
+  return 0;
+}
+
+static Camera makeCamera(const or3_camera *c) {
+  Camera cam(c->width, c->height, V(c->position), V(c->direction), V(c->up),
+             c->screen_height_world, c->distance_to_screen, c->focal_distance);
+  if (c->aperture_radius > 0) cam.SetAperture(std::make_shared<CircleAperture>(c->aperture_radius));
+  return cam;
+}
+
+#ifdef OR3REF_CFG
+void orref_set_depth_limits(int rr_min_depth, int max_depth) {
+  or3ref_min_depth = rr_min_depth;
+  or3ref_max_depth = max_depth;
+}
+#endif
+
+// Per-pixel moments of the reference estimator.  Each camera sample is one
+// PathTracer::Radiance call, exactly as in scanPixelsOnYAndCastRays
+// (src/renderer/PathTracer.cpp:143-175): per (row, pass) Random seed
+// y+1+prev*H, fixed ss x ss grid, one camera ray per sub-pixel per pass.
+// Rows are spread over `nthreads` threads dynamically.  sum/sumsq: W*H*3,
+// rows top-down.  Returns the wall-clock seconds in *seconds.
+int orref_render_moments(void *p, const or3_camera *c, int min_s, int max_s, int step, int ss,
+                         int nthreads, int nee, double *sum, double *sumsq, double *seconds) {
+  HarnessScene *s = static_cast<HarnessScene *>(p);
+  Camera cam = makeCamera(c);
+  PathTracer pt(cam, min_s, max_s, step, ss, nullptr);
+  pt.EnableNextEventEstimation(nee != 0);
+  const int W = (int)c->width, H = (int)c->height;
+  std::memset(sum, 0, sizeof(double) * 3 * W * H);
+  std::memset(sumsq, 0, sizeof(double) * 3 * W * H);
+  if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
+  auto t0 = std::chrono::steady_clock::now();
+  int prev = 0;
+  for (int next = min_s; next <= max_s; next += step) {
+    std::atomic<int> row(0);
+    auto work = [&]() {
+      for (int y = row.fetch_add(1); y < H; y = row.fetch_add(1)) {
+        Random rnd(static_cast<unsigned int>(y + 1 + prev * H));
+        for (int x = 0; x < W; x++) {
+          double *S = sum + 3 * ((size_t)(H - 1 - y) * W + x);
+          double *Q = sumsq + 3 * ((size_t)(H - 1 - y) * W + x);
+          for (int sy = 0; sy < ss; sy++)
+            for (int sx = 0; sx < ss; sx++) {
+              const double rx = (2.0 * sx + 1.0) / (2 * ss);
+              const double ry = (2.0 * sy + 1.0) / (2 * ss);
+              Ray ray(cam.SampleRayForPixel(x + rx, y + ry, rnd));
+              for (int k = prev + 1; k <= next; k++) {
+                Color L = pt.Radiance(*s, ray, rnd, 0);
+                S[0] += L.x; S[1] += L.y; S[2] += L.z;
+                Q[0] += L.x * L.x; Q[1] += L.y * L.y; Q[2] += L.z * L.z;
+              }
+            }
+        }
+      }
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < nthreads; i++) th.emplace_back(work);
+    for (auto &t : th) t.join();
+    prev = next;
+  }
+  if (seconds)
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return 0;
+}
+
+// The reference's own PathTracer::RenderScene.  `out` receives the
+// 2W x H result buffer (ScreenPixels::GetScreen); with nthreads <= 2 the whole
+// image lies in the left viewport (src/renderer/PathTracer.cpp:104-111).
+int orref_render_scene(void *p, const or3_camera *c, int min_s, int max_s, int step, int ss,
+                       int nthreads, int nee, double *out, double *seconds) {
+  HarnessScene *s = static_cast<HarnessScene *>(p);
+  Camera cam = makeCamera(c);
+  PathTracer *pt = new PathTracer(cam, min_s, max_s, step, ss, nullptr);
+  pt->EnableNextEventEstimation(nee != 0);
+  pt->SetMaxThreadCount(nthreads);
+  std::streambuf *old = std::cerr.rdbuf(nullptr);
+  auto t0 = std::chrono::steady_clock::now();
+  pt->RenderScene(*s);
+  double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::cerr.rdbuf(old);
+  const ScreenPixels *px = pt->GetResult();
+  const size_t n = px->CalcScreenWidth() * px->CalcScreenHeight();
+  const Color *img = px->GetScreen();
+  for (size_t i = 0; i < n; i++) {
+    out[3 * i] = img[i].x; out[3 * i + 1] = img[i].y; out[3 * i + 2] = img[i].z;
+  }
+  if (seconds) *seconds = sec;
+  // PathTracer's destructor frees a scalar `new` with delete[]
+  // (src/renderer/PathTracer.cpp:52 vs :62); free the result here so that
+  // destructor only sees a null pointer.
+  delete pt->m_result;
+  pt->m_result = nullptr;
+  delete pt;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Mpaths/s of the GB300 path-tracing hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload mesh|cornell|terrain]
+
+A step is one full render (or3_render) of the workload: by default the
+displaced level-6 icosphere (81,920 triangles, Lambert + Phong layers) in the
+Cornell box, 1024x768, 16x16 sub-pixel grid = 256 samples per pixel, max
+depth 10 -- 201,326,592 camera paths per step.  Synthetic, seeded scenes.
+
+value      camera paths / device time of the passes (CUDA events on the
+           library's stream, scene resident in HBM), Mpaths/s
+e2e        the same through the C ABI from host buffers: scene upload
+           (flatten + BVH build + H2D), render, frame D2H, per step
+roofline   extend (closest-hit) kernel: algorithmic bytes (64 B per wide node
+           fetched, 48 B per triangle record, 16 B per sphere record, counted
+           by an instrumented run of the same render) / its event-timed
+           duration, against the measured HBM copy bandwidth
+cpu_baseline  the C oracle (FP64 restatement of the reference path, its BVH)
+           on all host cores over a bounded, evenly spread sample of paths
+With --gpus N > 1 (torchrun), every rank renders a replica of the workload
+(the path does not exchange data between GPUs): scaling "weak".
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency when served"
+
+
+def workload(pkg, name):
+    W = pkg.workloads
+    if name == "cornell":
+        sd, cam, st = W.cornell_box(256, 256)
+        desc = "cornell_box_10tri_2spheres_256x256_ss8_64spp_rr3_maxdepth8"
+    elif name == "terrain":
+        sd, cam, st = W.terrain_ibl()
+        desc = "terrain_1048576tri_64glass_ibl2048x1024_1920x1080_ss32_1024spp_maxdepth12"
+    else:
+        sd, cam, st = W.icosphere_in_box()
+        desc = "displaced_icosphere_81920tri_phong_in_cornell_1024x768_ss16_256spp_maxdepth10"
+    return sd, cam, st, desc
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        if not self.rows:
+            return out
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        out["sm_mhz"] = float(np.median(sm)) if sm else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for k, nm in enumerate(names):
+            if any(len(r) > 5 + k and r[5 + k] == "Active" for r in self.rows):
+                out["reasons"].append(nm)
+        return out
+
+
+def desc_bytes(sd):
+    a = sd.arrays()
+    n = sum(v.nbytes for k, v in a.items() if isinstance(v, np.ndarray))
+    n += len(a["mat"]) * 80
+    if sd.env is not None:
+        n += sd.env.nbytes
+    return int(n)
+
+
+def cpu_baseline(pkg, sd, cam, st, target_s=15.0, nthreads=None):
+    """The oracle port on all host cores over an evenly spread sample of paths."""
+    orc = ge.load_oracle().CRestatement()
+    nthreads = nthreads or os.cpu_count()
+    scene = orc.scene(sd, use_bvh=True)
+    ss2 = st["supersamples"] ** 2
+    total = cam.width * cam.height * ss2 * st["max_samples"]
+    kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
+              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"], seed=1)
+    chunks = 64
+    # calibrate
+    probe = 4096
+    t0 = time.perf_counter()
+    for c in range(8):
+        scene.path_radiance(cam, (total // 8) * c, probe // 8, nthreads=nthreads, **kw)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(max(rate * target_s, 65536), total))
+    per = max(n // chunks, 1)
+    t0 = time.perf_counter()
+    for c in range(chunks):
+        scene.path_radiance(cam, (total // chunks) * c, per, nthreads=nthreads, **kw)
+    sec = time.perf_counter() - t0
+    return {"value": per * chunks / sec / 1e6, "unit": "Mpaths/s", "cores": nthreads, "kind": "port",
+            "sample": "%d camera paths in %d evenly spaced runs of the %d-path workload, FP64 C oracle, "
+                      "reference BVH, %.1f s" % (per * chunks, chunks, total, sec)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args, pkg, world, rank):
+    if rank != 0:
+        return
+    sd, cam, st, desc = workload(pkg, args.workload)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(pkg, sd, cam, st, target_s=2.0)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(pkg, sd, cam, st, target_s=args.cpu_seconds / max(args.steps, 1)))
+    v = float(np.mean([x["value"] for x in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = v
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "Mpaths/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "paths_per_step": cam.width * cam.height * st["supersamples"] ** 2
+                       * st["max_samples"]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0},
+            "note": "the reference's own C++ cannot be built on this host (its sources are not shipped); "
+                    "this arm times the FP64 C restatement of the same path (oracle port) on all host cores"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mesh", choices=["mesh", "cornell", "terrain"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local, dist = dist_setup(args)
+    pkg = ge.load_package()
+    if args.impl == "reference":
+        run_reference(args, pkg, world, rank)
+        return
+
+    import torch
+    ctx = pkg.Context(local)
+    sd, cam, st, desc = workload(pkg, args.workload)
+    A = pkg.abi
+    kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
+              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"])
+    t0 = time.perf_counter()
+    sid = ctx.upload(sd)
+    upload_s = time.perf_counter() - t0
+    info = ctx.scene_info(sid)
+
+    # algorithmic bytes per extension ray (instrumented run, untimed)
+    c = ctx.render(sid, cam, seed=99, flags=A.OR3_FLAG_COUNT_TRAVERSAL, **kw)
+    alg_bytes_per_ray = (64.0 * c["nodes_visited"] + 48.0 * c["tris_tested"] + 16.0 * c["spheres_tested"]) / \
+        max(c["extension_rays"], 1)
+
+    for i in range(args.warmup):
+        ctx.render(sid, cam, seed=1000 + i, **kw)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:%d" % local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    torch.cuda.synchronize()
+    render_ms = ext_ms = 0.0
+    ext_launches = paths = ext_rays = bounces = waves = passes = 0
+    w0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()  # L2 (129 MB) flushed between steps
+        s = ctx.render(sid, cam, seed=i, flags=A.OR3_FLAG_TIME_KERNELS, **kw)
+        render_ms += s["render_ms"]
+        ext_ms += s["extend_ms"]
+        ext_launches += s["extend_launches"]
+        paths += s["camera_paths"]
+        ext_rays += s["extension_rays"]
+        bounces += s["bounces"]
+        waves += s["waves"]
+        passes += s["passes"]
+    torch.cuda.synchronize()
+    barrier(dist)
+    wall_s = time.perf_counter() - w0
+    clk = clocks.stop()
+    dev_s = max_over_ranks(dist, render_ms / 1000.0)
+    total_paths = sum_over_ranks(dist, float(paths))
+    value = total_paths / dev_s / 1e6
+
+    # end to end through the C ABI from host buffers
+    e2e_steps = max(args.e2e_steps, 1)
+    frame_bytes = 2 * cam.width * cam.height * 3 * 8
+    h2d = desc_bytes(sd) + 2 * 200
+    barrier(dist)
+    e0 = time.perf_counter()
+    for i in range(e2e_steps):
+        sid2 = ctx.upload(sd)
+        ctx.render(sid2, cam, seed=50 + i, **kw)
+        img, _ = ctx.frame(cam.width, cam.height)
+        ctx.release(sid2)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - e0)
+    e2e_paths = sum_over_ranks(dist, float(paths / args.steps * e2e_steps))
+
+    launches = 2 * waves + 3 * bounces + passes
+    avg_ext_ms = ext_ms / max(ext_launches, 1)
+    achieved = alg_bytes_per_ray * ext_rays / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else None
+    peak, peak_kind = load_peaks()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pkg, sd, cam, st, target_s=args.cpu_seconds)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": render_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
+            "config": {"workload": desc, "paths_per_step": paths // args.steps,
+                       "extension_rays_per_step": ext_rays // args.steps, "triangles": int(info["num_primitives"]),
+                       "wide_nodes": int(info["num_nodes"]), "scene_upload_ms": upload_s * 1000.0,
+                       "bvh_build_ms": info["build_ms"], "l2": "flushed between steps (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "wall_s_timed": wall_s, "mrays_per_s": ext_rays / (render_ms / 1000.0) / 1e6},
+            "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": frame_bytes,
+                    "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},
+            "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": None,
+                         "alg_bytes_per_ray": alg_bytes_per_ray, "avg_launch_ms": avg_ext_ms,
+                         "launches": ext_launches},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.release(sid)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -139,6 +139,8 @@ typedef struct or3_camera {
 #define OR3_FLAG_UNSORTED 2u     /* shade without partitioning rays by material */
 #define OR3_FLAG_NO_GRAPH 4u     /* launch the bounce loop without a CUDA graph */
 #define OR3_FLAG_NO_TAIL 8u      /* no single-launch tail for the last few rays */
+#define OR3_FLAG_TIME_KERNELS 16u      /* CUDA events around every extend/shade launch */
+#define OR3_FLAG_COUNT_TRAVERSAL 32u   /* count nodes and primitives visited (slower) */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */
@@ -172,6 +174,15 @@ typedef struct or3_render_stats {
   double upload_ms;        /* scene upload + BVH build of the rendered scene */
   int32_t samples;         /* samples per subpixel accumulated */
   int32_t passes;
+  /* OR3_FLAG_TIME_KERNELS: summed device time and launch counts */
+  double extend_ms;
+  double shade_ms;
+  uint64_t extend_launches;
+  uint64_t shade_launches;
+  /* OR3_FLAG_COUNT_TRAVERSAL: totals over all extension rays */
+  uint64_t nodes_visited;  /* 64-byte wide nodes fetched */
+  uint64_t tris_tested;    /* 48-byte triangle records tested */
+  uint64_t spheres_tested; /* sphere records tested */
 } or3_render_stats;
 
 typedef struct or3_scene_info {

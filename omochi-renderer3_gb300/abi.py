@@ -27,6 +27,8 @@ OR3_FLAG_KEEP_PATHS = 1
 OR3_FLAG_UNSORTED = 2
 OR3_FLAG_NO_GRAPH = 4
 OR3_FLAG_NO_TAIL = 8
+OR3_FLAG_TIME_KERNELS = 16
+OR3_FLAG_COUNT_TRAVERSAL = 32
 
 API_VERSION = 1
 
@@ -78,7 +80,11 @@ class RenderStatsC(ctypes.Structure):
     _fields_ = [("camera_paths", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
                 ("shadow_rays", ctypes.c_uint64), ("bounces", ctypes.c_uint64), ("waves", ctypes.c_uint64),
                 ("render_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
-                ("samples", ctypes.c_int32), ("passes", ctypes.c_int32)]
+                ("samples", ctypes.c_int32), ("passes", ctypes.c_int32),
+                ("extend_ms", ctypes.c_double), ("shade_ms", ctypes.c_double),
+                ("extend_launches", ctypes.c_uint64), ("shade_launches", ctypes.c_uint64),
+                ("nodes_visited", ctypes.c_uint64), ("tris_tested", ctypes.c_uint64),
+                ("spheres_tested", ctypes.c_uint64)]
 
 
 class SceneInfoC(ctypes.Structure):

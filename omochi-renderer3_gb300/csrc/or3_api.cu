@@ -65,6 +65,7 @@ struct or3_context {
   uint64_t last_wave_paths = 0;
   bool last_kept_paths = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -263,6 +264,7 @@ int or3_context_create(int device, or3_context **out) {
   cudaMemset(ctx->dstats, 0, 8 * sizeof(unsigned long long));
   cudaEventCreate(&ctx->ev0);
   cudaEventCreate(&ctx->ev1);
+  for (int k = 0; k < 3; k++) cudaEventCreate(&ctx->kev[k]);
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(OR3_ERR_CUDA);
   *out = ctx;
   return OR3_OK;
@@ -289,6 +291,8 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFreeHost(ctx->frame_pinned);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (int k = 0; k < 3; k++)
+    if (ctx->kev[k]) cudaEventDestroy(ctx->kev[k]);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return OR3_OK;
@@ -609,6 +613,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const int grid_ext = ctx->num_sms * ctx->occ_extend;
   const int grid_sh = ctx->num_sms * ctx->occ_shade;
   const int smem_nodes = (int)std::min<uint64_t>(256, sg->view.num_nodes);
+  const bool timek = (prm->flags & OR3_FLAG_TIME_KERNELS) != 0;
+  const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
@@ -636,14 +642,26 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         int in = 0;
         uint32_t count = w.num_paths;
         for (int bounce = 0; count > 0; bounce++) {
-          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, st);
+          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[0], st));
+          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, st);
+          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
+          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
           launch_reset_count(q, in, st);
           in ^= 1;
           OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t),
                                         cudaMemcpyDeviceToHost, st));
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
           count = ctx->host_counters[in];
+          if (timek) {
+            float e = 0.f, s2 = 0.f;
+            cudaEventElapsedTime(&e, ctx->kev[0], ctx->kev[1]);
+            cudaEventElapsedTime(&s2, ctx->kev[1], ctx->kev[2]);
+            stats.extend_ms += e;
+            stats.shade_ms += s2;
+            stats.extend_launches++;
+            stats.shade_launches++;
+          }
           if (ctx->host_counters[2]) break;
           if (bounce > 100000) break;
         }
@@ -697,6 +715,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];
   stats.bounces = hs[2];
+  stats.nodes_visited = hs[3];
+  stats.tris_tested = hs[4];
+  stats.spheres_tested = hs[5];
   stats.samples = prev;
   stats.passes = passes;
   stats.upload_ms = sg->info.build_ms + sg->info.upload_ms;

@@ -182,9 +182,11 @@ __device__ __forceinline__ float safe_inv(float x) {
 //     then the not-in-BVH objects, as in the reference.
 // `nodes_smem`/`smem_nodes`: the first smem_nodes nodes may be read from
 // shared memory instead of global.
-template <bool ANY>
+// COUNT: adds nodes fetched, triangles and spheres tested to counts_out[0..2].
+template <bool ANY, bool COUNT = false>
 __device__ __forceinline__ Hit trace(const DevScene &S, V3 o, V3 d, float tmax, uint32_t *err,
-                                     const uint4 *nodes_smem = nullptr, uint32_t smem_nodes = 0) {
+                                     const uint4 *nodes_smem = nullptr, uint32_t smem_nodes = 0,
+                                     uint32_t *counts_out = nullptr) {
   Hit h;
   h.t = tmax;
   h.rec = kMissRec;
@@ -200,6 +202,7 @@ __device__ __forceinline__ Hit trace(const DevScene &S, V3 o, V3 d, float tmax, 
     uint32_t node = 0;
     for (;;) {
       uint4 n0, n1, n2, n3;
+      if (COUNT) counts_out[0]++;
       if (node < smem_nodes) {
         n0 = nodes_smem[4 * node + 0];
         n1 = nodes_smem[4 * node + 1];
@@ -252,6 +255,10 @@ __device__ __forceinline__ Hit trace(const DevScene &S, V3 o, V3 d, float tmax, 
         const uint32_t first = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
         const uint32_t cnt = (counts >> (8 * i)) & 0xFFu;
         const uint32_t ntri = cnt & 15u, nsph = cnt >> 4;
+        if (COUNT) {
+          counts_out[1] += ntri;
+          counts_out[2] += nsph;
+        }
         for (uint32_t k = 0; k < ntri; k++) {
           const float4 *pr = S.prims + 3 * (size_t)(first + k);
           const float4 a = __ldg(pr), b = __ldg(pr + 1), c = __ldg(pr + 2);

@@ -77,6 +77,9 @@ __global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
 
 constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 
+// Closest hit for every queued ray.  COUNT adds the nodes, triangles and
+// spheres each ray touched to stats[3..5] (the algorithmic byte count).
+template <bool COUNT>
 __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
   __shared__ uint4 snodes[kSmemNodes * 4];
   const uint32_t n = q.counters[in];
@@ -91,10 +94,25 @@ __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, in
   }
   const float4 *qo = q.orig[in];
   const float4 *qd = q.dir[in];
+  uint32_t cnt[3] = {0u, 0u, 0u};
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 ro = qo[i], rd = qd[i];
-    const Hit h = trace<false>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns);
+    const Hit h = trace<false, COUNT>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns, cnt);
     q.hits[i] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+  }
+  if (COUNT) {
+    unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
+#pragma unroll
+    for (int ofs = 16; ofs > 0; ofs >>= 1) {
+      c0 += __shfl_xor_sync(0xFFFFFFFFu, c0, ofs);
+      c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, ofs);
+      c2 += __shfl_xor_sync(0xFFFFFFFFu, c2, ofs);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+      atomicAdd(&q.stats[3], c0);
+      atomicAdd(&q.stats[4], c1);
+      atomicAdd(&q.stats[5], c2);
+    }
   }
 }
 
@@ -399,9 +417,11 @@ void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int ou
   k_raygen<<<g > 0 ? g : 1, block, 0, st>>>(rc, w, q, out);
 }
 
-void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes,
+void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    cudaStream_t st) {
-  k_extend<<<grid, block, 0, st>>>(S, q, in, smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes);
+  const int sn = smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes;
+  if (count) k_extend<true><<<grid, block, 0, st>>>(S, q, in, sn);
+  else k_extend<false><<<grid, block, 0, st>>>(S, q, in, sn);
 }
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
@@ -440,7 +460,7 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
   k_trace_occluded<<<grid_for(n, 128), 128, 0, st>>>(S, n, orig, dir, tmax, occ, err);
 }
 
-const void *kernel_extend_ptr() { return (const void *)k_extend; }
+const void *kernel_extend_ptr() { return (const void *)k_extend<false>; }
 const void *kernel_shade_ptr() { return (const void *)k_shade; }
 
 }  // namespace or3

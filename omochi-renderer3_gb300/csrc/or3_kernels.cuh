@@ -47,7 +47,7 @@ struct Queues {
   float4 *hits;
   float4 *pathL;  // per camera path radiance of the wave
   uint32_t *counters;         // [0],[1] queue lengths, [2] error bits
-  unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] bounces
+  unsigned long long *stats;  // [0] extension rays [1] shadow rays [2] bounces [3] nodes [4] tris [5] spheres
   uint32_t capacity;          // entries per queue
   uint32_t pad;
 };
@@ -63,7 +63,7 @@ struct LaunchCfg {
 // host launchers (or3_kernels.cu)
 void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int out, int grid, int block,
                    cudaStream_t st);
-void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes,
+void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    cudaStream_t st);
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                   int grid, int block, cudaStream_t st);

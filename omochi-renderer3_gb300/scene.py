@@ -126,6 +126,21 @@ class SceneDesc:
     def num_objects(self):
         return self._next_id
 
+    def digest(self):
+        """sha256 of the flattened scene (fixtures record which scene they were made from)."""
+        import hashlib
+        a = self.arrays()
+        h = hashlib.sha256()
+        h.update(repr(a["mat"]).encode())
+        for k in sorted(a):
+            if k == "mat" or a[k] is None:
+                continue
+            h.update(k.encode())
+            h.update(np.ascontiguousarray(a[k]).tobytes())
+        if self.env is not None:
+            h.update(self.env.tobytes())
+        return h.hexdigest()
+
     # ---- flattened arrays
     def arrays(self):
         a = {}

@@ -569,6 +569,16 @@ void orc_scene_destroy(orc_scene *s) {
 
 int orc_scene_bvh_nodes(const orc_scene *s) { return s->nnodes; }
 
+int orc_object_distance(const orc_scene *s, size_t n, const int32_t *id, const double *orig, const double *dir,
+                        double *t) {
+  for (size_t i = 0; i < n; i++) {
+    hitrec h;
+    t[i] = INF;
+    if (id[i] >= 0 && id[i] < s->n && obj_hit(&s->o[id[i]], ld(orig + 3 * i), ld(dir + 3 * i), &h)) t[i] = h.t;
+  }
+  return 0;
+}
+
 int orc_closest(const orc_scene *s, size_t n, const double *orig, const double *dir, int32_t *id, double *t,
                 double *normal) {
 #pragma omp parallel for schedule(dynamic, 256)

@@ -45,6 +45,11 @@ int orc_scene_bvh_nodes(const orc_scene *s);
 int orc_closest(const orc_scene *s, size_t n, const double *orig, const double *dir, int32_t *id, double *t,
                 double *normal);
 
+/* Distance at which ray i hits object id[i] alone (INF = no hit), to tell
+   ties from real disagreements. */
+int orc_object_distance(const orc_scene *s, size_t n, const int32_t *id, const double *orig, const double *dir,
+                        double *t);
+
 /* Radiance of camera paths g in [first, first + count) (the GPU's path order,
    include/or3.h), written to out[3 * (g - first)]. */
 int orc_path_radiance(const orc_scene *s, const or3_camera *cam, const orc_params *p, uint64_t first,

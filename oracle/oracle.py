@@ -64,6 +64,7 @@ class CRestatement:
         lib.orc_scene_destroy.argtypes = [ctypes.c_void_p]
         lib.orc_scene_bvh_nodes.argtypes = [ctypes.c_void_p]
         lib.orc_closest.argtypes = [ctypes.c_void_p, ctypes.c_size_t, f64p, f64p, i32p, f64p, f64p]
+        lib.orc_object_distance.argtypes = [ctypes.c_void_p, ctypes.c_size_t, i32p, f64p, f64p, f64p]
         lib.orc_path_radiance.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(OrcParams),
                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, f64p]
         lib.orc_render.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(OrcParams), ctypes.c_int,
@@ -107,6 +108,15 @@ class _OracleScene:
         self.orc.lib.orc_closest(self.h, n, _np(o, ctypes.c_double), _np(d, ctypes.c_double),
                                  _np(ids, ctypes.c_int32), _np(t, ctypes.c_double), _np(nrm, ctypes.c_double))
         return ids, t, nrm
+
+    def object_distance(self, ids, orig, dirs):
+        o = np.ascontiguousarray(orig, np.float64)
+        d = np.ascontiguousarray(dirs, np.float64)
+        i = np.ascontiguousarray(ids, np.int32)
+        t = np.zeros(len(i), np.float64)
+        self.orc.lib.orc_object_distance(self.h, len(i), _np(i, ctypes.c_int32), _np(o, ctypes.c_double),
+                                         _np(d, ctypes.c_double), _np(t, ctypes.c_double))
+        return t
 
     def path_radiance(self, camera, first, count, nthreads=0, **settings):
         cam = camera.to_c()

@@ -1,0 +1,141 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own code.
+
+    python tests/golden/make_golden.py [--rmse]
+
+Needs oracle/_ref (the reference sources compiled by `make -C oracle ref`),
+so it runs where the reference is present; the fixtures it writes are
+committed and are all the GPU tests need.
+
+  closest_<scene>.npz   seeded FP64 ray sets (primary rays from around the
+                        scene and secondary rays leaving surfaces) with the
+                        reference's Scene::CheckIntersection answers through
+                        its BVH (use_bvh=1) and its brute-force loop (use_bvh=0)
+  render_<name>.npz     per-pixel mean and standard error of the reference's
+                        PathTracer::Radiance estimator (float16), sample counts
+  rmse_cornell_cfg.npz  (--rmse) 16384-spp reference render of the Cornell
+                        workload, the RMSE target
+Each fixture stores a digest of the flattened scene it was made from.
+"""
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+pkg = ge.load_package()
+O = ge.load_oracle()
+W = pkg.workloads
+
+
+def scene_digest(sd):
+    return sd.digest()
+
+
+def ico_in_box(level):
+    sd, cam, st = W.icosphere_in_box(64, 48, level=level)
+    return sd
+
+
+CLOSEST_SCENES = {
+    "cornell": lambda: W.cornell_box()[0],
+    "refcornell": lambda: W.reference_cornell()[0],
+    "tris3000": lambda: W.random_triangles(3000, 7),
+    "ico3": lambda: ico_in_box(3),
+    "ico6": lambda: ico_in_box(6),
+}
+
+
+def secondary_rays(o, d, ids, t, seed):
+    """Rays leaving the first-hit points in random directions."""
+    rng = np.random.default_rng(seed)
+    hit = ids >= 0
+    p = o[hit] + d[hit] * t[hit][:, None]
+    v = rng.normal(size=p.shape)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return p, v
+
+
+def make_closest(name, nrays=2048, seed=5):
+    sd = CLOSEST_SCENES[name]()
+    ref = O.Reference()
+    rs_bvh = ref.scene(sd, use_bvh=True)
+    rs_bf = ref.scene(sd, use_bvh=False)
+    o1, d1 = W.random_rays(nrays, seed)
+    ids1, t1, _ = rs_bvh.closest(o1, d1)
+    o2, d2 = secondary_rays(o1, d1, ids1, t1, seed + 1)
+    o = np.concatenate([o1, o2])
+    d = np.concatenate([d1, d2])
+    ids, t, nrm = rs_bvh.closest(o, d)
+    ids_bf, t_bf, _ = rs_bf.closest(o, d)
+    path = os.path.join(HERE, "closest_%s.npz" % name)
+    np.savez_compressed(path, digest=scene_digest(sd), orig=o, dir=d, ids=ids, t=t, normal=nrm.astype(np.float32),
+                        ids_bruteforce=ids_bf, t_bruteforce=t_bf, n_primary=len(o1))
+    print("%s: %d rays, hit %.3f, bvh==bruteforce %.5f" % (path, len(o), (ids >= 0).mean(), (ids == ids_bf).mean()))
+
+
+RENDERS = {
+    # name: (builder, settings, cfg library (rr, max depth) or None, nthreads)
+    "cornell_ref": (lambda: W.cornell_box(256, 256),
+                    dict(supersamples=8, min_samples=1, max_samples=16, step_samples=1), None),
+    "cornell_cfg": (lambda: W.cornell_box(128, 128),
+                    dict(supersamples=8, min_samples=1, max_samples=16, step_samples=1), (3, 8)),
+    "refcornell": (lambda: W.reference_cornell(160, 120),
+                   dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
+}
+
+
+def make_render(name):
+    build, settings, cfg = RENDERS[name]
+    sd, cam, _ = build()
+    ref = O.Reference(cfg=cfg is not None)
+    if cfg is not None:
+        ref.set_depth_limits(*cfg)
+    t0 = time.time()
+    s, q, sec = ref.scene(sd, use_bvh=False).render_moments(cam, nthreads=os.cpu_count(), **settings)
+    n = settings["max_samples"] * settings["supersamples"] ** 2
+    mean = s / n
+    var = np.maximum(q / n - mean * mean, 0.0) / n
+    path = os.path.join(HERE, "render_%s.npz" % name)
+    np.savez_compressed(path, digest=scene_digest(sd), mean=mean.astype(np.float16),
+                        se=np.sqrt(var).astype(np.float16), n=n, width=cam.width, height=cam.height,
+                        rr_min_depth=cfg[0] if cfg else 5, max_depth=cfg[1] if cfg else 0,
+                        seconds=sec, **{k: v for k, v in settings.items()})
+    print("%s: %dx%d, %d paths/pixel, %.1fs (%.2f Mpaths/s)" % (path, cam.width, cam.height, n, time.time() - t0,
+                                                               cam.width * cam.height * n / sec / 1e6))
+
+
+def make_rmse():
+    sd, cam, _ = W.cornell_box(256, 256)
+    ref = O.Reference(cfg=True)
+    ref.set_depth_limits(3, 8)
+    settings = dict(supersamples=8, min_samples=1, max_samples=256, step_samples=1)
+    s, q, sec = ref.scene(sd, use_bvh=False).render_moments(cam, nthreads=os.cpu_count(), **settings)
+    n = 256 * 64
+    path = os.path.join(HERE, "rmse_cornell_cfg.npz")
+    np.savez_compressed(path, digest=scene_digest(sd), mean=(s / n).astype(np.float32), n=n, seconds=sec,
+                        rr_min_depth=3, max_depth=8, **settings)
+    print("%s: %d spp, %.0fs" % (path, n, sec))
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rmse", action="store_true")
+    ap.add_argument("--only", default="")
+    a = ap.parse_args()
+    if not O.reference_available():
+        O.build_oracle(reference=True)
+    if a.rmse:
+        make_rmse()
+        sys.exit(0)
+    for nm in CLOSEST_SCENES:
+        if not a.only or a.only == nm:
+            make_closest(nm)
+    for nm in RENDERS:
+        if not a.only or a.only == nm:
+            make_render(nm)

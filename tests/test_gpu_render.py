@@ -1,0 +1,199 @@
+"""GPU render parity through the C ABI (or3_render).
+
+Two bars:
+  * path by path against the C oracle, which replays the same counter-based
+    random numbers in FP64: a path's radiance must agree to 1e-3 relative
+    unless FP32 rounding flipped one of its discrete decisions (Russian
+    roulette, layer choice, a grazing hit); at most 1% of paths may differ;
+  * per pixel against the reference's own renders (golden fixtures): two-sample
+    z within 3 standard errors (see conftest.zscores), and image RMSE against
+    the 16384-spp reference render consistent with the GPU's own noise.
+"""
+import os
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden, moments_to_mean_se, zscores
+
+pytestmark = pytest.mark.gpu
+
+
+def _path_parity(pkg, ctx, orc, sd, cam, use_bvh=True, **settings):
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam, flags=pkg.abi.OR3_FLAG_KEEP_PATHS, **settings)
+        gpu = ctx.path_radiance().astype(np.float64)
+    finally:
+        ctx.release(sid)
+    ref = orc.scene(sd, use_bvh=use_bvh).path_radiance(cam, 0, gpu.shape[0], **settings)
+    close = (np.abs(gpu - ref) <= 1e-3 * (1.0 + np.abs(ref))).all(axis=1)
+    return gpu, ref, close
+
+
+@pytest.mark.parametrize("case", ["cornell", "cornell_refdepth", "refcornell", "ico_phong", "terrain_env"])
+def test_paths_match_oracle(pkg, ctx, orc, case):
+    W = pkg.workloads
+    if case == "cornell":
+        sd, cam, _ = W.cornell_box(48, 48)
+        st = dict(supersamples=4, rr_min_depth=3, max_depth=8)
+    elif case == "cornell_refdepth":
+        sd, cam, _ = W.cornell_box(48, 48)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
+    elif case == "refcornell":
+        sd, cam, _ = W.reference_cornell(64, 48)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
+    elif case == "ico_phong":
+        sd, cam, _ = W.icosphere_in_box(64, 48, level=4)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=10)
+    else:
+        sd, cam, _ = W.terrain_ibl(64, 36, cells_x=64, cells_z=32, spheres=16)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=12)
+    gpu, ref, close = _path_parity(pkg, ctx, orc, sd, cam, seed=1234, min_samples=1, max_samples=1,
+                                   step_samples=1, **st)
+    assert gpu.shape[0] == cam.width * cam.height * st["supersamples"] ** 2
+    assert np.isfinite(gpu).all()
+    assert close.mean() >= 0.99, close.mean()
+    # the few paths that diverge do not bias the image
+    mg, mr = gpu.mean(), ref.mean()
+    assert abs(mg - mr) <= 0.02 * max(mr, 1e-3) + 3 * gpu.std() / np.sqrt(len(gpu)), (mg, mr)
+
+
+RENDERS = [
+    ("render_cornell_ref.npz", lambda W: W.cornell_box(256, 256), 64, dict(rr_min_depth=5, max_depth=0)),
+    ("render_cornell_cfg.npz", lambda W: W.cornell_box(128, 128), 64, dict(rr_min_depth=3, max_depth=8)),
+    ("render_refcornell.npz", lambda W: W.reference_cornell(160, 120), 64, dict(rr_min_depth=5, max_depth=0)),
+]
+
+
+@pytest.mark.parametrize("fixture,build,samples,depth", RENDERS)
+def test_render_statistically_matches_reference(pkg, ctx, fixture, build, samples, depth):
+    g = golden(fixture)
+    sd, cam, _ = build(pkg.workloads)
+    assert sd.digest() == str(g["digest"])
+    ss = int(g["supersamples"])
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam, supersamples=ss, min_samples=samples, max_samples=samples, step_samples=1, seed=77,
+                   **depth)
+        s, q, n = ctx.moments(cam.width, cam.height)
+    finally:
+        ctx.release(sid)
+    assert n == samples * ss * ss
+    m, se = moments_to_mean_se(s, q, n)
+    z = zscores(m, se, n, g["mean"], g["se"], int(g["n"]))
+    assert np.mean(np.abs(z) > 3) < 0.01, np.mean(np.abs(z) > 3)
+    assert abs(z.mean()) < 0.05, z.mean()
+    assert 0.8 < z.var() < 1.25, z.var()
+    gm = g["mean"].astype(np.float64).mean()
+    assert abs(m.mean() - gm) / gm < 0.01
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "rmse_cornell_cfg.npz")), reason="no RMSE fixture")
+def test_rmse_against_16k_reference(pkg, ctx):
+    g = golden("rmse_cornell_cfg.npz")
+    sd, cam, st = pkg.workloads.cornell_box(256, 256)
+    assert sd.digest() == str(g["digest"])
+    sid = ctx.upload(sd)
+    ctx.render(sid, cam, supersamples=8, min_samples=1, max_samples=1, rr_min_depth=3, max_depth=8, seed=5)
+    s, q, n = ctx.moments(cam.width, cam.height)
+    ctx.release(sid)
+    m, se = moments_to_mean_se(s, q, n)
+    rmse = np.sqrt(np.mean((m - g["mean"]) ** 2))
+    # expected from the GPU's own noise plus the reference render's (n = 16384)
+    expect = np.sqrt(np.mean(se ** 2) * (1.0 + n / float(g["n"])))
+    assert rmse < 1.1 * expect, (rmse, expect)
+    assert rmse > 0.5 * expect, (rmse, expect)
+
+
+def test_frame_layout_and_progressive_callbacks(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(40, 24)
+    sid = ctx.upload(sd)
+    frames = []
+    ctx.render(sid, cam, supersamples=2, min_samples=1, max_samples=7, step_samples=3, seed=3,
+               callback=lambda s, img, w, h, mins: frames.append((s, img, w, h)))
+    last, samples = ctx.frame(cam.width, cam.height)
+    s, q, n = ctx.moments(cam.width, cam.height)
+    ctx.release(sid)
+    assert [f[0] for f in frames] == [1, 4, 7]  # PathTracer's pass schedule min..max step
+    for f in frames:
+        assert f[2] == 2 * cam.width and f[3] == cam.height
+        assert np.all(f[1][:, cam.width:] == 0)  # right viewport stays empty
+    assert samples == 7
+    np.testing.assert_array_equal(last, frames[-1][1])
+    # frame rows are top-down (ScreenPixels flips y): equal to the moments' mean
+    np.testing.assert_allclose(last[:, :cam.width], s / n, rtol=1e-12, atol=0)
+    assert n == 7 * 4
+
+
+def test_compact_layout(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(20, 10)
+    sid = ctx.upload(sd)
+    ctx.render(sid, cam, supersamples=1, seed=1, layout=pkg.abi.OR3_LAYOUT_COMPACT)
+    img, _ = ctx.frame(cam.width, cam.height, layout=pkg.abi.OR3_LAYOUT_COMPACT)
+    ctx.release(sid)
+    assert img.shape == (10, 20, 3) and img.sum() > 0
+
+
+def test_stop_rendering_from_another_thread(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(64, 64)
+    sid = ctx.upload(sd)
+    seen = []
+
+    def cb(samples, img, w, h, minutes):
+        seen.append(samples)
+        if samples >= 2:
+            threading.Thread(target=ctx.stop).start()
+            threading.Event().wait(0.2)
+
+    ctx.render(sid, cam, supersamples=2, min_samples=1, max_samples=1000, step_samples=1, seed=2, callback=cb)
+    ctx.reset_stop()
+    _, samples = ctx.frame(cam.width, cam.height)
+    ctx.release(sid)
+    assert 2 <= len(seen) < 1000
+    assert samples == seen[-1]
+
+
+def test_waves_do_not_change_the_image(pkg, ctx):
+    sd, cam, _ = pkg.workloads.icosphere_in_box(48, 32, level=3)
+    sid = ctx.upload(sd)
+    ctx.render(sid, cam, supersamples=4, min_samples=3, max_samples=3, seed=9, max_depth=10)
+    s1, q1, _ = ctx.moments(cam.width, cam.height)
+    ctx.render(sid, cam, supersamples=4, min_samples=3, max_samples=3, seed=9, max_depth=10, wave_paths=1000)
+    s2, q2, _ = ctx.moments(cam.width, cam.height)
+    st = ctx.stats()
+    ctx.release(sid)
+    assert st["waves"] > 10
+    np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-6)
+
+
+def test_invalid_arguments_are_reported(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(8, 8)
+    sid = ctx.upload(sd)
+    for bad in (dict(supersamples=0), dict(min_samples=0), dict(min_samples=3, max_samples=2),
+                dict(step_samples=0), dict(layout=7)):
+        with pytest.raises(pkg.Or3Error) as e:
+            ctx.render(sid, cam, **bad)
+        assert e.value.code == pkg.abi.OR3_ERR_INVALID_ARGUMENT
+    ctx.release(sid)
+    bad_scene = pkg.SceneDesc()
+    m = bad_scene.material(pkg.abi.OR3_LAMBERT, (1, 1, 1))
+    bad_scene.add_sphere((0, 0, 0), -1.0, bad_scene.layers(m))
+    with pytest.raises(pkg.Or3Error):
+        ctx.upload(bad_scene)
+
+
+def test_gpu_path_tracer_mirror(pkg):
+    """The Renderer-interface mirror renders progressively and exposes GetResult."""
+    sd, cam, _ = pkg.workloads.cornell_box(32, 32)
+    got = []
+    pt = pkg.GpuPathTracer(cam, 1, 3, 1, 2, callback=lambda s, img, w, h, m: got.append(s))
+    pt.EnableNextEventEstimation(False)
+    pt.SetMaxThreadCount(4)
+    pt.RenderScene(sd)
+    assert got == [1, 2, 3]
+    assert pt.GetCurrentSampleCount() == 3
+    r = pt.GetResult()
+    assert r.CalcScreenWidth() == 64 and r.CalcScreenHeight() == 32
+    assert "samples" in pt.GetCurrentRenderingInfo()

@@ -214,6 +214,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--res", default="", help="WxH override (smaller case for profiling)")
+    ap.add_argument("--ss", type=int, default=0, help="sub-pixel grid override")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local, dist = dist_setup(args)
@@ -225,6 +227,12 @@ def main():
     import torch
     ctx = pkg.Context(local)
     sd, cam, st, desc = workload(pkg, args.workload)
+    if args.res:
+        cam.width, cam.height = (int(x) for x in args.res.lower().split("x"))
+        desc += "_resized_%dx%d" % (cam.width, cam.height)
+    if args.ss:
+        st["supersamples"] = args.ss
+        desc += "_ss%d" % args.ss
     A = pkg.abi
     kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
               step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"])

@@ -334,6 +334,46 @@ __device__ __forceinline__ Hit trace(const DevScene &S, V3 o, V3 d, float tmax, 
   return h;
 }
 
+// Distance to the winning primitive re-evaluated in FP64 with the reference's
+// own formulas (Polygon.h:63-106, Sphere.h:21-78, AxisAlignedPlane.h:38-64,
+// InfiniteFloor.h:19-37).  The FP32 tests pick the primitive; one FP64
+// evaluation per ray then gives the reference's distance on the same inputs
+// even where FP32 is ill-conditioned (grazing exits, very short hops).
+__device__ __forceinline__ float refine_t(const DevScene &S, const Hit &h, V3 of, V3 df) {
+  if (h.rec == kMissRec) return h.t;
+  const double ox = of.x, oy = of.y, oz = of.z, dx = df.x, dy = df.y, dz = df.z;
+  double t;
+  if (h.rec & kPlaneBit) {
+    const PlaneRec &p = S.planes[h.rec & ~kPlaneBit];
+    if (p.kind == kPrimFloor) {
+      t = ((double)p.offset - oy) / dy;
+    } else {
+      const double dd = p.axis == 0 ? dz : p.axis == 1 ? dy : dx;
+      const double oo = p.axis == 0 ? oz : p.axis == 1 ? oy : ox;
+      t = ((double)p.offset - oo) / dd;
+    }
+  } else if ((S.info[h.rec].kind_flags & 0xFFu) == kPrimTriangle) {
+    const float4 *pr = S.prims + 3 * (size_t)h.rec;
+    const float4 a = __ldg(pr), b = __ldg(pr + 1), c = __ldg(pr + 2);
+    const double e1x = a.w, e1y = b.x, e1z = b.y, e2x = b.z, e2y = b.w, e2z = c.x;
+    const double px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+    const double det = px * e1x + py * e1y + pz * e1z;
+    const double tx = ox - a.x, ty = oy - a.y, tz = oz - a.z;
+    const double qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+    t = (qx * e2x + qy * e2y + qz * e2z) / det;
+  } else {
+    const float4 s = __ldg(S.prims + 3 * (size_t)h.rec);
+    const double cx = s.x - ox, cy = s.y - oy, cz = s.z - oz, r = s.w;
+    const double b = dx * cx + dy * cy + dz * cz;
+    const double D = b * b - (dx * dx + dy * dy + dz * dz) * (cx * cx + cy * cy + cz * cz - r * r);
+    const double sq = sqrt(D > 0.0 ? D : 0.0);
+    const double t1 = sq + b, t2 = -sq + b;
+    t = t2 > (double)kEpsD ? t2 : t1;
+  }
+  // keep the FP32 result if the FP64 re-evaluation falls outside the accepted range
+  return (t >= (double)kEpsD && t < 1e30) ? (float)t : h.t;
+}
+
 // Surface data at a hit, as HitInformation reports it (normal not yet
 // oriented toward the ray, uv when a layer is textured).
 struct Surface {

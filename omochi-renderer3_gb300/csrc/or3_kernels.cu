@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, in
   uint32_t cnt[3] = {0u, 0u, 0u};
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 ro = qo[i], rd = qd[i];
-    const Hit h = trace<false, COUNT>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns, cnt);
+    Hit h = trace<false, COUNT>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns, cnt);
+    h.t = refine_t(S, h, ld3(ro), ld3(rd));
     q.hits[i] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
   }
   if (COUNT) {
@@ -373,7 +374,8 @@ __global__ void k_trace_closest(DevScene S, size_t n, const float *orig, const f
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const V3 o = v3(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
     const V3 d = v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
-    const Hit h = trace<false>(S, o, d, kInf, err);
+    Hit h = trace<false>(S, o, d, kInf, err);
+    h.t = refine_t(S, h, o, d);
     if (h.rec == kMissRec) {
       prim[i] = -1;
       tout[i] = kInf;

@@ -126,6 +126,17 @@ class SceneDesc:
     def num_objects(self):
         return self._next_id
 
+    def quantized_f32(self):
+        """A copy whose geometry is exactly representable in FP32 (vertices,
+        sphere centres and radii, plane offsets), so an FP64 reference and the
+        FP32 kernels intersect identical primitives."""
+        import copy
+        q = copy.deepcopy(self)
+        q.tris = [(t[0].astype(np.float32).astype(np.float64),) + tuple(t[1:]) for t in q.tris]
+        q.spheres = [tuple(float(np.float32(x)) for x in s[:4]) + tuple(s[4:]) for s in q.spheres]
+        q.planes = [s[:2] + (float(np.float32(s[2])),) + tuple(s[3:]) for s in q.planes]
+        return q
+
     def digest(self):
         """sha256 of the flattened scene (fixtures record which scene they were made from)."""
         import hashlib

@@ -61,16 +61,23 @@ def secondary_rays(o, d, ids, t, seed):
     return p, v
 
 
+def f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
 def make_closest(name, nrays=2048, seed=5):
-    sd = CLOSEST_SCENES[name]()
+    # scene and rays exactly representable in FP32: the reference (FP64) and
+    # the kernels (FP32) then intersect identical rays with identical geometry
+    sd = CLOSEST_SCENES[name]().quantized_f32()
     ref = O.Reference()
     rs_bvh = ref.scene(sd, use_bvh=True)
     rs_bf = ref.scene(sd, use_bvh=False)
     o1, d1 = W.random_rays(nrays, seed)
+    o1, d1 = f32(o1), f32(d1)
     ids1, t1, _ = rs_bvh.closest(o1, d1)
     o2, d2 = secondary_rays(o1, d1, ids1, t1, seed + 1)
-    o = np.concatenate([o1, o2])
-    d = np.concatenate([d1, d2])
+    o = np.concatenate([o1, f32(o2)])
+    d = np.concatenate([d1, f32(d2)])
     ids, t, nrm = rs_bvh.closest(o, d)
     ids_bf, t_bf, _ = rs_bf.closest(o, d)
     path = os.path.join(HERE, "closest_%s.npz" % name)

@@ -1,8 +1,9 @@
 """GPU closest-hit / any-hit parity through the C ABI (or3_trace_closest).
 
 The reference answers come from the golden fixtures (the reference's own
-Scene::CheckIntersection on the same FP64 ray sets).  The GPU computes in
-FP32, so:
+Scene::CheckIntersection in FP64 on ray sets and geometry that are exactly
+representable in FP32, so both sides see identical inputs).  The GPU
+computes in FP32, so:
   * ids must match, except documented ties: the GPU's primitive is hit (in
     FP64) within 1e-6 relative distance of the reference's (a shared edge);
   * distances agree to 1e-5 relative (FP32 vs FP64);
@@ -27,7 +28,7 @@ def _scene(pkg, name):
         "tris3000": lambda: W.random_triangles(3000, 7),
         "ico3": lambda: W.icosphere_in_box(64, 48, level=3)[0],
         "ico6": lambda: W.icosphere_in_box(64, 48, level=6)[0],
-    }[name]()
+    }[name]().quantized_f32()
 
 
 def _classify(orc_scene, o, d, ids_gpu, ids_ref, t_ref):

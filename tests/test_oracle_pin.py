@@ -20,7 +20,7 @@ def _closest_scene(pkg, name):
         "tris3000": lambda: W.random_triangles(3000, 7),
         "ico3": lambda: W.icosphere_in_box(64, 48, level=3)[0],
         "ico6": lambda: W.icosphere_in_box(64, 48, level=6)[0],
-    }[name]()
+    }[name]().quantized_f32()
 
 
 def test_philox_known_answers(orc):

@@ -244,6 +244,33 @@ int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const fl
 int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *origins_host,
                        const float *dirs_host, const float *tmax_host, uint8_t *occluded_host);
 
+/* ---- rendering without allocating (no counterpart in the reference) ------
+ * For callers that must not allocate device memory while they render: code
+ * running in a host callback enqueued on a CUDA stream (CUDA calls that
+ * allocate are not allowed there), engines that give the whole device to
+ * their own pool at start-up (cudaMalloc would fail or fragment it), and
+ * frame loops that cannot afford cudaMalloc/cudaFree synchronising the device.
+ *
+ * Traces camera paths g in [first_path, first_path + num_paths) of the render
+ * that `camera` and `params` describe (the path order of or3_get_path_radiance;
+ * all paths must lie in one pass of the sample schedule) and writes 3 floats
+ * of radiance per path to radiance_dev (device memory of the context's GPU,
+ * provided by the caller).  The scene must already be uploaded.
+ *
+ * The ray queues live in one file-scope device array sized for
+ * OR3_NOALLOC_MAX_PATHS paths (about 3.7 MB, held by every GPU that loads the
+ * library until the process exits); larger num_paths is rejected with
+ * OR3_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a
+ * device looks up that array's device address, so make that first call before
+ * any stream capture.  Every call shares the array and it keeps the previous
+ * call's contents (the call clears what must start at zero); calls that
+ * overlap on the GPU -- from two host threads, or on two streams -- race on it.
+ * Blocks until the result is in radiance_dev.  stream NULL = the context's. */
+#define OR3_NOALLOC_MAX_PATHS 4096u
+int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *camera,
+                             const or3_render_params *params, uint64_t first_path, uint32_t num_paths,
+                             float *radiance_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,7 +120,12 @@ PROTOTYPES = {
                                                 ctypes.c_void_p]),
     "or3_trace_occluded": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, f32p, f32p, f32p,
                                           P(ctypes.c_uint8)]),
+    "or3_render_paths_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(CameraC), P(RenderParamsC),
+                                                ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
 }
+
+OR3_NOALLOC_MAX_PATHS = 4096
 
 _LIB = None
 

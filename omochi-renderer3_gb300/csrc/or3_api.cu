@@ -822,6 +822,54 @@ int or3_trace_closest(or3_context *ctx, int32_t scene, size_t n, const float *o,
   return rc;
 }
 
+int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3_render_params *prm,
+                             uint64_t first, uint32_t num_paths, float *radiance_dev, void *stream) {
+  if (!ctx || !cam || !prm || (num_paths && !radiance_dev))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  if (num_paths > OR3_NOALLOC_MAX_PATHS)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "num_paths %u exceeds the no-alloc scratch limit of %u paths",
+                num_paths, OR3_NOALLOC_MAX_PATHS);
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  if (cam->width == 0 || cam->height == 0 || prm->supersamples < 1 || prm->supersamples > 256 ||
+      prm->min_samples < 1 || prm->max_samples < prm->min_samples || prm->step_samples < 1)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "invalid camera or sample schedule");
+  if (num_paths == 0) return OR3_OK;
+  const uint64_t ss2 = (uint64_t)prm->supersamples * prm->supersamples;
+  const uint64_t per_sample = (uint64_t)cam->width * cam->height * ss2;
+  const uint64_t total = per_sample * (uint64_t)prm->max_samples;
+  if (first + num_paths > total)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "paths [%llu, +%u) outside the %llu paths of the render",
+                (unsigned long long)first, num_paths, (unsigned long long)total);
+  // the pass [prev, next) holding the first path; the range must not leave it
+  const uint64_t s0 = first / per_sample, s1 = (first + num_paths - 1) / per_sample;
+  int32_t prev = 0, next = prm->min_samples;
+  while ((uint64_t)next <= s0 && next + prm->step_samples <= prm->max_samples) {
+    prev = next;
+    next += prm->step_samples;
+  }
+  if (s1 >= (uint64_t)next) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "path range spans two passes");
+  RenderConst rc{};
+  camera_basis(cam, rc.cam);
+  rc.W = cam->width;
+  rc.H = cam->height;
+  rc.ss = (uint32_t)prm->supersamples;
+  rc.ss2 = (uint32_t)ss2;
+  rc.nee = prm->next_event_estimation;
+  rc.rr_min_depth = prm->rr_min_depth;
+  rc.max_depth = prm->max_depth;
+  rc.seed_lo = (uint32_t)prm->seed;
+  rc.seed_hi = (uint32_t)(prm->seed >> 32);
+  cudaSetDevice(ctx->device);
+  std::string err;
+  const int rcode = render_paths_noalloc(it->second->view, it->second->has_split, rc, first, num_paths,
+                                         (uint32_t)prev, ctx->device, ctx->num_sms * ctx->occ_extend,
+                                         ctx->num_sms * ctx->occ_shade, radiance_dev,
+                                         stream ? (cudaStream_t)stream : ctx->stream, &err);
+  if (rcode != OR3_OK) return fail(ctx, rcode, "%s", err.c_str());
+  return OR3_OK;
+}
+
 int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *o, const float *d,
                        const float *tmax, uint8_t *occ) {
   if (!ctx || (n && (!o || !d || !tmax || !occ))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");

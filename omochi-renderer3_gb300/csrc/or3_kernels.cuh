@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "or3_device.cuh"
 
 namespace or3 {
@@ -78,6 +80,11 @@ void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const 
                           float *t, float *normal, uint32_t *err, cudaStream_t st);
 void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
                            const float *tmax, uint8_t *occ, uint32_t *err, cudaStream_t st);
+
+// or3_noalloc.cu: the bounce loop on the static scratch array
+int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &rc, uint64_t first,
+                         uint32_t num_paths, uint32_t pass_first, int device, int grid_ext, int grid_sh,
+                         float *out, cudaStream_t st, std::string *err);
 
 // kernel handles for occupancy queries
 const void *kernel_extend_ptr();

@@ -69,10 +69,9 @@ class Context:
         return {k: getattr(info, k) for k, _ in abi.SceneInfoC._fields_}
 
     # ---- render
-    def render(self, scene, camera, *, supersamples=1, min_samples=1, max_samples=1, step_samples=1,
-               next_event_estimation=False, rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE,
-               seed=0, wave_paths=0, flags=0, callback=None):
-        cam = camera.to_c()
+    @staticmethod
+    def _params(supersamples=1, min_samples=1, max_samples=1, step_samples=1, next_event_estimation=False,
+                rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE, seed=0, wave_paths=0, flags=0):
         p = abi.RenderParamsC()
         p.min_samples, p.max_samples, p.step_samples = min_samples, max_samples, step_samples
         p.supersamples = supersamples
@@ -80,6 +79,23 @@ class Context:
         p.rr_min_depth, p.max_depth = rr_min_depth, max_depth
         p.output_layout = layout
         p.seed, p.wave_paths, p.flags = seed, wave_paths, flags
+        return p
+
+    def render_paths_noalloc(self, scene, camera, first_path, num_paths, radiance_dev_ptr, stream=None,
+                             **settings):
+        """or3_render_paths_noalloc: radiance of paths [first, first+num) into a caller-owned device buffer."""
+        cam = camera.to_c()
+        p = self._params(**settings)
+        self._check(self.lib.or3_render_paths_noalloc(self.h, scene, ctypes.byref(cam), ctypes.byref(p),
+                                                      first_path, num_paths, ctypes.c_void_p(radiance_dev_ptr),
+                                                      ctypes.c_void_p(stream)))
+
+    def render(self, scene, camera, *, supersamples=1, min_samples=1, max_samples=1, step_samples=1,
+               next_event_estimation=False, rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE,
+               seed=0, wave_paths=0, flags=0, callback=None):
+        cam = camera.to_c()
+        p = self._params(supersamples, min_samples, max_samples, step_samples, next_event_estimation,
+                         rr_min_depth, max_depth, layout, seed, wave_paths, flags)
         if callback is not None:
             def _cb(user, samples, rgb, w, h, minutes):
                 img = np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy()

@@ -155,8 +155,12 @@ typedef struct or3_render_params {
   uint64_t seed;         /* counter-based RNG key */
   uint64_t wave_paths;   /* camera paths per wave, 0 = automatic */
   uint32_t flags;        /* OR3_FLAG_* */
-  uint32_t reserved;
+  uint32_t tuning;       /* 0 = defaults; OR3_TUNE_* (kernel choices, set by the autotuner) */
 } or3_render_params;
+
+#define OR3_TUNE_EXTEND_MASK 0x7u  /* extend kernel: 0 default (= 2); 1 persistent, one node or leaf per step;
+                                      2 persistent, node steps with leaves in place; 3 one ray per thread */
+#define OR3_TUNE_SMEM_NODES 0x10u  /* stage the top BVH nodes in shared memory */
 
 /* Called after each pass, like PathTracer's RenderingFinishCallbackFunction
    (src/renderer/PathTracer.h:21): samples so far, the frame in the requested

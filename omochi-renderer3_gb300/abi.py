@@ -73,7 +73,7 @@ class RenderParamsC(ctypes.Structure):
                 ("next_event_estimation", ctypes.c_int32), ("rr_min_depth", ctypes.c_int32),
                 ("max_depth", ctypes.c_int32), ("output_layout", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("wave_paths", ctypes.c_uint64),
-                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("tuning", ctypes.c_uint32)]
 
 
 class RenderStatsC(ctypes.Structure):

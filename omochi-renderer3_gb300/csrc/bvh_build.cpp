@@ -275,32 +275,38 @@ struct Collapser {
     }
   }
 
-  // Emits the wide node for binary node `root` at index `slot`.
-  void emit(int root, uint32_t slot, int depth) {
-    max_depth = std::max(max_depth, depth);
+  // Emits the wide nodes breadth first from binary node 0 into slot 0, so the
+  // top levels are contiguous (the kernels stage the first nodes in shared
+  // memory).
+  void emit_all() {
+    struct Item { int root; uint32_t slot; int depth; };
+    std::vector<Item> fifo;
+    fifo.push_back({0, 0, 1});
     std::vector<int> kids;
-    gather(root, kids);
-    WideNode w;
-    std::memset(&w, 0, sizeof(w));
-    AABB boxes[4];
-    for (size_t i = 0; i < kids.size(); i++) boxes[i] = bn[kids[i]].box;
-    quantise(w, bn[root].box, boxes, (int)kids.size());
-    std::vector<std::pair<int, uint32_t>> internal;
-    for (size_t i = 0; i < kids.size(); i++) {
-      const BNode &k = bn[kids[i]];
-      if (k.leaf()) {
-        w.child[i] = k.first;
-        w.count[i] = (uint8_t)k.count;  // total for now; split by kind below
-      } else {
-        const uint32_t c = (uint32_t)out.size();
-        out.push_back(WideNode());
-        w.child[i] = c;
-        w.imask |= (uint8_t)(1u << i);
-        internal.push_back({kids[i], c});
+    for (size_t head = 0; head < fifo.size(); head++) {
+      const Item it = fifo[head];
+      max_depth = std::max(max_depth, it.depth);
+      gather(it.root, kids);
+      WideNode w;
+      std::memset(&w, 0, sizeof(w));
+      AABB boxes[4];
+      for (size_t i = 0; i < kids.size(); i++) boxes[i] = bn[kids[i]].box;
+      quantise(w, bn[it.root].box, boxes, (int)kids.size());
+      for (size_t i = 0; i < kids.size(); i++) {
+        const BNode &k = bn[kids[i]];
+        if (k.leaf()) {
+          w.child[i] = k.first;
+          w.count[i] = (uint8_t)k.count;  // total for now; split by kind below
+        } else {
+          const uint32_t c = (uint32_t)out.size();
+          out.push_back(WideNode());
+          w.child[i] = c;
+          w.imask |= (uint8_t)(1u << i);
+          fifo.push_back({kids[i], c, it.depth + 1});
+        }
       }
+      out[it.slot] = w;
     }
-    out[slot] = w;
-    for (auto &p : internal) emit(p.first, p.second, depth + 1);
   }
 };
 
@@ -361,7 +367,7 @@ bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max,
       out.nodes[0] = w;
       c.max_depth = 1;
     } else {
-      c.emit(0, 0, 1);
+      c.emit_all();
     }
     out.wide_depth = c.max_depth;
     if (out.wide_depth <= kMaxBinaryDepth / 2) break;

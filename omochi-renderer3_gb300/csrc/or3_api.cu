@@ -257,6 +257,7 @@ int or3_context_create(int device, or3_context **out) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_shade, kernel_shade_ptr(), 256, 0);
   ctx->occ_extend = std::max(ctx->occ_extend, 1);
   ctx->occ_shade = std::max(ctx->occ_shade, 1);
+  set_query_grid(ctx->num_sms * ctx->occ_extend);
   if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMallocHost(&ctx->host_counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
@@ -572,7 +573,11 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const uint32_t W = cam->width, H = cam->height, ss = (uint32_t)prm->supersamples, ss2 = ss * ss;
   const uint64_t npix = (uint64_t)W * H;
   const uint64_t paths_per_sample = npix * ss2;
-  uint64_t wave = prm->wave_paths ? prm->wave_paths : (1ull << 22);
+  // Default waves: 2^25 camera paths (2^23 when glass can split paths, whose
+  // queues need 8x capacity).  Fewer, larger waves mean fewer bounce
+  // iterations and kernel tails (measured on the mesh workload: 4M-path waves
+  // 1007 Mpaths/s, 32M-path waves 1285).
+  uint64_t wave = prm->wave_paths ? prm->wave_paths : (sg->has_split ? (1ull << 23) : (1ull << 25));
   wave = std::max<uint64_t>(wave, ss2);
   wave = std::min<uint64_t>(wave, 1ull << 30);
   // Waves: whole samples of the full image when one fits, else row chunks of one sample.
@@ -612,7 +617,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const int block = 256;
   const int grid_ext = ctx->num_sms * ctx->occ_extend;
   const int grid_sh = ctx->num_sms * ctx->occ_shade;
-  const int smem_nodes = (int)std::min<uint64_t>(256, sg->view.num_nodes);
+  const int smem_nodes =
+      (prm->tuning & OR3_TUNE_SMEM_NODES) ? (int)std::min<uint64_t>(256, sg->view.num_nodes) : 0;
+  const int variant = extend_variant(prm->tuning);
   const bool timek = (prm->flags & OR3_FLAG_TIME_KERNELS) != 0;
   const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
 
@@ -643,7 +650,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         uint32_t count = w.num_paths;
         for (int bounce = 0; count > 0; bounce++) {
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[0], st));
-          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, st);
+          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
@@ -789,7 +796,7 @@ int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const fl
   if (n == 0) return OR3_OK;
   cudaSetDevice(ctx->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  launch_trace_closest(it->second->view, n, o, d, prim, t, normal, ctx->counters + 2, st);
+  launch_trace_closest(it->second->view, n, o, d, prim, t, normal, ctx->counters, st);
   OR3_CUDA(ctx, cudaGetLastError());
   return OR3_OK;
 }
@@ -885,7 +892,7 @@ int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *o
   cudaMemcpyAsync(od, o, 3 * n * 4, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(dd, d, 3 * n * 4, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(tm, tmax, n * 4, cudaMemcpyHostToDevice, st);
-  launch_trace_occluded(it->second->view, n, od, dd, tm, oc, ctx->counters + 2, st);
+  launch_trace_occluded(it->second->view, n, od, dd, tm, oc, ctx->counters, st);
   cudaMemcpyAsync(occ, oc, n, cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(buf);

@@ -170,6 +170,303 @@ __device__ __forceinline__ float safe_inv(float x) {
   return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x));
 }
 
+// ---------------------------------------------------------------- stepped traversal
+// Traversal as a per-lane state machine, one unit of work per step: either
+// one 64-byte node (4 boxes) or one leaf (<= 4 primitives).  Leaf children are
+// ordered with internal children by entry distance and go through the same
+// stack, so a step never runs a variable-length leaf loop inside a node test
+// and lanes of a warp stay on the same branch more often.  The persistent
+// kernels (or3_kernels.cu) refill a lane with a new ray the moment its ray
+// finishes.
+constexpr uint32_t kLeafEntry = 0x80000000u;   // entry = kLeafEntry | count << 23 | first record
+constexpr uint32_t kMaxLeafFirst = 1u << 23;   // records addressable by a leaf entry
+constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
+
+struct TravState {
+  V3 o, d;
+  V3 inv, oi;
+  uint32_t signs;  // bit a: inv[a] < 0
+  float tmax;      // best distance so far (or the any-hit limit)
+  uint32_t rec;
+  float u, v;
+  uint32_t entry;
+  int sp;
+};
+
+__device__ __forceinline__ void trav_init(TravState &s, V3 o, V3 d, float tmax, uint32_t num_nodes) {
+  s.o = o;
+  s.d = d;
+  s.inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+  s.oi = v3(-o.x * s.inv.x, -o.y * s.inv.y, -o.z * s.inv.z);
+  s.signs = (s.inv.x < 0.f ? 1u : 0u) | (s.inv.y < 0.f ? 2u : 0u) | (s.inv.z < 0.f ? 4u : 0u);
+  s.tmax = tmax;
+  s.rec = kMissRec;
+  s.u = s.v = 0.f;
+  s.entry = num_nodes > 0 ? 0u : kNoEntry;
+  s.sp = 0;
+}
+
+// Pops the nearest pending entry that can still hold a closer hit; false when none.
+__device__ __forceinline__ bool trav_pop(TravState &s, const uint32_t *stk_e, const float *stk_t) {
+  while (s.sp > 0) {
+    s.sp--;
+    if (stk_t[s.sp] <= s.tmax * 1.0000010f) {
+      s.entry = stk_e[s.sp];
+      return true;
+    }
+  }
+  s.entry = kNoEntry;
+  return false;
+}
+
+// One step.  Returns true when the traversal of the BVH is over (the
+// not-in-BVH list is then tested by trav_finish).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &s, uint32_t *stk_e, float *stk_t,
+                                          const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
+  const uint32_t e = s.entry;
+  if (e == kNoEntry) return true;
+  if (!(e & kLeafEntry)) {
+    uint4 n0, n1, n2, n3;
+    if (COUNT) cnt[0]++;
+    if (e < ns) {
+      n0 = snodes[4 * e + 0];
+      n1 = snodes[4 * e + 1];
+      n2 = snodes[4 * e + 2];
+      n3 = snodes[4 * e + 3];
+    } else {
+      const uint4 *np = S.nodes + 4 * (size_t)e;
+      n0 = __ldg(np + 0);
+      n1 = __ldg(np + 1);
+      n2 = __ldg(np + 2);
+      n3 = __ldg(np + 3);
+    }
+    const uint32_t ew = n0.w;
+    const float ax = __uint_as_float((ew & 0xFFu) << 23) * s.inv.x;
+    const float ay = __uint_as_float(((ew >> 8) & 0xFFu) << 23) * s.inv.y;
+    const float az = __uint_as_float(((ew >> 16) & 0xFFu) << 23) * s.inv.z;
+    const uint32_t imask = ew >> 24;
+    const float bx = fmaf(__uint_as_float(n0.x), s.inv.x, s.oi.x);
+    const float by = fmaf(__uint_as_float(n0.y), s.inv.y, s.oi.y);
+    const float bz = fmaf(__uint_as_float(n0.z), s.inv.z, s.oi.z);
+    // byte words: lo x,y,z = n1.x,n1.y,n1.z ; hi x,y,z = n1.w,n2.x,n2.y
+    const uint32_t wnx = (s.signs & 1u) ? n1.w : n1.x, wfx = (s.signs & 1u) ? n1.x : n1.w;
+    const uint32_t wny = (s.signs & 2u) ? n2.x : n1.y, wfy = (s.signs & 2u) ? n1.y : n2.x;
+    const uint32_t wnz = (s.signs & 4u) ? n2.y : n1.z, wfz = (s.signs & 4u) ? n1.z : n2.y;
+    const uint32_t counts = n3.z;
+    const float tlimit = s.tmax * 1.0000010f;
+    float key[4];
+    uint32_t kid[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const float tnx = fmaf(qbyte(wnx, i), ax, bx), tfx = fmaf(qbyte(wfx, i), ax, bx);
+      const float tny = fmaf(qbyte(wny, i), ay, by), tfy = fmaf(qbyte(wfy, i), ay, by);
+      const float tnz = fmaf(qbyte(wnz, i), az, bz), tfz = fmaf(qbyte(wfz, i), az, bz);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+      const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
+      const bool internal = (imask >> i) & 1u;
+      const uint32_t c = (counts >> (8 * i)) & 0xFFu;
+      const uint32_t ch = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
+      const bool valid = internal || c != 0u;
+      key[i] = (valid && tn <= tf && tn <= tlimit) ? tn : kInf * 2.f;
+      kid[i] = internal ? ch : (kLeafEntry | (c << 23) | ch);
+    }
+#define OR3_CSWAP(a, b)                                       \
+  if (key[b] < key[a]) {                                      \
+    const float tk = key[a]; key[a] = key[b]; key[b] = tk;     \
+    const uint32_t tc = kid[a]; kid[a] = kid[b]; kid[b] = tc;  \
+  }
+    OR3_CSWAP(0, 1) OR3_CSWAP(2, 3) OR3_CSWAP(0, 2) OR3_CSWAP(1, 3) OR3_CSWAP(1, 2)
+#undef OR3_CSWAP
+    const float inf2 = kInf * 2.f;
+    if (key[0] < inf2) {
+#pragma unroll
+      for (int j = 3; j >= 1; j--) {
+        if (key[j] < inf2) {
+          if (s.sp < kStackSize) {
+            stk_e[s.sp] = kid[j];
+            stk_t[s.sp] = key[j];
+            s.sp++;
+          } else {
+            atomicOr(err, 1u);  // not reachable: the builder bounds the tree depth
+          }
+        }
+      }
+      s.entry = kid[0];
+      return false;
+    }
+    return !trav_pop(s, stk_e, stk_t);
+  }
+  // leaf: triangles then spheres
+  const uint32_t first = e & (kMaxLeafFirst - 1u);
+  const uint32_t c = (e >> 23) & 0xFFu;
+  const uint32_t ntri = c & 15u, nsph = c >> 4;
+  if (COUNT) {
+    cnt[1] += ntri;
+    cnt[2] += nsph;
+  }
+  for (uint32_t k = 0; k < ntri; k++) {
+    const float4 *pr = S.prims + 3 * (size_t)(first + k);
+    const float4 a = __ldg(pr), b = __ldg(pr + 1), cc = __ldg(pr + 2);
+    float t, u, v;
+    if (isect_triangle(a, b, cc, s.o, s.d, s.tmax, t, u, v)) {
+      s.tmax = t;
+      s.rec = first + k;
+      s.u = u;
+      s.v = v;
+    }
+  }
+  for (uint32_t k = ntri; k < ntri + nsph; k++) {
+    const float4 a = __ldg(S.prims + 3 * (size_t)(first + k));
+    float t;
+    if (isect_sphere(a, s.o, s.d, s.tmax, t)) {
+      s.tmax = t;
+      s.rec = first + k;
+      s.u = s.v = 0.f;
+    }
+  }
+  if (ANY && s.rec != kMissRec) return true;
+  return !trav_pop(s, stk_e, stk_t);
+}
+
+// Tests the primitives of one leaf slot (triangles then spheres).
+template <bool COUNT>
+__device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint32_t first, uint32_t c,
+                                          uint32_t *cnt) {
+  const uint32_t ntri = c & 15u, nsph = c >> 4;
+  if (COUNT) {
+    cnt[1] += ntri;
+    cnt[2] += nsph;
+  }
+  for (uint32_t k = 0; k < ntri; k++) {
+    const float4 *pr = S.prims + 3 * (size_t)(first + k);
+    const float4 a = __ldg(pr), b = __ldg(pr + 1), cc = __ldg(pr + 2);
+    float t, u, v;
+    if (isect_triangle(a, b, cc, s.o, s.d, s.tmax, t, u, v)) {
+      s.tmax = t;
+      s.rec = first + k;
+      s.u = u;
+      s.v = v;
+    }
+  }
+  for (uint32_t k = ntri; k < ntri + nsph; k++) {
+    const float4 a = __ldg(S.prims + 3 * (size_t)(first + k));
+    float t;
+    if (isect_sphere(a, s.o, s.d, s.tmax, t)) {
+      s.tmax = t;
+      s.rec = first + k;
+      s.u = s.v = 0.f;
+    }
+  }
+}
+
+// One node per step; the node's hit leaf children are tested right away and
+// only internal children go through the stack (stack entries are node indices).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, uint32_t *stk_e, float *stk_t,
+                                                 const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
+  const uint32_t e = s.entry;
+  if (e == kNoEntry) return true;
+  uint4 n0, n1, n2, n3;
+  if (COUNT) cnt[0]++;
+  if (e < ns) {
+    n0 = snodes[4 * e + 0];
+    n1 = snodes[4 * e + 1];
+    n2 = snodes[4 * e + 2];
+    n3 = snodes[4 * e + 3];
+  } else {
+    const uint4 *np = S.nodes + 4 * (size_t)e;
+    n0 = __ldg(np + 0);
+    n1 = __ldg(np + 1);
+    n2 = __ldg(np + 2);
+    n3 = __ldg(np + 3);
+  }
+  const uint32_t ew = n0.w;
+  const float ax = __uint_as_float((ew & 0xFFu) << 23) * s.inv.x;
+  const float ay = __uint_as_float(((ew >> 8) & 0xFFu) << 23) * s.inv.y;
+  const float az = __uint_as_float(((ew >> 16) & 0xFFu) << 23) * s.inv.z;
+  const uint32_t imask = ew >> 24;
+  const float bx = fmaf(__uint_as_float(n0.x), s.inv.x, s.oi.x);
+  const float by = fmaf(__uint_as_float(n0.y), s.inv.y, s.oi.y);
+  const float bz = fmaf(__uint_as_float(n0.z), s.inv.z, s.oi.z);
+  const uint32_t wnx = (s.signs & 1u) ? n1.w : n1.x, wfx = (s.signs & 1u) ? n1.x : n1.w;
+  const uint32_t wny = (s.signs & 2u) ? n2.x : n1.y, wfy = (s.signs & 2u) ? n1.y : n2.x;
+  const uint32_t wnz = (s.signs & 4u) ? n2.y : n1.z, wfz = (s.signs & 4u) ? n1.z : n2.y;
+  const uint32_t counts = n3.z;
+  const float tlimit = s.tmax * 1.0000010f;
+  float key[4];
+  uint32_t kid[4];
+  uint32_t leafmask = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float tnx = fmaf(qbyte(wnx, i), ax, bx), tfx = fmaf(qbyte(wfx, i), ax, bx);
+    const float tny = fmaf(qbyte(wny, i), ay, by), tfy = fmaf(qbyte(wfy, i), ay, by);
+    const float tnz = fmaf(qbyte(wnz, i), az, bz), tfz = fmaf(qbyte(wfz, i), az, bz);
+    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+    const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
+    const bool internal = (imask >> i) & 1u;
+    const uint32_t c = (counts >> (8 * i)) & 0xFFu;
+    const bool hitbox = tn <= tf && tn <= tlimit;
+    key[i] = (hitbox && internal) ? tn : kInf * 2.f;
+    kid[i] = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
+    if (hitbox && !internal && c != 0u) leafmask |= 1u << i;
+  }
+  while (leafmask) {
+    const uint32_t i = __ffs(leafmask) - 1;
+    leafmask &= leafmask - 1;
+    const uint32_t first = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
+    trav_leaf<COUNT>(S, s, first, (counts >> (8 * i)) & 0xFFu, cnt);
+  }
+  if (ANY && s.rec != kMissRec) return true;
+#define OR3_CSWAP(a, b)                                       \
+  if (key[b] < key[a]) {                                      \
+    const float tk = key[a]; key[a] = key[b]; key[b] = tk;     \
+    const uint32_t tc = kid[a]; kid[a] = kid[b]; kid[b] = tc;  \
+  }
+  OR3_CSWAP(0, 1) OR3_CSWAP(2, 3) OR3_CSWAP(0, 2) OR3_CSWAP(1, 3) OR3_CSWAP(1, 2)
+#undef OR3_CSWAP
+  const float inf2 = kInf * 2.f;
+  const float tl2 = s.tmax * 1.0000010f;
+  if (key[0] < inf2 && key[0] <= tl2) {
+#pragma unroll
+    for (int j = 3; j >= 1; j--) {
+      if (key[j] < inf2 && key[j] <= tl2) {
+        if (s.sp < kStackSize) {
+          stk_e[s.sp] = kid[j];
+          stk_t[s.sp] = key[j];
+          s.sp++;
+        } else {
+          atomicOr(err, 1u);
+        }
+      }
+    }
+    s.entry = kid[0];
+    return false;
+  }
+  return !trav_pop(s, stk_e, stk_t);
+}
+
+// After the BVH: the not-in-BVH objects, strictly closer only (Scene.cpp:73-83).
+template <bool ANY>
+__device__ __forceinline__ Hit trav_finish(const DevScene &S, const TravState &s) {
+  Hit h;
+  h.t = s.tmax;
+  h.rec = s.rec;
+  h.u = s.u;
+  h.v = s.v;
+  if (ANY && h.rec != kMissRec) return h;
+  for (uint32_t p = 0; p < S.num_planes; p++) {
+    float t;
+    if (isect_plane(S.planes[p], s.o, s.d, h.t, t)) {
+      h.t = t;
+      h.rec = kPlaneBit | p;
+      h.u = h.v = 0.f;
+      if (ANY) return h;
+    }
+  }
+  return h;
+}
+
 // Closest hit (ANY = false) or first hit (ANY = true) against the wide BVH
 // and the not-in-BVH list.  Replaces Scene::CheckIntersection
 // (src/scenes/Scene.cpp:51-85), BVH::CheckIntersection (src/renderer/BVH.cpp:19-88)

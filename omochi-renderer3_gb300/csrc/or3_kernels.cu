@@ -60,7 +60,10 @@ __device__ __forceinline__ void camera_ray(const RenderConst &rc, uint32_t x, ui
 
 __global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) q.counters[out] = w.num_paths;
+  if (i == 0) {
+    q.counters[out] = w.num_paths;
+    q.counters[4 + out] = 0;  // extend fetch counter of this queue
+  }
   if (i >= w.num_paths) return;
   const uint64_t g = w.g_first + i;
   const uint32_t sub = (uint32_t)(g % rc.ss2);
@@ -77,29 +80,120 @@ __global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
 
 constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 
-// Closest hit for every queued ray.  COUNT adds the nodes, triangles and
-// spheres each ray touched to stats[3..5] (the algorithmic byte count).
-template <bool COUNT>
-__global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
-  __shared__ uint4 snodes[kSmemNodes * 4];
-  const uint32_t n = q.counters[in];
+// Persistent traversal over a ray source: every lane traces one ray at a time
+// and takes the next one the moment its ray is finished (warp-aggregated
+// fetch from a global counter that starts at zero), so no lane idles behind
+// the slowest ray of a fixed batch and the grid has no tail of its own.
+// All 32 lanes of every warp must enter (blockDim is a multiple of 32).
+// STEP 1: one node or one leaf per step (leaves go through the stack), refill
+//         any idle lane every step;
+// STEP 2: one node per step with its hit leaves tested in place, refill only
+//         once at least half of the warp is idle (amortises the atomic).
+template <bool ANY, bool COUNT, int STEP, class Src, class Sink>
+__device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
+                                                 const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
+                                                 uint32_t *err) {
+  uint32_t stk_e[kStackSize];
+  float stk_t[kStackSize];
+  TravState st;
+  uint32_t r = kNoEntry;
+  bool exhausted = false;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    const bool need = (r == kNoEntry) && !exhausted;
+    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    if (STEP == 2 && __popc(m) < 16 && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        if (idx < n) {
+          V3 o, d;
+          float tmax;
+          src.load(idx, o, d, tmax);
+          trav_init(st, o, d, tmax, S.num_nodes);
+          r = idx;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
+    if (r != kNoEntry) {
+      const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
+                                  : trav_step_inline<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err);
+      if (done) {
+        sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
+        r = kNoEntry;
+      }
+    }
+  }
+}
+
+struct QueueSrc {
+  const float4 *orig, *dir;
+  __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d, float &tmax) const {
+    o = ld3(orig[i]);
+    d = ld3(dir[i]);
+    tmax = kInf;
+  }
+};
+
+// The render keeps the FP32 distance: GB300 runs FP64 at a small fraction of
+// the FP32 rate, and one FP64 re-evaluation per ray cost more than the whole
+// traversal (measured: 2.7x slower extend).  The ray-query API refines.
+struct HitSink {
+  float4 *hits;
+  __device__ __forceinline__ void store(const DevScene &, uint32_t i, Hit h, V3, V3) const {
+    hits[i] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+  }
+};
+
+__device__ __forceinline__ uint32_t stage_nodes(const DevScene &S, uint4 *snodes, int smem_nodes) {
   const uint32_t ns = min((uint32_t)smem_nodes, S.num_nodes);
   if (ns > 0) {
     for (uint32_t k = threadIdx.x; k < ns * 4; k += blockDim.x) snodes[k] = S.nodes[k];
     __syncthreads();
   }
+  return ns;
+}
+
+// One thread per ray over a grid-stride loop; the whole traversal of a ray
+// (trace) runs in one go.
+template <bool ANY, bool COUNT, class Src, class Sink>
+__device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, const Src &src, const Sink &sink,
+                                                 const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    V3 o, d;
+    float tmax;
+    src.load(i, o, d, tmax);
+    const Hit h = trace<ANY, COUNT>(S, o, d, tmax, err, snodes, ns, cnt);
+    sink.store(S, i, h, o, d);
+  }
+}
+
+// Closest hit for every queued ray.  COUNT adds the nodes, triangles and
+// spheres each ray touched to stats[3..5] (the algorithmic byte count).
+// VARIANT 0: gridstride_trace; 1, 2: persistent_trace<STEP = VARIANT>.
+template <bool COUNT, int VARIANT>
+__global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
+  __shared__ uint4 snodes[kSmemNodes * 4];
+  const uint32_t n = q.counters[in];
+  const uint32_t ns = stage_nodes(S, snodes, smem_nodes);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&q.stats[0], (unsigned long long)n);
     if (n) atomicAdd(&q.stats[2], 1ull);
   }
-  const float4 *qo = q.orig[in];
-  const float4 *qd = q.dir[in];
   uint32_t cnt[3] = {0u, 0u, 0u};
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 ro = qo[i], rd = qd[i];
-    Hit h = trace<false, COUNT>(S, ld3(ro), ld3(rd), kInf, &q.counters[2], snodes, ns, cnt);
-    h.t = refine_t(S, h, ld3(ro), ld3(rd));
-    q.hits[i] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+  if (VARIANT == 0) {
+    gridstride_trace<false, COUNT>(S, n, QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
+                                   &q.counters[2]);
+  } else {
+    persistent_trace<false, COUNT, VARIANT == 1 ? 1 : 2>(S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]},
+                                                         HitSink{q.hits}, snodes, ns, cnt, &q.counters[2]);
   }
   if (COUNT) {
     unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
@@ -309,7 +403,11 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, RenderConst rc, Wave 
   }
 }
 
-__global__ void k_reset_count(uint32_t *counters, int which) { counters[which] = 0; }
+// Clears a consumed queue's length and its extend fetch counter.
+__global__ void k_reset_count(uint32_t *counters, int which) {
+  counters[which] = 0;
+  counters[4 + which] = 0;
+}
 
 // Per-pixel sums of the wave's path radiance: one warp per pixel, lanes over
 // the pixel's samples (coalesced), FP32 partials added into FP64 sums.
@@ -369,46 +467,66 @@ __global__ void k_moments(const double *sum, const double *sumsq, uint32_t W, ui
   }
 }
 
-__global__ void k_trace_closest(DevScene S, size_t n, const float *orig, const float *dir, int32_t *prim,
-                                float *tout, float *nout, uint32_t *err) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const V3 o = v3(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
-    const V3 d = v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
-    Hit h = trace<false>(S, o, d, kInf, err);
+// Ray-set queries run the render's own traversal (persistent_trace), so their
+// parity tests cover the extend kernel's code.
+struct ArraySrc {
+  const float *orig, *dir, *tmax;
+  __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d, float &tm) const {
+    o = v3(orig[3 * (size_t)i], orig[3 * (size_t)i + 1], orig[3 * (size_t)i + 2]);
+    d = v3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
+    tm = tmax ? tmax[i] : kInf;
+  }
+};
+
+struct QuerySink {
+  int32_t *prim;
+  float *tout, *nout;
+  __device__ __forceinline__ void store(const DevScene &S, uint32_t i, Hit h, V3 o, V3 d) const {
     h.t = refine_t(S, h, o, d);
     if (h.rec == kMissRec) {
       prim[i] = -1;
       tout[i] = kInf;
-      if (nout) nout[3 * i] = nout[3 * i + 1] = nout[3 * i + 2] = 0.f;
+      if (nout) nout[3 * (size_t)i] = nout[3 * (size_t)i + 1] = nout[3 * (size_t)i + 2] = 0.f;
     } else {
       const Surface s = surface_at(S, h, o, d);
       prim[i] = (int32_t)s.object_id;
       tout[i] = h.t;
       if (nout) {
-        nout[3 * i] = s.n.x;
-        nout[3 * i + 1] = s.n.y;
-        nout[3 * i + 2] = s.n.z;
+        nout[3 * (size_t)i] = s.n.x;
+        nout[3 * (size_t)i + 1] = s.n.y;
+        nout[3 * (size_t)i + 2] = s.n.z;
       }
     }
   }
-}
+};
 
-__global__ void k_trace_occluded(DevScene S, size_t n, const float *orig, const float *dir, const float *tmax,
-                                 uint8_t *occ, uint32_t *err) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const V3 o = v3(orig[3 * i], orig[3 * i + 1], orig[3 * i + 2]);
-    const V3 d = v3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
-    const Hit h = trace<true>(S, o, d, tmax[i], err);
+struct OccludedSink {
+  uint8_t *occ;
+  __device__ __forceinline__ void store(const DevScene &, uint32_t i, Hit h, V3, V3) const {
     occ[i] = h.rec != kMissRec ? 1 : 0;
   }
+};
+
+// counters[2] = error bits, counters[8] = fetch counter (zeroed by the launcher)
+__global__ void __launch_bounds__(256) k_trace_closest(DevScene S, uint32_t n, const float *orig, const float *dir,
+                                                       int32_t *prim, float *tout, float *nout, uint32_t *counters,
+                                                       int smem_nodes) {
+  __shared__ uint4 snodes[kSmemNodes * 4];
+  const uint32_t ns = stage_nodes(S, snodes, smem_nodes);
+  persistent_trace<false, false, 2>(S, n, &counters[8], ArraySrc{orig, dir, nullptr}, QuerySink{prim, tout, nout},
+                                    snodes, ns, nullptr, &counters[2]);
 }
 
-int grid_for(size_t n, int block) {
-  size_t g = (n + block - 1) / block;
-  if (g < 1) g = 1;
-  if (g > 152 * 64) g = 152 * 64;
-  return (int)g;
+__global__ void __launch_bounds__(256) k_trace_occluded(DevScene S, uint32_t n, const float *orig, const float *dir,
+                                                        const float *tmax, uint8_t *occ, uint32_t *counters,
+                                                        int smem_nodes) {
+  __shared__ uint4 snodes[kSmemNodes * 4];
+  const uint32_t ns = stage_nodes(S, snodes, smem_nodes);
+  persistent_trace<true, false, 2>(S, n, &counters[8], ArraySrc{orig, dir, tmax}, OccludedSink{occ}, snodes, ns,
+                                   nullptr, &counters[2]);
 }
+
+int g_query_grid = 152 * 4;
 
 }  // namespace
 
@@ -420,10 +538,16 @@ void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int ou
 }
 
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
-                   cudaStream_t st) {
+                   int variant, cudaStream_t st) {
   const int sn = smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes;
-  if (count) k_extend<true><<<grid, block, 0, st>>>(S, q, in, sn);
-  else k_extend<false><<<grid, block, 0, st>>>(S, q, in, sn);
+  switch ((count ? 8 : 0) | (variant & 7)) {
+    case 1: k_extend<false, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 8: k_extend<true, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 9: k_extend<true, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 10: k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    default: k_extend<false, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
+  }
 }
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
@@ -452,17 +576,31 @@ void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t
   k_moments<<<(n + 255) / 256, 256, 0, st>>>(sum, sumsq, W, H, so, qo);
 }
 
+void set_query_grid(int grid) { g_query_grid = grid > 0 ? grid : 1; }
+
 void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const float *dir, int32_t *prim,
-                          float *t, float *normal, uint32_t *err, cudaStream_t st) {
-  k_trace_closest<<<grid_for(n, 128), 128, 0, st>>>(S, n, orig, dir, prim, t, normal, err);
+                          float *t, float *normal, uint32_t *counters, cudaStream_t st) {
+  const int sn = 0;  // no shared-memory node staging by default (measured slower)
+  for (size_t b = 0; b < n; b += (size_t)1 << 30) {
+    const uint32_t m = (uint32_t)((n - b) < ((size_t)1 << 30) ? (n - b) : ((size_t)1 << 30));
+    cudaMemsetAsync(counters + 8, 0, sizeof(uint32_t), st);
+    k_trace_closest<<<g_query_grid, 256, 0, st>>>(S, m, orig + 3 * b, dir + 3 * b, prim + b, t + b,
+                                                  normal ? normal + 3 * b : nullptr, counters, sn);
+  }
 }
 
 void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
-                           const float *tmax, uint8_t *occ, uint32_t *err, cudaStream_t st) {
-  k_trace_occluded<<<grid_for(n, 128), 128, 0, st>>>(S, n, orig, dir, tmax, occ, err);
+                           const float *tmax, uint8_t *occ, uint32_t *counters, cudaStream_t st) {
+  const int sn = 0;  // no shared-memory node staging by default (measured slower)
+  for (size_t b = 0; b < n; b += (size_t)1 << 30) {
+    const uint32_t m = (uint32_t)((n - b) < ((size_t)1 << 30) ? (n - b) : ((size_t)1 << 30));
+    cudaMemsetAsync(counters + 8, 0, sizeof(uint32_t), st);
+    k_trace_occluded<<<g_query_grid, 256, 0, st>>>(S, m, orig + 3 * b, dir + 3 * b, tmax + b, occ + b, counters,
+                                                   sn);
+  }
 }
 
-const void *kernel_extend_ptr() { return (const void *)k_extend<false>; }
+const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }
 const void *kernel_shade_ptr() { return (const void *)k_shade; }
 
 }  // namespace or3

@@ -65,8 +65,15 @@ struct LaunchCfg {
 // host launchers (or3_kernels.cu)
 void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int out, int grid, int block,
                    cudaStream_t st);
+// variant: 0 one thread per ray over a grid-stride loop, 1 and 2 persistent
+// lane-refilled traversal (see persistent_trace)
+// Maps OR3_TUNE_EXTEND_MASK to a kernel variant (0 = default = 2, 3 = grid-stride).
+inline int extend_variant(uint32_t tuning) {
+  const uint32_t v = tuning & 0x7u;
+  return v == 0 ? 2 : v == 3 ? 0 : (int)v;
+}
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
-                   cudaStream_t st);
+                   int variant, cudaStream_t st);
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                   int grid, int block, cudaStream_t st);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
@@ -76,10 +83,12 @@ void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double 
                   cudaStream_t st);
 void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t H, double *sum_out,
                     double *sumsq_out, cudaStream_t st);
+// counters: the context's counter block ([2] error bits, [8] query fetch counter)
 void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const float *dir, int32_t *prim,
-                          float *t, float *normal, uint32_t *err, cudaStream_t st);
+                          float *t, float *normal, uint32_t *counters, cudaStream_t st);
 void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
-                           const float *tmax, uint8_t *occ, uint32_t *err, cudaStream_t st);
+                           const float *tmax, uint8_t *occ, uint32_t *counters, cudaStream_t st);
+void set_query_grid(int grid);
 
 // or3_noalloc.cu: the bounce loop on the static scratch array
 int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &rc, uint64_t first,

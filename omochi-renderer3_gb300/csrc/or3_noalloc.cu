@@ -103,7 +103,7 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
   int in = 0;
   uint32_t count = num_paths, errbits = 0;
   for (int bounce = 0; count > 0 && bounce < 1 << 20; bounce++) {
-    launch_extend(S, q, in, grid_ext, 256, (int)(S.num_nodes < 256 ? S.num_nodes : 256), false, st);
+    launch_extend(S, q, in, grid_ext, 256, 0, false, extend_variant(0), st);
     launch_shade(S, rc, w, q, in, grid_sh, 256, st);
     launch_reset_count(q, in, st);
     in ^= 1;

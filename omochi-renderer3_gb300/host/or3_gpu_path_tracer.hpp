@@ -45,7 +45,7 @@ class GpuPathTracer {
     params_.seed = 0;
     params_.wave_paths = 0;
     params_.flags = 0;
-    params_.reserved = 0;
+    params_.tuning = 0;
     status_ = or3_context_create(device, &ctx_);
     if (status_ != OR3_OK) report("cannot create a CUDA context");
   }

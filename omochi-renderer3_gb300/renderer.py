@@ -71,14 +71,15 @@ class Context:
     # ---- render
     @staticmethod
     def _params(supersamples=1, min_samples=1, max_samples=1, step_samples=1, next_event_estimation=False,
-                rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE, seed=0, wave_paths=0, flags=0):
+                rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE, seed=0, wave_paths=0, flags=0,
+                tuning=0):
         p = abi.RenderParamsC()
         p.min_samples, p.max_samples, p.step_samples = min_samples, max_samples, step_samples
         p.supersamples = supersamples
         p.next_event_estimation = 1 if next_event_estimation else 0
         p.rr_min_depth, p.max_depth = rr_min_depth, max_depth
         p.output_layout = layout
-        p.seed, p.wave_paths, p.flags = seed, wave_paths, flags
+        p.seed, p.wave_paths, p.flags, p.tuning = seed, wave_paths, flags, tuning
         return p
 
     def render_paths_noalloc(self, scene, camera, first_path, num_paths, radiance_dev_ptr, stream=None,
@@ -92,10 +93,10 @@ class Context:
 
     def render(self, scene, camera, *, supersamples=1, min_samples=1, max_samples=1, step_samples=1,
                next_event_estimation=False, rr_min_depth=5, max_depth=0, layout=abi.OR3_LAYOUT_REFERENCE,
-               seed=0, wave_paths=0, flags=0, callback=None):
+               seed=0, wave_paths=0, flags=0, tuning=0, callback=None):
         cam = camera.to_c()
         p = self._params(supersamples, min_samples, max_samples, step_samples, next_event_estimation,
-                         rr_min_depth, max_depth, layout, seed, wave_paths, flags)
+                         rr_min_depth, max_depth, layout, seed, wave_paths, flags, tuning)
         if callback is not None:
             def _cb(user, samples, rgb, w, h, minutes):
                 img = np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy()

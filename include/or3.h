@@ -248,6 +248,107 @@ int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const fl
 int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *origins_host,
                        const float *dirs_host, const float *tmax_host, uint8_t *occluded_host);
 
+/* ---- batched form (no counterpart in the reference) ----------------------
+ * Many renders ("jobs": scene, camera, sample budget) traced together: every
+ * wave of the wavefront holds camera paths of several jobs, so small jobs fill
+ * the GPU together instead of one after another.  A job's paths are numbered
+ * and seeded exactly as in or3_render with the same camera and params, so a
+ * job gives the same image alone or in a batch.  Scenes must be uploaded. */
+typedef struct or3_batch_job {
+  int32_t scene;
+  uint32_t reserved;
+  or3_camera camera;
+  or3_render_params params; /* supersamples, sample schedule, depth policy, seed, output layout */
+  double *frame_host;       /* final frame (params.output_layout), NULL = none */
+  size_t frame_capacity;    /* doubles */
+} or3_batch_job;
+
+typedef struct or3_batch_params {
+  uint64_t wave_paths;     /* camera paths per wave, 0 = automatic */
+  uint32_t flags;          /* OR3_FLAG_NO_GRAPH, OR3_FLAG_COUNT_TRAVERSAL */
+  uint32_t graph_bounces;  /* bounce iterations per graph launch, 0 = 8 */
+  uint32_t blocks_per_sm;  /* persistent kernel blocks per SM, 0 = occupancy limit */
+  uint32_t reserved;
+} or3_batch_params;
+
+int or3_render_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n_jobs,
+                     const or3_batch_params *params, or3_render_stats *stats_out);
+/* Per-pixel path-radiance sums of job `job` of the last batch (rows top-down,
+   W*H*3 doubles each, either may be NULL); count = paths per pixel. */
+int or3_get_batch_moments(or3_context *ctx, size_t job, double *sum_host, double *sumsq_host,
+                          size_t capacity, uint64_t *count_out);
+/* Autotuner: renders a reduced copy of the batch (every job's sample budget cut
+   so the copy holds about `sample_paths` camera paths) under candidate wave
+   sizes, graph depths and block counts, and writes the fastest to *best. */
+int or3_autotune_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n_jobs, uint64_t sample_paths,
+                       or3_batch_params *best, double *best_mpaths_out);
+
+/* ---- served form (no counterpart in the reference) -----------------------
+ * A request loop on its own host thread.  Jobs (or3_batch_job) are submitted
+ * from any thread; the loop admits them as slots and device memory free up
+ * (accumulation and frame buffers counted against hbm_budget_bytes), gives
+ * every admitted job a fair share of each wave so new work overlaps running
+ * work on the device, delivers a progressive frame every frame_every_samples
+ * samples and a final frame, and records latency from submission to the final
+ * frame.  Scenes stay resident (or3_scene_upload before submitting); while the
+ * server runs, no other call may use the context except the or3_server_*
+ * functions and or3_stop. */
+typedef struct or3_server_params {
+  uint64_t wave_paths;          /* camera paths per wave, 0 = automatic */
+  uint64_t hbm_budget_bytes;    /* admitted jobs' buffers, 0 = half of the free device memory */
+  uint32_t max_active_jobs;     /* 0 = 64 */
+  uint32_t frame_every_samples; /* progressive frame cadence, 0 = 16 */
+  uint32_t graph_bounces;       /* 0 = 8 */
+  uint32_t flags;               /* OR3_SERVER_KEEP_MOMENTS */
+} or3_server_params;
+
+#define OR3_SERVER_KEEP_MOMENTS 1u /* keep finished jobs' pixel sums on the host for or3_server_get_moments */
+
+/* frame of job `job_id`: samples so far, frame in the job's output layout,
+   final = 1 for the last one.  Called on the server thread. */
+typedef void (*or3_job_frame_callback)(void *user, uint64_t job_id, int32_t samples, const double *rgb,
+                                       size_t width, size_t height, int32_t final_frame);
+
+#define OR3_JOB_QUEUED 0
+#define OR3_JOB_RUNNING 1
+#define OR3_JOB_DONE 2
+#define OR3_JOB_CANCELLED 3
+#define OR3_JOB_FAILED 4
+
+typedef struct or3_job_status {
+  int32_t state;           /* OR3_JOB_* */
+  int32_t samples_done;
+  double submit_s;         /* seconds since the server started */
+  double admit_s;
+  double first_frame_s;
+  double done_s;
+} or3_job_status;
+
+typedef struct or3_server_stats {
+  uint64_t jobs_submitted, jobs_done, jobs_cancelled;
+  uint64_t camera_paths;
+  uint64_t waves;
+  double busy_s;           /* wall time with admitted work */
+  double device_ms;        /* device time of the waves (CUDA events) */
+  double latency_p50_s, latency_p99_s;   /* submit -> final frame, completed jobs */
+  double queue_p50_s, queue_p99_s;       /* submit -> admission */
+  double first_frame_p50_s;
+  uint64_t peak_active_jobs;
+  uint64_t peak_budget_bytes;
+} or3_server_stats;
+
+int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_frame_callback cb, void *user);
+int or3_server_submit(or3_context *ctx, const or3_batch_job *job, uint64_t *job_id_out);
+int or3_server_poll(or3_context *ctx, uint64_t job_id, or3_job_status *status_out);
+int or3_server_cancel(or3_context *ctx, uint64_t job_id);
+/* Blocks until every submitted job has finished, or timeout_s passes (OR3_ERR_BUSY). */
+int or3_server_drain(or3_context *ctx, double timeout_s);
+int or3_server_get_stats(or3_context *ctx, or3_server_stats *stats_out);
+/* Per-pixel sums of a finished job (kept until or3_server_stop). */
+int or3_server_get_moments(or3_context *ctx, uint64_t job_id, double *sum_host, double *sumsq_host,
+                           size_t capacity, uint64_t *count_out);
+int or3_server_stop(or3_context *ctx);
+
 /* ---- rendering without allocating (no counterpart in the reference) ------
  * For callers that must not allocate device memory while they render: code
  * running in a host callback enqueued on a CUDA stream (CUDA calls that

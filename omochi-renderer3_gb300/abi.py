@@ -96,6 +96,44 @@ class SceneInfoC(ctypes.Structure):
 FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, f64p, ctypes.c_size_t, ctypes.c_size_t,
                             ctypes.c_double)
 
+
+class BatchJobC(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_int32), ("reserved", ctypes.c_uint32), ("camera", CameraC),
+                ("params", RenderParamsC), ("frame_host", f64p), ("frame_capacity", ctypes.c_size_t)]
+
+
+class BatchParamsC(ctypes.Structure):
+    _fields_ = [("wave_paths", ctypes.c_uint64), ("flags", ctypes.c_uint32), ("graph_bounces", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class ServerParamsC(ctypes.Structure):
+    _fields_ = [("wave_paths", ctypes.c_uint64), ("hbm_budget_bytes", ctypes.c_uint64),
+                ("max_active_jobs", ctypes.c_uint32), ("frame_every_samples", ctypes.c_uint32),
+                ("graph_bounces", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+class JobStatusC(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("samples_done", ctypes.c_int32), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("first_frame_s", ctypes.c_double), ("done_s", ctypes.c_double)]
+
+
+class ServerStatsC(ctypes.Structure):
+    _fields_ = [("jobs_submitted", ctypes.c_uint64), ("jobs_done", ctypes.c_uint64),
+                ("jobs_cancelled", ctypes.c_uint64), ("camera_paths", ctypes.c_uint64), ("waves", ctypes.c_uint64),
+                ("busy_s", ctypes.c_double), ("device_ms", ctypes.c_double), ("latency_p50_s", ctypes.c_double),
+                ("latency_p99_s", ctypes.c_double), ("queue_p50_s", ctypes.c_double),
+                ("queue_p99_s", ctypes.c_double), ("first_frame_p50_s", ctypes.c_double),
+                ("peak_active_jobs", ctypes.c_uint64), ("peak_budget_bytes", ctypes.c_uint64)]
+
+
+JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, f64p, ctypes.c_size_t,
+                                ctypes.c_size_t, ctypes.c_int32)
+
+OR3_JOB_QUEUED, OR3_JOB_RUNNING, OR3_JOB_DONE, OR3_JOB_CANCELLED, OR3_JOB_FAILED = 0, 1, 2, 3, 4
+OR3_SERVER_KEEP_MOMENTS = 1
+OR3_TUNE_SMEM_NODES = 0x10
+
 # name -> (restype, argtypes); every function declared in include/or3.h
 PROTOTYPES = {
     "or3_api_version": (ctypes.c_int, []),
@@ -123,6 +161,21 @@ PROTOTYPES = {
     "or3_render_paths_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(CameraC), P(RenderParamsC),
                                                 ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "or3_render_batch": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), ctypes.c_size_t, P(BatchParamsC),
+                                        P(RenderStatsC)]),
+    "or3_get_batch_moments": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, f64p, f64p, ctypes.c_size_t,
+                                             P(ctypes.c_uint64)]),
+    "or3_autotune_batch": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), ctypes.c_size_t, ctypes.c_uint64,
+                                          P(BatchParamsC), P(ctypes.c_double)]),
+    "or3_server_start": (ctypes.c_int, [ctypes.c_void_p, P(ServerParamsC), JOB_FRAME_CB, ctypes.c_void_p]),
+    "or3_server_submit": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), P(ctypes.c_uint64)]),
+    "or3_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, P(JobStatusC)]),
+    "or3_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "or3_server_drain": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "or3_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(ServerStatsC)]),
+    "or3_server_get_moments": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, f64p, f64p, ctypes.c_size_t,
+                                              P(ctypes.c_uint64)]),
+    "or3_server_stop": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 OR3_NOALLOC_MAX_PATHS = 4096

@@ -17,9 +17,11 @@
 #include "bvh_build.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 namespace or3 {
 namespace {
@@ -95,6 +97,19 @@ struct Builder {
     return mid;
   }
 
+  struct Task { int node; uint32_t first, count; int depth; };
+  struct Scratch {
+    std::vector<AABB> binBox;
+    std::vector<uint32_t> binCnt;
+    std::vector<double> rightArea;
+    std::vector<uint32_t> rightCnt;
+    explicit Scratch(int bins) : binBox(3 * bins), binCnt(3 * bins), rightArea(bins), rightCnt(bins) {}
+  };
+
+  // Builds the tree.  The top of the tree is split serially, breadth first,
+  // until there are enough independent subtrees; those are then built on all
+  // host threads (each into its own node array, over its own disjoint range
+  // of the index array) and merged.  The tree is the same as a serial build's.
   void build() {
     const uint32_t n = (uint32_t)prims.size();
     idx.resize(n);
@@ -105,34 +120,180 @@ struct Builder {
     }
     nodes.reserve(2 * (size_t)n);
     nodes.push_back(BNode());
-    struct Task { int node; uint32_t first, count; int depth; };
-    std::vector<Task> stack;
-    stack.push_back({0, 0, n, 1});
-    std::vector<AABB> binBox(3 * bins);
-    std::vector<uint32_t> binCnt(3 * bins);
-    std::vector<double> rightArea(bins);
-    std::vector<uint32_t> rightCnt(bins);
-    while (!stack.empty()) {
-      Task t = stack.back();
-      stack.pop_back();
-      max_depth = std::max(max_depth, t.depth);
-      AABB box, cb;
-      for (uint32_t k = t.first; k < t.first + t.count; k++) {
-        box.grow(prim_box(idx[k]));
-        cb.grow(&cent[3 * idx[k]]);
+    unsigned threads = std::thread::hardware_concurrency();
+    threads = std::max(1u, std::min(threads, 64u));
+    host_threads = threads;  // large top nodes bin on all threads
+    Scratch sc(bins);
+    std::vector<Task> fifo;
+    fifo.push_back({0, 0, n, 1});
+    std::vector<Task> pending, kids;
+    size_t head = 0;
+    while (head < fifo.size() && fifo.size() - head < 4 * (size_t)threads) {
+      const Task t = fifo[head++];
+      if (t.count < 4096 || threads == 1) {
+        pending.push_back(t);
+        continue;
       }
+      kids.clear();
+      process(t, nodes, kids, sc, max_depth);
+      for (const Task &k : kids) fifo.push_back(k);
+    }
+    for (; head < fifo.size(); head++) pending.push_back(fifo[head]);
+
+    host_threads = 1;  // subtrees run one per thread
+    struct Local { std::vector<BNode> nodes; int maxd = 0; };
+    std::vector<Local> locals(pending.size());
+    std::atomic<size_t> next(0);
+    auto worker = [&]() {
+      Scratch wsc(bins);
+      std::vector<Task> st;
+      for (size_t i; (i = next.fetch_add(1)) < pending.size();) {
+        Local &L = locals[i];
+        L.nodes.push_back(BNode());
+        st.clear();
+        st.push_back({0, pending[i].first, pending[i].count, pending[i].depth});
+        while (!st.empty()) {
+          const Task t = st.back();
+          st.pop_back();
+          process(t, L.nodes, st, wsc, L.maxd);
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    const unsigned nt = (unsigned)std::min<size_t>(threads, pending.size());
+    for (unsigned k = 1; k < nt; k++) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
+
+    for (size_t i = 0; i < pending.size(); i++) {
+      Local &L = locals[i];
+      const int slot = pending[i].node;
+      const int base = (int)nodes.size() - 1;  // local index k >= 1 -> base + k
+      auto remap = [&](int k) { return k == 0 ? slot : base + k; };
+      for (size_t k = 1; k < L.nodes.size(); k++) {
+        BNode b = L.nodes[k];
+        if (!b.leaf()) {
+          b.left = remap(b.left);
+          b.right = remap(b.right);
+        }
+        nodes.push_back(b);
+      }
+      BNode r = L.nodes[0];
+      if (!r.leaf()) {
+        r.left = remap(r.left);
+        r.right = remap(r.right);
+      }
+      nodes[slot] = r;
+      max_depth = std::max(max_depth, L.maxd);
+    }
+  }
+
+  // Node bounds and centroid bounds of idx[first, first+count); large ranges
+  // are split over host threads.
+  void bounds(uint32_t first, uint32_t count, AABB &box, AABB &cb, unsigned threads) const {
+    const unsigned nt = count > (1u << 13) ? threads : 1u;
+    if (nt == 1) {
+      for (uint32_t i = first; i < first + count; i++) {
+        box.grow(prim_box(idx[i]));
+        cb.grow(&cent[3 * idx[i]]);
+      }
+      return;
+    }
+    std::vector<AABB> b(nt), c(nt);
+    auto run = [&](unsigned k) {
+      const uint32_t s = first + (uint32_t)((uint64_t)count * k / nt), e = first + (uint32_t)((uint64_t)count * (k + 1) / nt);
+      for (uint32_t i = s; i < e; i++) {
+        b[k].grow(prim_box(idx[i]));
+        c[k].grow(&cent[3 * idx[i]]);
+      }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < nt; k++) pool.emplace_back(run, k);
+    run(0);
+    for (auto &th : pool) th.join();
+    for (unsigned k = 0; k < nt; k++) {
+      box.grow(b[k]);
+      cb.grow(c[k]);
+    }
+  }
+
+  // Per-axis bin boxes and counts of idx[first, first+count) (all three axes
+  // in one pass; large ranges over host threads).
+  void bin_all(uint32_t first, uint32_t count, const AABB &cb, AABB *binBox, uint32_t *binCnt,
+               unsigned threads) const {
+    const unsigned nt = count > (1u << 13) ? threads : 1u;
+    float scale[3];
+    for (int a = 0; a < 3; a++) {
+      const float ext = cb.hi[a] - cb.lo[a];
+      scale[a] = ext > 0.f ? (float)bins / ext : 0.f;
+    }
+    auto bin_range = [&](uint32_t s, uint32_t e, AABB *bb, uint32_t *bc) {
+      for (uint32_t i = s; i < e; i++) {
+        const uint32_t p = idx[i];
+        const AABB pbox = prim_box(p);
+        for (int a = 0; a < 3; a++) {
+          int bi = (int)((cent[3 * p + a] - cb.lo[a]) * scale[a]);
+          bi = std::min(std::max(bi, 0), bins - 1);
+          bb[a * bins + bi].grow(pbox);
+          bc[a * bins + bi]++;
+        }
+      }
+    };
+    if (nt == 1) {
+      for (int j = 0; j < 3 * bins; j++) {
+        binBox[j] = AABB();
+        binCnt[j] = 0;
+      }
+      bin_range(first, first + count, binBox, binCnt);
+      return;
+    }
+    std::vector<AABB> pb((size_t)nt * 3 * bins);
+    std::vector<uint32_t> pc((size_t)nt * 3 * bins, 0);
+    auto run = [&](unsigned k) {
+      const uint32_t s = first + (uint32_t)((uint64_t)count * k / nt), e = first + (uint32_t)((uint64_t)count * (k + 1) / nt);
+      AABB *bb = &pb[(size_t)k * 3 * bins];
+      uint32_t *bc = &pc[(size_t)k * 3 * bins];
+      bin_range(s, e, bb, bc);
+    };
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < nt; k++) pool.emplace_back(run, k);
+    run(0);
+    for (auto &th : pool) th.join();
+    for (int j = 0; j < 3 * bins; j++) {
+      binBox[j] = AABB();
+      binCnt[j] = 0;
+      for (unsigned k = 0; k < nt; k++) {
+        binBox[j].grow(pb[(size_t)k * 3 * bins + j]);
+        binCnt[j] += pc[(size_t)k * 3 * bins + j];
+      }
+    }
+  }
+
+  unsigned host_threads = 1;
+
+  // One node: bounds, then leaf or split; children are allocated in `nodes`
+  // and pushed on `stack`.
+  void process(const Task &t, std::vector<BNode> &nodes, std::vector<Task> &stack, Scratch &sc, int &maxd) {
+    std::vector<AABB> &binBox = sc.binBox;
+    std::vector<uint32_t> &binCnt = sc.binCnt;
+    std::vector<double> &rightArea = sc.rightArea;
+    std::vector<uint32_t> &rightCnt = sc.rightCnt;
+    {
+      maxd = std::max(maxd, t.depth);
+      AABB box, cb;
+      bounds(t.first, t.count, box, cb, host_threads);
       BNode &nd = nodes[t.node];
       nd.box = box;
       nd.first = t.first;
       nd.count = t.count;
-      if (t.count <= 1) continue;
+      if (t.count <= 1) return;
 
       // Depth guard: finishing with median splits needs ceil(log2(count/leaf_max)) levels.
       const int need = ceil_log2((t.count + leaf_max - 1) / leaf_max);
       uint32_t split = 0;
       bool have = false;
       if (t.depth + need >= kMaxBinaryDepth) {
-        if (t.count <= (uint32_t)leaf_max) continue;
+        if (t.count <= (uint32_t)leaf_max) return;
         split = median_split(t.first, t.count, cb);
         have = true;
       } else {
@@ -140,20 +301,12 @@ struct Builder {
         const double parentArea = box.area();
         double bestCost = DBL_MAX;
         int bestAxis = -1, bestBin = -1;
+        bin_all(t.first, t.count, cb, binBox.data(), binCnt.data(), host_threads);
         for (int a = 0; a < 3; a++) {
           const float ext = cb.hi[a] - cb.lo[a];
           if (!(ext > 0.f)) continue;
-          const float scale = (float)bins / ext;
           AABB *bb = &binBox[a * bins];
           uint32_t *bc = &binCnt[a * bins];
-          for (int b = 0; b < bins; b++) { bb[b] = AABB(); bc[b] = 0; }
-          for (uint32_t k = t.first; k < t.first + t.count; k++) {
-            const uint32_t p = idx[k];
-            int b = (int)((cent[3 * p + a] - cb.lo[a]) * scale);
-            b = std::min(std::max(b, 0), bins - 1);
-            bb[b].grow(prim_box(p));
-            bc[b]++;
-          }
           AABB acc;
           uint32_t cnt = 0;
           for (int b = bins - 1; b > 0; b--) {
@@ -173,7 +326,7 @@ struct Builder {
             if (cost < bestCost) { bestCost = cost; bestAxis = a; bestBin = b; }
           }
         }
-        if (t.count <= (uint32_t)leaf_max && (bestAxis < 0 || (double)t.count <= bestCost)) continue;
+        if (t.count <= (uint32_t)leaf_max && (bestAxis < 0 || (double)t.count <= bestCost)) return;
         if (bestAxis < 0) {
           split = median_split(t.first, t.count, cb);
         } else {
@@ -190,7 +343,7 @@ struct Builder {
         }
         have = true;
       }
-      if (!have) continue;
+      if (!have) return;
       const int l = (int)nodes.size();
       nodes.push_back(BNode());
       nodes.push_back(BNode());
@@ -279,20 +432,22 @@ struct Collapser {
   // top levels are contiguous (the kernels stage the first nodes in shared
   // memory).
   void emit_all() {
-    struct Item { int root; uint32_t slot; int depth; };
+    // structure (serial, cheap): children and indices, breadth first
+    struct Item { int root; uint32_t slot; int depth; int kids[4]; int nkids; };
     std::vector<Item> fifo;
-    fifo.push_back({0, 0, 1});
+    fifo.push_back({0, 0, 1, {0, 0, 0, 0}, 0});
     std::vector<int> kids;
     for (size_t head = 0; head < fifo.size(); head++) {
-      const Item it = fifo[head];
+      Item &it = fifo[head];
       max_depth = std::max(max_depth, it.depth);
       gather(it.root, kids);
+      it.nkids = (int)kids.size();
+      const uint32_t slot = it.slot;
+      const int depth = it.depth;
       WideNode w;
       std::memset(&w, 0, sizeof(w));
-      AABB boxes[4];
-      for (size_t i = 0; i < kids.size(); i++) boxes[i] = bn[kids[i]].box;
-      quantise(w, bn[it.root].box, boxes, (int)kids.size());
       for (size_t i = 0; i < kids.size(); i++) {
+        fifo[head].kids[i] = kids[i];
         const BNode &k = bn[kids[i]];
         if (k.leaf()) {
           w.child[i] = k.first;
@@ -302,11 +457,31 @@ struct Collapser {
           out.push_back(WideNode());
           w.child[i] = c;
           w.imask |= (uint8_t)(1u << i);
-          fifo.push_back({kids[i], c, it.depth + 1});
+          fifo.push_back({kids[i], c, depth + 1, {0, 0, 0, 0}, 0});
         }
       }
-      out[it.slot] = w;
+      out[slot] = w;
     }
+    // quantised boxes (independent per node): all host threads
+    unsigned threads = std::thread::hardware_concurrency();
+    threads = std::max(1u, std::min(threads, 64u));
+    if (fifo.size() < 4096) threads = 1;
+    std::atomic<size_t> next(0);
+    auto worker = [&]() {
+      for (size_t b; (b = next.fetch_add(1024)) < fifo.size();) {
+        const size_t e = std::min(fifo.size(), b + 1024);
+        for (size_t i = b; i < e; i++) {
+          const Item &it = fifo[i];
+          AABB boxes[4];
+          for (int k = 0; k < it.nkids; k++) boxes[k] = bn[it.kids[k]].box;
+          quantise(out[it.slot], bn[it.root].box, boxes, it.nkids);
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < threads; k++) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
   }
 };
 

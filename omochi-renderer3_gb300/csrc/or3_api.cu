@@ -16,78 +16,12 @@
 
 #include "bvh_build.h"
 #include "or3.h"
+#include "or3_internal.h"
 #include "or3_kernels.cuh"
 
 using namespace or3;
 
 namespace {
-
-struct SceneGPU {
-  DevScene view{};
-  std::vector<void *> allocs;
-  or3_scene_info info{};
-  bool has_split = false;  // a refractive layer exists: paths can split at depth <= 2
-};
-
-}  // namespace
-
-struct or3_context {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  std::map<int32_t, SceneGPU *> scenes;
-  int32_t next_scene = 1;
-  int num_sms = 0;
-  int occ_extend = 1, occ_shade = 1;
-
-  // queues
-  size_t cap_rays = 0, cap_paths = 0;
-  float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
-  float4 *hits = nullptr, *pathL = nullptr;
-  uint32_t *counters = nullptr;
-  unsigned long long *dstats = nullptr;
-  uint32_t *host_counters = nullptr;  // pinned
-
-  // accumulation + frames
-  size_t cap_pixels = 0;
-  double *pix_sum = nullptr, *pix_sumsq = nullptr;
-  size_t cap_frame = 0;
-  double *frame_dev = nullptr, *frame_pinned = nullptr;
-  std::vector<double> frame_host;  // last completed frame (Renderer::GetResult)
-  std::mutex frame_mu;
-  int32_t frame_samples = 0;
-
-  std::atomic<bool> stop{false};
-  or3_render_stats last{};
-  uint32_t last_W = 0, last_H = 0;
-  uint64_t last_count = 0;  // paths per pixel in the moments
-  bool moments_valid = false;
-  uint64_t last_wave_paths = 0;
-  bool last_kept_paths = false;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
-};
-
-namespace {
-
-int fail(or3_context *ctx, int code, const char *fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(buf, sizeof(buf), fmt, ap);
-  va_end(ap);
-  if (ctx) ctx->err = buf;
-  return code;
-}
-
-#define OR3_CUDA(ctx, call)                                                                      \
-  do {                                                                                           \
-    cudaError_t e_ = (call);                                                                     \
-    if (e_ != cudaSuccess) {                                                                     \
-      return fail(ctx, e_ == cudaErrorMemoryAllocation ? OR3_ERR_OUT_OF_MEMORY : OR3_ERR_CUDA,   \
-                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);  \
-    }                                                                                            \
-  } while (0)
 
 template <class T>
 int dev_upload(or3_context *ctx, SceneGPU *sg, const std::vector<T> &v, const T **out) {
@@ -135,6 +69,10 @@ uint32_t layer_flags(const or3_scene_desc *d, const uint32_t *lay) {
   }
   return f;
 }
+
+}  // namespace
+
+namespace or3 {
 
 int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   if (paths <= ctx->cap_paths && rays <= ctx->cap_rays) return OR3_OK;
@@ -199,6 +137,32 @@ Queues make_queues(or3_context *ctx) {
 }
 
 // Camera::Camera (src/renderer/Camera.h:12-43) in double.
+int validate_render(or3_context *ctx, const or3_camera *cam, const or3_render_params *prm) {
+  if (cam->width == 0 || cam->height == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "empty image");
+  if ((uint64_t)cam->width * cam->height > (1ull << 28))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "image too large");
+  if (prm->supersamples < 1 || prm->supersamples > 256)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "supersamples must be in [1,256]");
+  if (prm->min_samples < 1 || prm->max_samples < prm->min_samples || prm->step_samples < 1)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sample schedule must satisfy 1 <= min <= max, step >= 1");
+  if (prm->output_layout != OR3_LAYOUT_REFERENCE && prm->output_layout != OR3_LAYOUT_COMPACT)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "unknown output layout");
+  return OR3_OK;
+}
+
+void fill_render_const(const or3_camera *cam, const or3_render_params *prm, RenderConst &rc) {
+  camera_basis(cam, rc.cam);
+  rc.W = cam->width;
+  rc.H = cam->height;
+  rc.ss = (uint32_t)prm->supersamples;
+  rc.ss2 = rc.ss * rc.ss;
+  rc.nee = prm->next_event_estimation;
+  rc.rr_min_depth = prm->rr_min_depth;
+  rc.max_depth = prm->max_depth;
+  rc.seed_lo = (uint32_t)prm->seed;
+  rc.seed_hi = (uint32_t)(prm->seed >> 32);
+}
+
 void camera_basis(const or3_camera *c, Camera32 &out) {
   double dir[3] = {c->direction[0], c->direction[1], c->direction[2]};
   double upv[3] = {c->up[0], c->up[1], c->up[2]};
@@ -275,6 +239,8 @@ int or3_context_destroy(or3_context *ctx) {
   if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  destroy_server_state(ctx);
+  destroy_batch_state(ctx);
   for (auto &kv : ctx->scenes) free_scene(kv.second);
   for (int k = 0; k < 2; k++) {
     cudaFree(ctx->qorig[k]);
@@ -559,15 +525,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   auto it = ctx->scenes.find(scene);
   if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
   SceneGPU *sg = it->second;
-  if (cam->width == 0 || cam->height == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "empty image");
-  if ((uint64_t)cam->width * cam->height > (1ull << 28))
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "image too large");
-  if (prm->supersamples < 1 || prm->supersamples > 256)
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "supersamples must be in [1,256]");
-  if (prm->min_samples < 1 || prm->max_samples < prm->min_samples || prm->step_samples < 1)
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sample schedule must satisfy 1 <= min <= max, step >= 1");
-  if (prm->output_layout != OR3_LAYOUT_REFERENCE && prm->output_layout != OR3_LAYOUT_COMPACT)
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "unknown output layout");
+  if (int v = validate_render(ctx, cam, prm)) return v;
   cudaSetDevice(ctx->device);
 
   const uint32_t W = cam->width, H = cam->height, ss = (uint32_t)prm->supersamples, ss2 = ss * ss;
@@ -595,16 +553,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   if ((rc = ensure_pixels(ctx, npix, frame_doubles))) return rc;
 
   RenderConst rcst{};
-  camera_basis(cam, rcst.cam);
-  rcst.W = W;
-  rcst.H = H;
-  rcst.ss = ss;
-  rcst.ss2 = ss2;
-  rcst.nee = prm->next_event_estimation;
-  rcst.rr_min_depth = prm->rr_min_depth;
-  rcst.max_depth = prm->max_depth;
-  rcst.seed_lo = (uint32_t)prm->seed;
-  rcst.seed_hi = (uint32_t)(prm->seed >> 32);
+  fill_render_const(cam, prm, rcst);
 
   cudaStream_t st = ctx->stream;
   OR3_CUDA(ctx, cudaMemsetAsync(ctx->pix_sum, 0, npix * 3 * sizeof(double), st));

@@ -1,0 +1,415 @@
+// or3_batch.cu -- the batched form: many renders in one wavefront.
+//
+// The reference renders one scene per RenderScene call
+// (src/renderer/PathTracer.cpp:55-85).  Small renders leave a GB300 mostly
+// idle: a 128x128, 16-spp job is 262k camera paths, a few bounce waves of
+// short kernels.  Here every job's path space (its samples in pass order,
+// pixels, sub-pixels) is cut into segments aligned to whole pixel-samples,
+// and a planner packs segments of all jobs into waves of up to `wave_paths`
+// camera paths.  Rays carry their segment index, so the multi-job kernels
+// (raygen/extend/shade/accumulate *_batch) pick scene, camera, depth policy and
+// RNG numbering per ray.  The bounce loop of a wave is a captured CUDA graph of
+// `graph_bounces` extend/shade/reset iterations, replayed until the wave's
+// queue is empty (one host round trip per replay instead of per kernel).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "or3_internal.h"
+
+namespace or3 {
+
+struct BatchBuffers {
+  double *sum = nullptr, *sumsq = nullptr;
+  size_t cap_pixels = 0, cap_sumsq = 0;
+  size_t cap_frame_pinned = 0;
+  DevScene *scenes = nullptr;
+  size_t cap_scenes = 0;
+  JobDev *jobs = nullptr;
+  size_t cap_jobs = 0;
+  Segment *segs = nullptr;
+  size_t cap_segs = 0;
+  WaveInfo *info = nullptr;
+  Segment *segs_host = nullptr;  // pinned staging
+  size_t cap_segs_host = 0;
+  WaveInfo *info_host = nullptr;  // pinned
+  double *frame_dev = nullptr, *frame_pinned = nullptr;
+  size_t cap_frame = 0;
+  struct JobOut {
+    uint64_t pix_base;
+    uint32_t W, H;
+    uint64_t count;  // paths per pixel
+  };
+  std::vector<JobOut> last;
+  bool valid = false;
+};
+
+void destroy_batch_state(or3_context *ctx) {
+  BatchBuffers *b = ctx->batch;
+  if (!b) return;
+  cudaFree(b->sum);
+  cudaFree(b->sumsq);
+  cudaFree(b->scenes);
+  cudaFree(b->jobs);
+  cudaFree(b->segs);
+  cudaFree(b->info);
+  cudaFreeHost(b->segs_host);
+  cudaFreeHost(b->info_host);
+  cudaFree(b->frame_dev);
+  cudaFreeHost(b->frame_pinned);
+  delete b;
+  ctx->batch = nullptr;
+}
+
+namespace {
+
+template <class T>
+int grow_dev(or3_context *ctx, T *&p, size_t &cap, size_t n) {
+  if (n <= cap && p) return OR3_OK;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  OR3_CUDA(ctx, cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  cap = std::max<size_t>(n, 1);
+  return OR3_OK;
+}
+
+template <class T>
+int grow_pinned(or3_context *ctx, T *&p, size_t &cap, size_t n) {
+  if (n <= cap && p) return OR3_OK;
+  cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  OR3_CUDA(ctx, cudaMallocHost(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  cap = std::max<size_t>(n, 1);
+  return OR3_OK;
+}
+
+struct JobPlan {
+  uint64_t per_sample;  // W*H*ss2
+  uint32_t ss2;
+  int32_t min_s, max_s, step;
+  int32_t samples;  // samples the schedule renders (its last pass end)
+};
+
+struct PlannedWave {
+  std::vector<Segment> segs;
+  uint32_t num_paths = 0;
+  uint32_t ngroups = 0;
+};
+
+// Cuts every job's passes into segments of whole pixel-samples and packs them
+// into waves of at most `cap` paths, jobs in order.
+void plan_waves(const std::vector<JobPlan> &jp, uint64_t cap, std::vector<PlannedWave> &waves) {
+  waves.clear();
+  PlannedWave cur;
+  auto flush = [&]() {
+    if (cur.num_paths) waves.push_back(cur);
+    cur = PlannedWave();
+  };
+  for (uint32_t j = 0; j < jp.size(); j++) {
+    const JobPlan &p = jp[j];
+    int32_t prev = 0;
+    for (int32_t next = p.min_s; next <= p.max_s; next += p.step) {
+      uint64_t g = (uint64_t)prev * p.per_sample;
+      const uint64_t end = (uint64_t)next * p.per_sample;
+      while (g < end) {
+        const uint64_t room = cap - cur.num_paths;
+        const uint64_t take = std::min<uint64_t>(end - g, room) / p.ss2 * p.ss2;
+        if (take == 0) {
+          flush();
+          continue;
+        }
+        Segment s{};
+        s.g_first = g;
+        s.job = j;
+        s.wave_first = cur.num_paths;
+        s.count = (uint32_t)take;
+        s.pass_first = (uint32_t)prev;
+        s.group_first = cur.ngroups;
+        cur.segs.push_back(s);
+        cur.num_paths += (uint32_t)take;
+        cur.ngroups += (uint32_t)(take / p.ss2);
+        g += take;
+      }
+      prev = next;
+    }
+  }
+  flush();
+}
+
+int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_batch_params *bp,
+              or3_render_stats *out, bool write_frames) {
+  if (!ctx || (n && !jobs)) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  if (n == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "empty batch");
+  if (n > (1u << 20)) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "too many jobs");
+  or3_batch_params defaults{};
+  if (!bp) bp = &defaults;
+  cudaSetDevice(ctx->device);
+  if (!ctx->batch) ctx->batch = new BatchBuffers();
+  BatchBuffers &B = *ctx->batch;
+  B.valid = false;
+
+  // scenes and jobs
+  std::map<int32_t, uint32_t> scene_index;
+  std::vector<DevScene> scenes;
+  bool split = false;
+  std::vector<JobDev> jd(n);
+  std::vector<JobPlan> jp(n);
+  std::vector<BatchBuffers::JobOut> outs(n);
+  uint64_t pixels = 0, total_paths = 0, max_ss2 = 1;
+  for (size_t j = 0; j < n; j++) {
+    const or3_batch_job &job = jobs[j];
+    auto it = ctx->scenes.find(job.scene);
+    if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "job %zu: scene %d not found", j, job.scene);
+    if (int v = validate_render(ctx, &job.camera, &job.params)) return v;
+    if (!scene_index.count(job.scene)) {
+      scene_index[job.scene] = (uint32_t)scenes.size();
+      scenes.push_back(it->second->view);
+      split = split || it->second->has_split;
+    }
+    fill_render_const(&job.camera, &job.params, jd[j].rc);
+    jd[j].scene = scene_index[job.scene];
+    const uint64_t npix = (uint64_t)job.camera.width * job.camera.height;
+    JobPlan &p = jp[j];
+    p.ss2 = jd[j].rc.ss2;
+    p.per_sample = npix * p.ss2;
+    p.min_s = job.params.min_samples;
+    p.max_s = job.params.max_samples;
+    p.step = job.params.step_samples;
+    p.samples = p.min_s + (p.max_s - p.min_s) / p.step * p.step;
+    outs[j] = {pixels, job.camera.width, job.camera.height, (uint64_t)p.samples * p.ss2};
+    pixels += npix;
+    total_paths += (uint64_t)p.samples * p.per_sample;
+    max_ss2 = std::max<uint64_t>(max_ss2, p.ss2);
+  }
+  uint64_t cap = bp->wave_paths ? bp->wave_paths : (split ? (1ull << 23) : (1ull << 25));
+  cap = std::max<uint64_t>(cap, max_ss2);
+  cap = std::min<uint64_t>(cap, 1ull << 30);
+  cap = std::min<uint64_t>(cap, std::max<uint64_t>(total_paths, max_ss2));
+  std::vector<PlannedWave> waves;
+  plan_waves(jp, cap, waves);
+  size_t max_segs = 1;
+  for (const PlannedWave &w : waves) max_segs = std::max(max_segs, w.segs.size());
+
+  // device state
+  int rc = ensure_queues(ctx, cap, cap * (split ? 8 : 1));
+  if (rc) return rc;
+  if ((rc = grow_dev(ctx, B.sum, B.cap_pixels, 3 * pixels))) return rc;
+  if ((rc = grow_dev(ctx, B.sumsq, B.cap_sumsq, 3 * pixels))) return rc;
+  if ((rc = grow_dev(ctx, B.scenes, B.cap_scenes, scenes.size()))) return rc;
+  if ((rc = grow_dev(ctx, B.jobs, B.cap_jobs, n))) return rc;
+  if ((rc = grow_dev(ctx, B.segs, B.cap_segs, max_segs))) return rc;
+  if ((rc = grow_pinned(ctx, B.segs_host, B.cap_segs_host, max_segs))) return rc;
+  if (!B.info) OR3_CUDA(ctx, cudaMalloc(&B.info, sizeof(WaveInfo)));
+  if (!B.info_host) OR3_CUDA(ctx, cudaMallocHost(&B.info_host, sizeof(WaveInfo)));
+  cudaStream_t st = ctx->stream;
+  for (size_t j = 0; j < n; j++) {
+    jd[j].sum = B.sum + 3 * outs[j].pix_base;
+    jd[j].sumsq = B.sumsq + 3 * outs[j].pix_base;
+  }
+  OR3_CUDA(ctx, cudaMemcpyAsync(B.scenes, scenes.data(), scenes.size() * sizeof(DevScene), cudaMemcpyHostToDevice, st));
+  OR3_CUDA(ctx, cudaMemcpyAsync(B.jobs, jd.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, st));
+  OR3_CUDA(ctx, cudaMemsetAsync(B.sum, 0, 3 * pixels * sizeof(double), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(B.sumsq, 0, 3 * pixels * sizeof(double), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->dstats, 0, 8 * sizeof(unsigned long long), st));
+
+  Batch b{B.scenes, B.jobs, B.segs, B.info};
+  const Queues q = make_queues(ctx);
+  const int bps_ext = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, ctx->occ_extend) : ctx->occ_extend;
+  const int bps_sh = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, ctx->occ_shade) : ctx->occ_shade;
+  const int grid_ext = ctx->num_sms * std::max(bps_ext, 1);
+  const int grid_sh = ctx->num_sms * std::max(bps_sh, 1);
+  const bool count = (bp->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
+  int unroll = bp->graph_bounces ? (int)bp->graph_bounces : 8;
+  unroll = std::max(2, std::min(unroll, 64));
+  unroll += unroll & 1;  // even: the live queue is queue 0 after every replay
+
+  // the bounce loop, captured once per call
+  cudaGraphExec_t gexec = nullptr;
+  const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
+  auto launch_bounces = [&]() {
+    for (int k = 0; k < unroll; k++) {
+      const int in = k & 1;
+      launch_extend_batch(b, q, in, grid_ext, count, st);
+      launch_shade_batch(b, q, in, grid_sh, st);
+      launch_reset_count(q, in, st);
+    }
+  };
+  if (use_graph) {
+    cudaGraph_t graph = nullptr;
+    OR3_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_bounces();
+    OR3_CUDA(ctx, cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  struct GraphGuard {
+    cudaGraphExec_t g;
+    ~GraphGuard() {
+      if (g) cudaGraphExecDestroy(g);
+    }
+  } guard{gexec};
+
+  or3_render_stats stats{};
+  OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  for (const PlannedWave &w : waves) {
+    std::memcpy(B.segs_host, w.segs.data(), w.segs.size() * sizeof(Segment));
+    B.info_host->nseg = (uint32_t)w.segs.size();
+    B.info_host->ngroups = w.ngroups;
+    B.info_host->num_paths = w.num_paths;
+    OR3_CUDA(ctx, cudaMemcpyAsync(B.segs, B.segs_host, w.segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
+    OR3_CUDA(ctx, cudaMemcpyAsync(B.info, B.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, st));
+    launch_raygen_batch(b, w.num_paths, q, 0, st);
+    for (int rep = 0;; rep++) {
+      if (use_graph) OR3_CUDA(ctx, cudaGraphLaunch(gexec, st));
+      else launch_bounces();
+      OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      OR3_CUDA(ctx, cudaStreamSynchronize(st));
+      if (ctx->host_counters[2]) {
+        const uint32_t bits = ctx->host_counters[2];
+        cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
+        cudaStreamSynchronize(st);
+        return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x in a batch", bits);
+      }
+      if (ctx->host_counters[0] == 0) break;
+      if (rep > (1 << 16)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+    }
+    launch_accumulate_batch(b, w.ngroups, q, st);
+    stats.waves++;
+    stats.camera_paths += w.num_paths;
+  }
+  OR3_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  stats.render_ms = ms;
+
+  if (write_frames) {
+    size_t need = 0;
+    for (size_t j = 0; j < n; j++)
+      if (jobs[j].frame_host)
+        need = std::max(need, (size_t)(jobs[j].params.output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) *
+                                  jobs[j].camera.width * jobs[j].camera.height * 3);
+    if (need) {
+      if ((rc = grow_dev(ctx, B.frame_dev, B.cap_frame, need))) return rc;
+      if ((rc = grow_pinned(ctx, B.frame_pinned, B.cap_frame_pinned, B.cap_frame))) return rc;
+    }
+    for (size_t j = 0; j < n; j++) {
+      const or3_batch_job &job = jobs[j];
+      if (!job.frame_host) continue;
+      const size_t doubles = (size_t)(job.params.output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * job.camera.width *
+                             job.camera.height * 3;
+      if (job.frame_capacity < doubles)
+        return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "job %zu: frame needs %zu doubles", j, doubles);
+      OR3_CUDA(ctx, cudaMemsetAsync(B.frame_dev, 0, doubles * sizeof(double), st));
+      launch_frame(B.sum + 3 * outs[j].pix_base, job.camera.width, job.camera.height, job.params.output_layout,
+                   1.0 / (double)outs[j].count, B.frame_dev, st);
+      OR3_CUDA(ctx, cudaMemcpyAsync(B.frame_pinned, B.frame_dev, doubles * sizeof(double), cudaMemcpyDeviceToHost, st));
+      OR3_CUDA(ctx, cudaStreamSynchronize(st));
+      std::memcpy(job.frame_host, B.frame_pinned, doubles * sizeof(double));
+    }
+  }
+  unsigned long long hs[8];
+  OR3_CUDA(ctx, cudaMemcpy(hs, ctx->dstats, sizeof(hs), cudaMemcpyDeviceToHost));
+  stats.extension_rays = hs[0];
+  stats.shadow_rays = hs[1];
+  stats.bounces = hs[2];
+  stats.nodes_visited = hs[3];
+  stats.tris_tested = hs[4];
+  stats.spheres_tested = hs[5];
+  stats.passes = 1;
+  if (out) *out = stats;
+  B.last = outs;
+  B.valid = true;
+  return OR3_OK;
+}
+
+}  // namespace
+}  // namespace or3
+
+using namespace or3;
+
+extern "C" {
+
+int or3_render_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n_jobs, const or3_batch_params *params,
+                     or3_render_stats *stats_out) {
+  return run_batch(ctx, jobs, n_jobs, params, stats_out, true);
+}
+
+int or3_get_batch_moments(or3_context *ctx, size_t job, double *sum, double *sumsq, size_t capacity,
+                          uint64_t *count_out) {
+  if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
+  if (!ctx->batch || !ctx->batch->valid) return fail(ctx, OR3_ERR_NOT_FOUND, "no completed batch");
+  BatchBuffers &B = *ctx->batch;
+  if (job >= B.last.size()) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "job %zu out of range", job);
+  const BatchBuffers::JobOut &o = B.last[job];
+  const size_t nd = (size_t)o.W * o.H * 3;
+  if (capacity < nd) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "moments need %zu doubles", nd);
+  cudaSetDevice(ctx->device);
+  double *tmp = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&tmp, 2 * nd * sizeof(double)));
+  launch_moments(B.sum + 3 * o.pix_base, B.sumsq + 3 * o.pix_base, o.W, o.H, tmp, tmp + nd, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && sum) e = cudaMemcpy(sum, tmp, nd * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && sumsq) e = cudaMemcpy(sumsq, tmp + nd, nd * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "batch moments: %s", cudaGetErrorString(e));
+  if (count_out) *count_out = o.count;
+  return OR3_OK;
+}
+
+int or3_autotune_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, uint64_t sample_paths,
+                       or3_batch_params *best, double *best_mpaths) {
+  if (!ctx || !jobs || !best || n == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  // reduced copy: every job keeps its image and sub-pixel grid, its sample
+  // budget is cut so the whole copy is about sample_paths camera paths
+  uint64_t total = 0;
+  for (size_t j = 0; j < n; j++)
+    total += (uint64_t)jobs[j].camera.width * jobs[j].camera.height * jobs[j].params.supersamples *
+             jobs[j].params.supersamples * (uint64_t)std::max(jobs[j].params.max_samples, 1);
+  const double f = sample_paths && total > sample_paths ? (double)sample_paths / (double)total : 1.0;
+  std::vector<or3_batch_job> small(jobs, jobs + n);
+  for (or3_batch_job &j : small) {
+    const int32_t s = std::max<int32_t>(1, (int32_t)std::lround(j.params.max_samples * f));
+    j.params.min_samples = s;
+    j.params.max_samples = s;
+    j.params.step_samples = 1;
+    j.frame_host = nullptr;
+  }
+  const uint64_t waves[] = {1ull << 21, 1ull << 22, 1ull << 23, 1ull << 24, 1ull << 25};
+  const uint32_t unrolls[] = {4, 8, 16};
+  double best_rate = -1.0;
+  or3_batch_params bestp{};
+  for (uint64_t wv : waves) {
+    for (uint32_t un : unrolls) {
+      for (uint32_t bps : {0u, 2u}) {
+        or3_batch_params p{};
+        p.wave_paths = wv;
+        p.graph_bounces = un;
+        p.blocks_per_sm = bps;
+        or3_render_stats s{};
+        int rc = run_batch(ctx, small.data(), n, &p, &s, false);  // warm-up
+        if (rc == OR3_OK) rc = run_batch(ctx, small.data(), n, &p, &s, false);
+        if (rc != OR3_OK) return rc;
+        const double rate = (double)s.camera_paths / (s.render_ms * 1e3);
+        if (rate > best_rate) {
+          best_rate = rate;
+          bestp = p;
+        }
+      }
+    }
+  }
+  *best = bestp;
+  if (best_mpaths) *best_mpaths = best_rate;
+  return OR3_OK;
+}
+
+}  // extern "C"

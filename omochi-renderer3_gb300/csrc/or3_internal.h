@@ -1,0 +1,106 @@
+// or3_internal.h -- the context and helpers shared by the host translation
+// units (or3_api.cu: plain render and queries; or3_batch.cu: batched and
+// served forms).  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "or3.h"
+#include "or3_kernels.cuh"
+
+namespace or3 {
+
+struct SceneGPU {
+  DevScene view{};
+  std::vector<void *> allocs;
+  or3_scene_info info{};
+  bool has_split = false;  // a refractive layer exists: paths can split at depth <= 2
+};
+
+struct BatchBuffers;  // or3_batch.cu
+struct Server;        // or3_batch.cu
+
+}  // namespace or3
+
+struct or3_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<int32_t, or3::SceneGPU *> scenes;
+  int32_t next_scene = 1;
+  int num_sms = 0;
+  int occ_extend = 1, occ_shade = 1;
+
+  // queues
+  size_t cap_rays = 0, cap_paths = 0;
+  float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
+  float4 *hits = nullptr, *pathL = nullptr;
+  uint32_t *counters = nullptr;
+  unsigned long long *dstats = nullptr;
+  uint32_t *host_counters = nullptr;  // pinned
+
+  // accumulation + frames
+  size_t cap_pixels = 0;
+  double *pix_sum = nullptr, *pix_sumsq = nullptr;
+  size_t cap_frame = 0;
+  double *frame_dev = nullptr, *frame_pinned = nullptr;
+  std::vector<double> frame_host;  // last completed frame (Renderer::GetResult)
+  std::mutex frame_mu;
+  int32_t frame_samples = 0;
+
+  std::atomic<bool> stop{false};
+  or3_render_stats last{};
+  uint32_t last_W = 0, last_H = 0;
+  uint64_t last_count = 0;  // paths per pixel in the moments
+  bool moments_valid = false;
+  uint64_t last_wave_paths = 0;
+  bool last_kept_paths = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
+
+  or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
+  or3::Server *server = nullptr;       // served form state (or3_batch.cu)
+};
+
+namespace or3 {
+
+inline int fail(or3_context *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return code;
+}
+
+#define OR3_CUDA(ctx, call)                                                                      \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) {                                                                     \
+      return ::or3::fail(ctx, e_ == cudaErrorMemoryAllocation ? OR3_ERR_OUT_OF_MEMORY : OR3_ERR_CUDA, \
+                         "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    }                                                                                            \
+  } while (0)
+
+// or3_api.cu
+int ensure_queues(or3_context *ctx, size_t paths, size_t rays);
+Queues make_queues(or3_context *ctx);
+void camera_basis(const or3_camera *c, Camera32 &out);
+int validate_render(or3_context *ctx, const or3_camera *cam, const or3_render_params *prm);
+void fill_render_const(const or3_camera *cam, const or3_render_params *prm, RenderConst &rc);
+
+// or3_batch.cu
+void destroy_batch_state(or3_context *ctx);
+// or3_server.cu
+void destroy_server_state(or3_context *ctx);
+
+}  // namespace or3

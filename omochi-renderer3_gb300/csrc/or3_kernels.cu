@@ -368,7 +368,20 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   }
 }
 
-__global__ void __launch_bounds__(256) k_shade(DevScene S, RenderConst rc, Wave w, Queues q, int in) {
+__device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t nseg, uint32_t wave_index) {
+  uint32_t lo = 0, hi = nseg;  // last segment with wave_first <= wave_index
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (segs[mid].wave_first <= wave_index) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// BATCH: the ray's segment (beta.w) selects the job's scene, constants and
+// RNG numbering; continuation rays inherit it.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in, Batch b) {
   const uint32_t n = q.counters[in];
   const int out = in ^ 1;
   const uint32_t lane = threadIdx.x & 31u;
@@ -376,7 +389,19 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, RenderConst rc, Wave 
     const uint32_t i = base + threadIdx.x;
     NewRay r0, r1;
     int cnt = 0;
-    if (i < n) cnt = shade_one(S, rc, w, q, in, i, r0, r1);
+    uint32_t tag = 0;
+    if (i < n) {
+      if (BATCH) {
+        tag = __float_as_uint(q.beta[in][i].w);
+        const Segment sg = b.segs[tag];
+        const JobDev &job = b.jobs[sg.job];
+        Wave w = w0;
+        w.g_first = sg.g_first - sg.wave_first;
+        cnt = shade_one(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1);
+      } else {
+        cnt = shade_one(S0, rc0, w0, q, in, i, r0, r1);
+      }
+    }
     // warp-aggregated append to the output queue
     int incl = cnt;
 #pragma unroll
@@ -398,7 +423,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, RenderConst rc, Wave 
       }
       q.orig[out][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
       q.dir[out][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
-      q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, 0.f);
+      q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, __uint_as_float(tag));
     }
   }
 }
@@ -528,6 +553,123 @@ __global__ void __launch_bounds__(256) k_trace_occluded(DevScene S, uint32_t n, 
 
 int g_query_grid = 152 * 4;
 
+// ---------------------------------------------------------------- batched form kernels
+
+__global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    q.counters[out] = num_paths;
+    q.counters[4 + out] = 0;
+  }
+  if (i >= num_paths) return;
+  const uint32_t si = find_segment(b.segs, b.info->nseg, i);
+  const Segment sg = b.segs[si];
+  const RenderConst &rc = b.jobs[sg.job].rc;
+  const uint64_t g = sg.g_first + (i - sg.wave_first);
+  const uint32_t sub = (uint32_t)(g % rc.ss2);
+  const uint64_t pg = g / rc.ss2;
+  const uint32_t pix = (uint32_t)(pg % ((uint64_t)rc.W * rc.H));
+  V3 o, d;
+  camera_ray(rc, pix % rc.W, pix / rc.W, sub % rc.ss, sub / rc.ss, pix * rc.ss2 + sub, sg.pass_first, o, d);
+  q.orig[out][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
+  q.dir[out][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+  q.beta[out][i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(si));
+  q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// persistent_trace (STEP 2) with the scene chosen per ray by its segment.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in) {
+  const uint32_t n = q.counters[in];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+    if (n) atomicAdd(&q.stats[2], 1ull);
+  }
+  uint32_t cnt[3] = {0u, 0u, 0u};
+  uint32_t stk_e[kStackSize];
+  float stk_t[kStackSize];
+  TravState st;
+  const DevScene *sp = nullptr;
+  uint32_t r = kNoEntry;
+  bool exhausted = false;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t *fetch = &q.counters[4 + in];
+  for (;;) {
+    const bool need = (r == kNoEntry) && !exhausted;
+    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    if (__popc(m) < 16 && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        if (idx < n) {
+          const uint32_t tag = __float_as_uint(q.beta[in][idx].w);
+          sp = &b.scenes[b.jobs[b.segs[tag].job].scene];
+          trav_init(st, ld3(q.orig[in][idx]), ld3(q.dir[in][idx]), kInf, sp->num_nodes);
+          r = idx;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
+    if (r != kNoEntry) {
+      if (trav_step_inline<false, COUNT>(*sp, st, stk_e, stk_t, nullptr, 0u, cnt, &q.counters[2])) {
+        const Hit h = trav_finish<false>(*sp, st);
+        q.hits[r] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+        r = kNoEntry;
+      }
+    }
+  }
+  if (COUNT) {
+    unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
+#pragma unroll
+    for (int ofs = 16; ofs > 0; ofs >>= 1) {
+      c0 += __shfl_xor_sync(0xFFFFFFFFu, c0, ofs);
+      c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, ofs);
+      c2 += __shfl_xor_sync(0xFFFFFFFFu, c2, ofs);
+    }
+    if (lane == 0) {
+      atomicAdd(&q.stats[3], c0);
+      atomicAdd(&q.stats[4], c1);
+      atomicAdd(&q.stats[5], c2);
+    }
+  }
+}
+
+// One thread per pixel-sample group (ss2 consecutive paths of one pixel and
+// sample); FP32 partial sums added to the job's FP64 pixel sums.
+__global__ void k_accumulate_batch(Batch b, Queues q) {
+  const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= b.info->ngroups) return;
+  uint32_t lo = 0, hi = b.info->nseg;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (b.segs[mid].group_first <= gi) lo = mid;
+    else hi = mid;
+  }
+  const Segment sg = b.segs[lo];
+  const JobDev &job = b.jobs[sg.job];
+  const uint32_t ss2 = job.rc.ss2;
+  const uint32_t local = gi - sg.group_first;
+  const uint64_t gstart = sg.g_first + (uint64_t)local * ss2;
+  const uint32_t wstart = sg.wave_first + local * ss2;
+  const uint64_t pix = (gstart / ss2) % ((uint64_t)job.rc.W * job.rc.H);
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f;
+  for (uint32_t k = 0; k < ss2; k++) {
+    const float4 L = q.pathL[wstart + k];
+    s0 += L.x; s1 += L.y; s2 += L.z;
+    q0 += L.x * L.x; q1 += L.y * L.y; q2 += L.z * L.z;
+  }
+  double *S = job.sum + 3 * pix;
+  double *Q = job.sumsq + 3 * pix;
+  atomicAdd(S, (double)s0); atomicAdd(S + 1, (double)s1); atomicAdd(S + 2, (double)s2);
+  atomicAdd(Q, (double)q0); atomicAdd(Q + 1, (double)q1); atomicAdd(Q + 2, (double)q2);
+}
+
 }  // namespace
 
 void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int out, int grid, int block,
@@ -552,7 +694,7 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                   int grid, int block, cudaStream_t st) {
-  k_shade<<<grid, block, 0, st>>>(S, rc, w, q, in);
+  k_shade<false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
 }
 
 void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
@@ -601,6 +743,26 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
 }
 
 const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }
-const void *kernel_shade_ptr() { return (const void *)k_shade; }
+const void *kernel_shade_ptr() { return (const void *)k_shade<false>; }
+
+// ---------------------------------------------------------------- batched form
+
+void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, int out, cudaStream_t st) {
+  k_raygen_batch<<<(num_paths + 255) / 256 > 0 ? (num_paths + 255) / 256 : 1, 256, 0, st>>>(b, num_paths, q, out);
+}
+
+void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, cudaStream_t st) {
+  if (count) k_extend_batch<true><<<grid, 256, 0, st>>>(b, q, in);
+  else k_extend_batch<false><<<grid, 256, 0, st>>>(b, q, in);
+}
+
+void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, cudaStream_t st) {
+  k_shade<true><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
+}
+
+void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st) {
+  const uint32_t g = (max_groups + 255) / 256;
+  k_accumulate_batch<<<g > 0 ? g : 1, 256, 0, st>>>(b, q);
+}
 
 }  // namespace or3

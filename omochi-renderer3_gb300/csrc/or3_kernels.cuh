@@ -57,6 +57,49 @@ struct Queues {
 constexpr uint32_t kErrStack = 1u;
 constexpr uint32_t kErrQueue = 2u;
 
+// ---- batched form: one wave holds path ranges ("segments") of many jobs.
+// A job is one render (scene, camera, sample budget); its camera paths keep
+// the plain render's numbering and RNG keys, so a job renders the same paths
+// alone or in a batch.  Rays carry their segment index in beta.w.
+struct JobDev {
+  RenderConst rc;
+  uint32_t scene;     // index into Batch::scenes
+  uint32_t pad;
+  double *sum;        // the job's per-pixel sums (3 per pixel, camera order y*W+x)
+  double *sumsq;
+};
+
+struct Segment {
+  uint64_t g_first;      // first job path index (a multiple of ss2)
+  uint32_t job;
+  uint32_t wave_first;   // wave path index of the segment's first path
+  uint32_t count;        // paths (a multiple of ss2)
+  uint32_t pass_first;   // first sample of the pass (lens key)
+  uint32_t group_first;  // first pixel-sample group of the segment in the wave
+  uint32_t pad;
+};
+
+// Wave description read by the kernels from device memory, so one captured
+// graph of the bounce loop serves every wave.
+struct WaveInfo {
+  uint32_t nseg;
+  uint32_t ngroups;   // pixel-sample groups (ss2 paths each) in the wave
+  uint32_t num_paths;
+  uint32_t pad;
+};
+
+struct Batch {
+  const DevScene *scenes;
+  const JobDev *jobs;
+  const Segment *segs;
+  const WaveInfo *info;
+};
+
+void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, int out, cudaStream_t st);
+void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, cudaStream_t st);
+void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, cudaStream_t st);
+void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st);
+
 struct LaunchCfg {
   int grid_extend, grid_shade, grid_raygen, grid_accum;
   int block;

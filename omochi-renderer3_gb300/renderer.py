@@ -140,6 +140,99 @@ class Context:
         self._check(self.lib.or3_get_path_radiance(self.h, out.ctypes.data_as(abi.f32p), out.size, ctypes.byref(n)))
         return out
 
+    # ---- batched form
+    def _job(self, scene, camera, settings, frame=None):
+        j = abi.BatchJobC()
+        j.scene = scene
+        j.camera = camera.to_c()
+        j.params = self._params(**settings)
+        if frame is not None:
+            j.frame_host = frame.ctypes.data_as(abi.f64p)
+            j.frame_capacity = frame.size
+        return j
+
+    def render_batch(self, jobs, *, wave_paths=0, graph_bounces=0, blocks_per_sm=0, flags=0, frames=False):
+        """jobs: list of (scene, camera, settings dict).  Returns (stats, frames or None)."""
+        n = len(jobs)
+        arr = (abi.BatchJobC * n)()
+        outs = []
+        for k, (sid, cam, st) in enumerate(jobs):
+            fr = None
+            if frames:
+                w = cam.width * (2 if st.get("layout", abi.OR3_LAYOUT_REFERENCE) == abi.OR3_LAYOUT_REFERENCE else 1)
+                fr = np.zeros((cam.height, w, 3), np.float64)
+                outs.append(fr)
+            arr[k] = self._job(sid, cam, st, fr)
+        bp = abi.BatchParamsC(wave_paths, flags, graph_bounces, blocks_per_sm, 0)
+        s = abi.RenderStatsC()
+        self._check(self.lib.or3_render_batch(self.h, arr, n, ctypes.byref(bp), ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.RenderStatsC._fields_}, (outs if frames else None)
+
+    def batch_moments(self, job, width, height):
+        s = np.zeros((height, width, 3), np.float64)
+        q = np.zeros_like(s)
+        n = ctypes.c_uint64()
+        self._check(self.lib.or3_get_batch_moments(self.h, job, s.ctypes.data_as(abi.f64p),
+                                                   q.ctypes.data_as(abi.f64p), s.size, ctypes.byref(n)))
+        return s, q, n.value
+
+    def autotune_batch(self, jobs, sample_paths=1 << 24):
+        n = len(jobs)
+        arr = (abi.BatchJobC * n)()
+        for k, (sid, cam, st) in enumerate(jobs):
+            arr[k] = self._job(sid, cam, st)
+        best = abi.BatchParamsC()
+        rate = ctypes.c_double()
+        self._check(self.lib.or3_autotune_batch(self.h, arr, n, sample_paths, ctypes.byref(best), ctypes.byref(rate)))
+        return dict(wave_paths=best.wave_paths, graph_bounces=best.graph_bounces,
+                    blocks_per_sm=best.blocks_per_sm), rate.value
+
+    # ---- served form
+    def server_start(self, *, wave_paths=0, hbm_budget_bytes=0, max_active_jobs=0, frame_every_samples=0,
+                     graph_bounces=0, keep_moments=False, on_frame=None):
+        p = abi.ServerParamsC(wave_paths, hbm_budget_bytes, max_active_jobs, frame_every_samples, graph_bounces,
+                              abi.OR3_SERVER_KEEP_MOMENTS if keep_moments else 0)
+        if on_frame is not None:
+            def _cb(user, job_id, samples, rgb, w, h, final):
+                on_frame(job_id, samples, np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy(), bool(final))
+            self._server_cb = abi.JOB_FRAME_CB(_cb)
+        else:
+            self._server_cb = abi.JOB_FRAME_CB()
+        self._check(self.lib.or3_server_start(self.h, ctypes.byref(p), self._server_cb, None))
+
+    def server_submit(self, scene, camera, **settings):
+        j = self._job(scene, camera, settings)
+        jid = ctypes.c_uint64()
+        self._check(self.lib.or3_server_submit(self.h, ctypes.byref(j), ctypes.byref(jid)))
+        return jid.value
+
+    def server_poll(self, job_id):
+        s = abi.JobStatusC()
+        self._check(self.lib.or3_server_poll(self.h, job_id, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.JobStatusC._fields_}
+
+    def server_cancel(self, job_id):
+        self._check(self.lib.or3_server_cancel(self.h, job_id))
+
+    def server_drain(self, timeout_s=0.0):
+        self._check(self.lib.or3_server_drain(self.h, timeout_s))
+
+    def server_stats(self):
+        s = abi.ServerStatsC()
+        self._check(self.lib.or3_server_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.ServerStatsC._fields_}
+
+    def server_moments(self, job_id, width, height):
+        s = np.zeros((height, width, 3), np.float64)
+        q = np.zeros_like(s)
+        n = ctypes.c_uint64()
+        self._check(self.lib.or3_server_get_moments(self.h, job_id, s.ctypes.data_as(abi.f64p),
+                                                    q.ctypes.data_as(abi.f64p), s.size, ctypes.byref(n)))
+        return s, q, n.value
+
+    def server_stop(self):
+        self._check(self.lib.or3_server_stop(self.h))
+
     # ---- ray queries
     def trace_closest(self, scene, origins, dirs):
         o = np.ascontiguousarray(origins, np.float32)

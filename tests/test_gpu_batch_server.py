@@ -1,0 +1,155 @@
+"""Batched and served forms through the C ABI.
+
+The property both must keep: a job's image is the same alone and in a mix.
+Each job's camera paths keep or3_render's numbering and Philox keys, so its
+per-pixel sums must equal a plain or3_render of the same job to float
+rounding (the only order-dependent step is the float atomics that add the two
+branches of a glass split): rtol 1e-5.
+"""
+import threading
+import time
+from collections import defaultdict
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs(pkg, ctx):
+    W = pkg.workloads
+    a = W.cornell_box(40, 32)
+    b = W.icosphere_in_box(48, 32, level=3)
+    c = W.reference_cornell(32, 24)
+    sids = [ctx.upload(x[0]) for x in (a, b, c)]
+    jobs = [
+        (sids[0], a[1], dict(supersamples=2, min_samples=1, max_samples=3, step_samples=1, rr_min_depth=3,
+                             max_depth=8, seed=5)),
+        (sids[1], b[1], dict(supersamples=4, min_samples=2, max_samples=2, step_samples=1, rr_min_depth=5,
+                             max_depth=10, seed=6)),
+        (sids[2], c[1], dict(supersamples=1, min_samples=4, max_samples=8, step_samples=4, rr_min_depth=5,
+                             max_depth=0, seed=7)),
+    ]
+    return sids, jobs
+
+
+def _plain(ctx, sid, cam, st):
+    ctx.render(sid, cam, **st)
+    s, q, n = ctx.moments(cam.width, cam.height)
+    img, _ = ctx.frame(cam.width, cam.height)
+    return s, q, n, img
+
+
+@pytest.mark.parametrize("wave_paths", [0, 3000])
+def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths):
+    sids, jobs = _jobs(pkg, ctx)
+    try:
+        alone = [_plain(ctx, *j) for j in jobs]
+        stats, frames = ctx.render_batch(jobs, frames=True, wave_paths=wave_paths)
+        if wave_paths:
+            assert stats["waves"] > 3  # jobs really were cut and mixed across waves
+        for k, (sid, cam, st) in enumerate(jobs):
+            s, q, n = ctx.batch_moments(k, cam.width, cam.height)
+            s0, q0, n0, img0 = alone[k]
+            assert n == n0
+            np.testing.assert_allclose(s, s0, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(q, q0, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(frames[k], img0, rtol=1e-5, atol=1e-7)
+        assert stats["camera_paths"] == sum(c.width * c.height * st["supersamples"] ** 2 *
+                                            (st["min_samples"] + (st["max_samples"] - st["min_samples"]) //
+                                             st["step_samples"] * st["step_samples"]) for _, c, st in jobs)
+    finally:
+        for s in sids:
+            ctx.release(s)
+
+
+def test_batch_without_graph_and_autotune(pkg, ctx):
+    sids, jobs = _jobs(pkg, ctx)
+    try:
+        ctx.render_batch(jobs, graph_bounces=4)
+        s1 = [ctx.batch_moments(k, c.width, c.height)[0] for k, (_, c, _) in enumerate(jobs)]
+        ctx.render_batch(jobs, flags=pkg.abi.OR3_FLAG_NO_GRAPH)
+        s2 = [ctx.batch_moments(k, c.width, c.height)[0] for k, (_, c, _) in enumerate(jobs)]
+        for a, b in zip(s1, s2):
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+        best, rate = ctx.autotune_batch(jobs, sample_paths=100000)
+        assert best["wave_paths"] in (1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25)
+        assert best["graph_bounces"] in (4, 8, 16)
+        assert rate > 0
+    finally:
+        for s in sids:
+            ctx.release(s)
+
+
+def test_batch_rejects_bad_jobs(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(8, 8)
+    sid = ctx.upload(sd)
+    with pytest.raises(pkg.Or3Error):
+        ctx.render_batch([(sid + 1000, cam, dict(supersamples=1))])
+    with pytest.raises(pkg.Or3Error):
+        ctx.render_batch([(sid, cam, dict(supersamples=0))])
+    ctx.release(sid)
+
+
+def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx):
+    sids, jobs = _jobs(pkg, ctx)
+    alone = [_plain(ctx, *j) for j in jobs]
+    frames = defaultdict(list)
+    lock = threading.Lock()
+
+    def on_frame(jid, samples, img, final):
+        with lock:
+            frames[jid].append((samples, final, img))
+
+    ctx.server_start(keep_moments=True, frame_every_samples=1, wave_paths=1 << 16, on_frame=on_frame)
+    try:
+        ids = [ctx.server_submit(*jobs[0][:2], **jobs[0][2])]
+        time.sleep(0.05)  # later arrivals join while the first job runs
+        ids += [ctx.server_submit(j[0], j[1], **j[2]) for j in jobs[1:]]
+        ctx.server_drain(120.0)
+        stats = ctx.server_stats()
+        for k, jid in enumerate(ids):
+            cam = jobs[k][1]
+            st = ctx.server_poll(jid)
+            assert st["state"] == pkg.abi.OR3_JOB_DONE
+            s, q, n = ctx.server_moments(jid, cam.width, cam.height)
+            s0, q0, n0, img0 = alone[k]
+            assert n == n0
+            np.testing.assert_allclose(s, s0, rtol=1e-5, atol=1e-6)
+            fs = frames[jid]
+            assert fs[-1][1] and not any(f[1] for f in fs[:-1])
+            assert [f[0] for f in fs] == sorted(f[0] for f in fs)
+            np.testing.assert_allclose(fs[-1][2], img0, rtol=1e-5, atol=1e-7)
+        assert stats["jobs_done"] == 3
+        assert stats["latency_p99_s"] >= stats["latency_p50_s"] > 0
+        assert stats["peak_active_jobs"] >= 2  # the jobs overlapped on the device
+    finally:
+        ctx.server_stop()
+        for s in sids:
+            ctx.release(s)
+
+
+def test_server_budget_admission_and_cancel(pkg, ctx):
+    sids, jobs = _jobs(pkg, ctx)
+    big = pkg.workloads.cornell_box(64, 64)
+    bsid = ctx.upload(big[0])
+    # budget (80 kB) above any one small job's buffers (<= 48x32 px x 48 B = 73.7 kB)
+    # and below any two: admission serialises them; the big job (196 kB) only
+    # gets in because nothing else is running
+    ctx.server_start(hbm_budget_bytes=80000, wave_paths=1 << 16)
+    try:
+        long_id = ctx.server_submit(bsid, big[1], supersamples=2, min_samples=400, max_samples=400, seed=1)
+        ids = [ctx.server_submit(j[0], j[1], **j[2]) for j in jobs]
+        time.sleep(0.05)
+        ctx.server_cancel(long_id)
+        ctx.server_drain(120.0)
+        assert ctx.server_poll(long_id)["state"] == pkg.abi.OR3_JOB_CANCELLED
+        for jid in ids:
+            assert ctx.server_poll(jid)["state"] == pkg.abi.OR3_JOB_DONE
+        st = ctx.server_stats()
+        assert st["peak_active_jobs"] == 1
+        assert st["jobs_cancelled"] == 1
+    finally:
+        ctx.server_stop()
+        for s in sids + [bsid]:
+            ctx.release(s)

@@ -204,6 +204,118 @@ def run_reference(args, pkg, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, pkg):
+    """Batched workload: 64 seeded scenes rendered one by one (plain form) and as one batch."""
+    W = pkg.workloads
+    ctx = pkg.Context(0)
+    t0 = time.perf_counter()
+    jobs_sd = W.batched_jobs(n=args.jobs, scale=args.scale)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sids = [ctx.upload(sd) for sd, _, _ in jobs_sd]
+    upload_s = time.perf_counter() - t0
+    jobs = [(sid, cam, st) for sid, (_, cam, st) in zip(sids, jobs_sd)]
+    tris = sum(ctx.scene_info(s)["num_primitives"] for s in sids)
+    paths = sum(c.width * c.height * st["supersamples"] ** 2 * st["max_samples"] for _, c, st in jobs)
+    best = {}
+    if args.autotune:
+        best, _ = ctx.autotune_batch(jobs, sample_paths=1 << 25)
+    for _ in range(max(args.warmup, 1)):
+        ctx.render_batch(jobs[:4], **best)
+        for sid, cam, st in jobs[:4]:
+            ctx.render(sid, cam, **st)
+    plain_ms = 0.0
+    plain_wall = time.perf_counter()
+    for sid, cam, st in jobs:
+        plain_ms += ctx.render(sid, cam, **st)["render_ms"]
+    plain_wall = time.perf_counter() - plain_wall
+    batch_ms, batch_wall = [], []
+    for _ in range(args.steps):
+        w0 = time.perf_counter()
+        s, _ = ctx.render_batch(jobs, **best)
+        batch_wall.append(time.perf_counter() - w0)
+        batch_ms.append(s["render_ms"])
+    # equal images: a batched job equals its plain render (same paths), checked on a few jobs
+    maxdiff = 0.0
+    for k in (0, 1, len(jobs) - 1):
+        sid, cam, st = jobs[k]
+        ctx.render(sid, cam, **st)
+        sp, _, _ = ctx.moments(cam.width, cam.height)
+        ctx.render_batch([jobs[k]], **best)
+        sb, _, _ = ctx.batch_moments(0, cam.width, cam.height)
+        maxdiff = max(maxdiff, float(np.max(np.abs(sb - sp) / (np.abs(sp) + 1e-3))))
+    bms = float(np.median(batch_ms))
+    line = {"metric": METRIC, "form": "batched", "value": paths / bms / 1e3, "unit": "Mpaths/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
+            "config": {"workload": "batched_%d_scenes_1k-2M_tris_log_uniform_x%g_128-1024px_16-512spp" %
+                                   (len(jobs), args.scale),
+                       "triangles_total": int(tris), "camera_paths": int(paths), "scene_gen_s": gen_s,
+                       "scene_upload_s": upload_s, "tuning": best},
+            "plain_form": {"value": paths / plain_ms / 1e3, "ms": plain_ms, "wall_s": plain_wall,
+                           "what": "the same 64 renders, one or3_render call each, scenes resident"},
+            "speedup_vs_plain": plain_ms / bms, "batch_wall_s": float(np.median(batch_wall)),
+            "equal_images_max_rel_diff": maxdiff}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_served(args, pkg):
+    """Served workload: Poisson requests over a resident scene pool, continuous batching."""
+    W = pkg.workloads
+    ctx = pkg.Context(0)
+    t0 = time.perf_counter()
+    pool = W.served_pool(n=args.scenes, scale=args.scale, env=(args.env_w, args.env_h))
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sids = [ctx.upload(sd) for sd, _ in pool]
+    upload_s = time.perf_counter() - t0
+    eyes = [e for _, e in pool]
+    results = {}
+    rng = np.random.default_rng(11)
+    mean_paths = np.mean([w * h for w, h in W.SERVED_RES]) * np.mean(W.SERVED_SPP)
+    for label, rate, secs in (("stated_rate", args.rate, args.seconds),
+                              ("sustainable_rate", None, args.sustain_seconds)):
+        if rate is None:
+            cap = results["stated_rate"]["mpaths_per_s"] * 1e6
+            rate = 0.6 * cap / mean_paths
+        ctx.server_start(frame_every_samples=1)
+        submitted = 0
+        tstart = time.perf_counter()
+        tnext = tstart
+        while True:
+            tnext += rng.exponential(1.0 / rate)
+            if tnext - tstart > secs:
+                break
+            time.sleep(max(0.0, tnext - time.perf_counter()))
+            s, cam, st = W.served_request(rng, len(sids), lambda k: eyes[k])
+            ctx.server_submit(sids[s], cam, **st)
+            submitted += 1
+        ctx.server_drain(args.drain_timeout)
+        wall = time.perf_counter() - tstart
+        stt = ctx.server_stats()
+        ctx.server_stop()
+        results[label] = {"rate_req_per_s": rate, "arrival_window_s": secs, "requests": submitted,
+                          "latency_p50_s": stt["latency_p50_s"], "latency_p99_s": stt["latency_p99_s"],
+                          "queue_p50_s": stt["queue_p50_s"], "queue_p99_s": stt["queue_p99_s"],
+                          "first_frame_p50_s": stt["first_frame_p50_s"],
+                          "mpaths_per_s": stt["camera_paths"] / (stt["device_ms"] / 1e3) / 1e6,
+                          "mpaths_per_s_wall": stt["camera_paths"] / max(stt["busy_s"], 1e-9) / 1e6,
+                          "camera_paths": stt["camera_paths"], "wall_s": wall,
+                          "peak_active_jobs": stt["peak_active_jobs"]}
+    sr = results["stated_rate"]
+    line = {"metric": METRIC, "form": "served", "value": sr["mpaths_per_s"], "unit": "Mpaths/s", "n_gpus": 1,
+            "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, Poisson arrivals)",
+            "config": {"workload": "served_%d_scenes_10k-4M_tris_x%g_env%dx%d" % (args.scenes, args.scale,
+                                                                                args.env_w, args.env_h),
+                       "scene_gen_s": gen_s, "scene_upload_s": upload_s,
+                       "requests": "res {256^2,512^2,1280x720,1920x1080} x spp {16,64,256,1024}, frames every 16 spp"},
+            "served": results}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -216,10 +328,27 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--res", default="", help="WxH override (smaller case for profiling)")
     ap.add_argument("--ss", type=int, default=0, help="sub-pixel grid override")
+    ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"])
+    ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--scenes", type=int, default=32)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--seconds", type=float, default=2.0)
+    ap.add_argument("--sustain-seconds", type=float, default=20.0)
+    ap.add_argument("--drain-timeout", type=float, default=600.0)
+    ap.add_argument("--env-w", type=int, default=2048)
+    ap.add_argument("--env-h", type=int, default=1024)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    world, rank, local, dist = dist_setup(args)
     pkg = ge.load_package()
+    if args.form == "batched":
+        run_batched(args, pkg)
+        return
+    if args.form == "served":
+        run_served(args, pkg)
+        return
+    world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, pkg, world, rank)
         return

@@ -204,6 +204,108 @@ def reference_cornell(width=160, height=120):
     return sd, cam, settings
 
 
+def _mesh_scene(rng, tris, kind, env_size=(512, 256)):
+    """One seeded scene of about `tris` triangles: a displaced icosphere in the
+    Cornell box (kind 0) or a heightfield under a sky (kind 1); the main
+    surface is Lambertian, mirror or glass, with a few mirror/glass spheres."""
+    sd = SceneDesc()
+    pick = rng.random()
+    albedo = tuple(rng.uniform(0.4, 0.85, 3))
+    if pick < 0.6:
+        main = sd.material(abi.OR3_LAMBERT, albedo)
+    elif pick < 0.8:
+        main = sd.material(abi.OR3_SPECULAR, (0.95, 0.95, 0.95))
+    else:
+        main = sd.material(abi.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    mirror = sd.material(abi.OR3_SPECULAR, (0.95, 0.95, 0.95))
+    glass = sd.material(abi.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    seed = int(rng.integers(1 << 30))
+    if kind == 0:
+        white = sd.material(abi.OR3_LAMBERT, (0.75, 0.75, 0.75))
+        red = sd.material(abi.OR3_LAMBERT, (0.75, 0.25, 0.25))
+        blue = sd.material(abi.OR3_LAMBERT, (0.25, 0.25, 0.75))
+        light = sd.material(abi.OR3_LAMBERT, (0.0, 0.0, 0.0), emission=(12.0, 12.0, 12.0))
+        _box_walls(sd, white, red, blue)
+        _box_light(sd, light)
+        level = int(np.clip(np.round(np.log(max(tris, 80) / 20.0) / np.log(4.0)), 2, 9))
+        v, f = icosphere(level)
+        pos = v * (22.0 * (1.0 + 0.1 * fbm3(v * 2.0, seed)))[:, None] + np.array([50.0, 40.0, 50.0])
+        sd.add_triangles(pos[f], sd.layers(main), normals=vertex_normals(pos, f)[f])
+        for k in range(3):
+            sd.add_sphere((15.0 + 35.0 * k, 8.0, 85.0), 7.0, sd.layers(mirror if k % 2 else glass))
+        cam = None
+    else:
+        cells = max(tris // 2, 8)
+        cx = max(int(np.sqrt(cells * 2)), 2)
+        cz = max(cells // cx, 2)
+        ex, ez = 400.0, 400.0 * cz / cx
+        xs, zs = np.linspace(-ex / 2, ex / 2, cx + 1), np.linspace(-ez / 2, ez / 2, cz + 1)
+        X, Z = np.meshgrid(xs, zs)
+        h = fbm3(np.stack([X / 80.0, np.zeros_like(X), Z / 80.0], -1), seed) * 15.0
+        P = np.stack([X, h, Z], -1).reshape(-1, 3)
+        idx = np.arange((cz + 1) * (cx + 1)).reshape(cz + 1, cx + 1)
+        a, b = idx[:-1, :-1].ravel(), idx[:-1, 1:].ravel()
+        c, d = idx[1:, :-1].ravel(), idx[1:, 1:].ravel()
+        f = np.concatenate([np.stack([a, c, b], 1), np.stack([b, c, d], 1)])
+        sd.add_triangles(P[f], sd.layers(main), normals=vertex_normals(P, f)[f])
+        for k in range(4):
+            sd.add_sphere((rng.uniform(-60, 60), 25.0, rng.uniform(-60, 60)), rng.uniform(5, 12),
+                          sd.layers(mirror if k % 2 else glass))
+        sky, _ = sky_image(env_size[0], env_size[1], seed=seed % 1000)
+        sd.set_env(sky)
+        cam = (0.0, 90.0, 260.0)
+    return sd, cam
+
+
+def batched_jobs(n=64, seed=4, scale=1.0):
+    """Batched workload: n seeded scenes, triangle counts log-uniform in [1k, 2M] (x scale),
+    alternating displaced icospheres and heightfields, mixed Lambert/mirror/glass,
+    square images with sides uniform in [128, 1024], spp uniform in [16, 512]
+    (a 4x4 sub-pixel grid times spp/16 samples).  Returns [(SceneDesc, Camera, settings)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        tris = int(np.exp(rng.uniform(np.log(1e3), np.log(2e6))) * scale)
+        sd, eye = _mesh_scene(rng, tris, i % 2)
+        side = int(rng.integers(128, 1025))
+        spp = int(rng.integers(16, 513)) // 16 * 16 or 16
+        if eye is None:
+            cam = cornell_camera(side, side)
+        else:
+            cam = Camera.from_fov(side, side, eye, (0.0, 0.0, 0.0), 50.0)
+        st = dict(supersamples=4, min_samples=spp // 16, max_samples=spp // 16, step_samples=1,
+                  rr_min_depth=5, max_depth=8, seed=1000 + i)
+        out.append((sd, cam, st))
+    return out
+
+
+SERVED_RES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+SERVED_SPP = [16, 64, 256, 1024]
+
+
+def served_pool(n=32, seed=5, scale=1.0, env=(2048, 1024)):
+    """Served workload: n resident scenes of 10k-4M triangles (log-uniform, x scale), each
+    with its own float32 equirect sky of `env` size.  Returns [(SceneDesc, eye)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        tris = int(np.exp(rng.uniform(np.log(1e4), np.log(4e6))) * scale)
+        sd, eye = _mesh_scene(rng, tris, 1, env_size=env)
+        out.append((sd, eye))
+    return out
+
+
+def served_request(rng, pool_size, eye_of):
+    """One request: a resident scene, a resolution from SERVED_RES and an spp from SERVED_SPP."""
+    s = int(rng.integers(pool_size))
+    w, h = SERVED_RES[int(rng.integers(len(SERVED_RES)))]
+    spp = SERVED_SPP[int(rng.integers(len(SERVED_SPP)))]
+    cam = Camera.from_fov(w, h, eye_of(s), (0.0, 0.0, 0.0), 50.0)
+    st = dict(supersamples=4, min_samples=spp // 16, max_samples=spp // 16, step_samples=1, rr_min_depth=5,
+              max_depth=8, seed=int(rng.integers(1 << 31)), layout=abi.OR3_LAYOUT_COMPACT)
+    return s, cam, st
+
+
 def random_triangles(n=2000, seed=7, extent=100.0, size=8.0):
     """Triangle soup for closest-hit parity (random orientation, both windings)."""
     rng = np.random.default_rng(seed)

@@ -45,7 +45,7 @@ def workload(pkg, name):
         desc = "cornell_box_10tri_2spheres_256x256_ss8_64spp_rr3_maxdepth8"
     elif name == "terrain":
         sd, cam, st = W.terrain_ibl()
-        desc = "terrain_1048576tri_64glass_ibl2048x1024_1920x1080_ss32_1024spp_maxdepth12"
+        desc = "terrain_1048576tri_64glass_ibl2048x1024_envcdf_nee_1920x1080_ss32_1024spp_maxdepth12"
     else:
         sd, cam, st = W.icosphere_in_box()
         desc = "displaced_icosphere_81920tri_phong_in_cornell_1024x768_ss16_256spp_maxdepth10"

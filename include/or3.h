@@ -148,7 +148,12 @@ typedef struct or3_render_params {
   int32_t step_samples;  /* m_step_samples */
   int32_t supersamples;  /* m_supersamples (ss x ss fixed grid per pixel) */
   int32_t next_event_estimation; /* 0 = off (the reference default);
-                                    1 = light sampling with shadow rays (not in the reference) */
+                                    1 = one light sample per Lambert/Phong vertex with an
+                                    any-hit shadow ray: emissive triangles and spheres by
+                                    power, the environment by its marginal/conditional CDF.
+                                    The reference's own NEE weights by the receiver's
+                                    emission (PathTracer.cpp:311-314) and renders black;
+                                    this is the estimator it describes, not its output. */
   int32_t rr_min_depth;  /* Russian roulette for depth > this; reference MinDepth = 5 */
   int32_t max_depth;     /* rays at depth >= max_depth are not traced; 0 = unbounded (reference) */
   int32_t output_layout; /* OR3_LAYOUT_* */
@@ -196,7 +201,7 @@ typedef struct or3_scene_info {
   double build_ms;         /* host BVH build */
   double upload_ms;        /* H2D copies */
   int32_t tree_depth;
-  int32_t reserved;
+  int32_t num_lights;      /* next-event lights: in-BVH objects with an emissive layer */
 } or3_scene_info;
 
 typedef struct or3_context or3_context;
@@ -363,7 +368,7 @@ int or3_server_stop(or3_context *ctx);
  * provided by the caller).  The scene must already be uploaded.
  *
  * The ray queues live in one file-scope device array sized for
- * OR3_NOALLOC_MAX_PATHS paths (about 3.7 MB, held by every GPU that loads the
+ * OR3_NOALLOC_MAX_PATHS paths (about 5.3 MB, held by every GPU that loads the
  * library until the process exits); larger num_paths is rejected with
  * OR3_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a
  * device looks up that array's device address, so make that first call before

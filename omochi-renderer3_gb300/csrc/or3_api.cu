@@ -70,6 +70,126 @@ uint32_t layer_flags(const or3_scene_desc *d, const uint32_t *lay) {
   return f;
 }
 
+// Probability that the layer roulette (PathTracer.cpp:370-382) picks layer k.
+double layer_prob(const or3_scene_desc *d, const uint32_t *lay, uint32_t k) {
+  double lo = 0;
+  for (uint32_t j = 0; j < k; j++) lo += d->layer_rate[lay[0] + j];
+  lo = std::min(1.0, std::max(0.0, lo));
+  double hi = k + 1 == lay[1] ? 1.0 : lo + d->layer_rate[lay[0] + k];
+  hi = std::min(1.0, std::max(0.0, hi));
+  return hi > lo ? hi - lo : 0.0;
+}
+
+constexpr double kPiD = 3.14159265358979323846264338327950288419716939;
+
+// Next-event light tables.  Local lights are the in-BVH objects with an
+// emissive layer (triangles, then spheres, in description order), chosen with
+// probability proportional to area * sum(p_layer * |emission|) (the power
+// measure of SphereLight::TotalPower, src/renderer/SphereLight.h:71-78).  The
+// environment is sampled through a piecewise-constant marginal/conditional CDF
+// over max(r, g, b) * sin(theta) per texel (the reference's importance map,
+// src/renderer/IBL.h:104-189, is a stub), or uniformly over directions when
+// it is a constant background.
+struct LightTables {
+  std::vector<LightDev> lights;
+  std::vector<float> cdf, pdf, env_marg, env_cond;
+  int env_light = 0;
+  float env_prob = 0.f;
+};
+
+void build_light_tables(const or3_scene_desc *d, const std::vector<float> &geom, LightTables &T) {
+  const uint32_t nt = d->num_triangles, nsph = d->num_spheres;
+  std::vector<double> power;
+  double total = 0;
+  auto add_light = [&](const uint32_t *lay, double area, LightDev L) {
+    double le[3] = {0, 0, 0}, mag = 0;
+    for (uint32_t k = 0; k < lay[1]; k++) {
+      const double p = layer_prob(d, lay, k);
+      const double *e = d->materials[d->layer_material[lay[0] + k]].emission;
+      for (int a = 0; a < 3; a++) le[a] += e[a] * p;
+      mag += p * std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    }
+    for (int a = 0; a < 3; a++) L.le[a] = (float)le[a];
+    T.lights.push_back(L);
+    power.push_back(area * mag);
+    total += area * mag;
+  };
+  for (uint32_t i = 0; i < nt; i++) {
+    const uint32_t *lay = d->tri_layers + 2 * i;
+    if (!(layer_flags(d, lay) & kFlagEmissive)) continue;
+    const double *v = d->tri_vertices + 9 * (size_t)i;
+    const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+    const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+    const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    LightDev L{};
+    const float *g = &geom[12 * (size_t)i];
+    for (int a = 0; a < 3; a++) {
+      L.p[a] = g[a];
+      L.e1[a] = g[3 + a];
+      L.e2[a] = g[6 + a];
+    }
+    L.kind = kLightTriangle;
+    add_light(lay, 0.5 * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]), L);
+  }
+  for (uint32_t j = 0; j < nsph; j++) {
+    const uint32_t *lay = d->sphere_layers + 2 * j;
+    if (!(layer_flags(d, lay) & kFlagEmissive)) continue;
+    const double r = d->spheres[4 * (size_t)j + 3];
+    LightDev L{};
+    const float *g = &geom[12 * (size_t)(nt + j)];
+    for (int a = 0; a < 3; a++) L.p[a] = g[a];
+    L.r = g[3];
+    L.kind = kLightSphere;
+    add_light(lay, 4 * kPiD * r * r, L);
+  }
+  if (!(total > 0)) T.lights.clear();
+  const size_t nl = T.lights.size();
+  T.cdf.resize(nl);
+  T.pdf.resize(nl);
+  double run = 0;
+  for (size_t k = 0; k < nl; k++) {
+    run += power[k];
+    T.cdf[k] = k + 1 == nl ? 1.0f : (float)(run / total);
+    T.pdf[k] = (float)(power[k] / total);
+  }
+  if (d->env_rgb) {
+    const uint32_t W = d->env_width, H = d->env_height;
+    std::vector<double> rows(H);
+    T.env_cond.resize((size_t)W * H);
+    T.env_marg.resize(H);
+    auto weight = [&](uint32_t i, uint32_t j) {
+      const float *p = d->env_rgb + 3 * ((size_t)i * W + j);
+      const float mx = std::max(p[0], std::max(p[1], p[2]));
+      return (mx > 0 ? mx : 0) * std::sin(kPiD * (i + 0.5) / H);
+    };
+    double etot = 0;
+    for (uint32_t i = 0; i < H; i++) {
+      double r = 0;
+      for (uint32_t j = 0; j < W; j++) r += weight(i, j);
+      rows[i] = r;
+      etot += r;
+    }
+    for (uint32_t i = 0; i < H; i++) {
+      double r = 0;
+      for (uint32_t j = 0; j < W; j++) {
+        r += weight(i, j);
+        T.env_cond[(size_t)i * W + j] =
+            j + 1 == W ? 1.0f : rows[i] > 0 ? (float)(r / rows[i]) : (float)((j + 1.0) / W);
+      }
+    }
+    double run2 = 0;
+    for (uint32_t i = 0; i < H; i++) {
+      run2 += rows[i];
+      T.env_marg[i] = i + 1 == H ? 1.0f : etot > 0 ? (float)(run2 / etot) : (float)((i + 1.0) / H);
+    }
+    T.env_light = etot > 0 ? 1 : 0;
+  } else {
+    const double *b = d->background;
+    T.env_light = (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) != 0 ? 2 : 0;
+  }
+  T.env_prob = T.env_light ? (nl ? 0.5f : 1.0f) : 0.0f;
+}
+
 }  // namespace
 
 namespace or3 {
@@ -84,7 +204,10 @@ int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   }
   cudaFree(ctx->hits);
   cudaFree(ctx->pathL);
-  ctx->hits = ctx->pathL = nullptr;
+  cudaFree(ctx->sorig);
+  cudaFree(ctx->sdir);
+  cudaFree(ctx->scontrib);
+  ctx->hits = ctx->pathL = ctx->sorig = ctx->sdir = ctx->scontrib = nullptr;
   ctx->cap_paths = ctx->cap_rays = 0;
   for (int k = 0; k < 2; k++) {
     OR3_CUDA(ctx, cudaMalloc(&ctx->qorig[k], rays * sizeof(float4)));
@@ -93,6 +216,9 @@ int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   }
   OR3_CUDA(ctx, cudaMalloc(&ctx->hits, rays * sizeof(float4)));
   OR3_CUDA(ctx, cudaMalloc(&ctx->pathL, paths * sizeof(float4)));
+  OR3_CUDA(ctx, cudaMalloc(&ctx->sorig, rays * sizeof(float4)));
+  OR3_CUDA(ctx, cudaMalloc(&ctx->sdir, rays * sizeof(float4)));
+  OR3_CUDA(ctx, cudaMalloc(&ctx->scontrib, rays * sizeof(float4)));
   ctx->cap_paths = paths;
   ctx->cap_rays = rays;
   return OR3_OK;
@@ -130,6 +256,9 @@ Queues make_queues(or3_context *ctx) {
   }
   q.hits = ctx->hits;
   q.pathL = ctx->pathL;
+  q.sorig = ctx->sorig;
+  q.sdir = ctx->sdir;
+  q.scontrib = ctx->scontrib;
   q.counters = ctx->counters;
   q.stats = ctx->dstats;
   q.capacity = (uint32_t)ctx->cap_rays;
@@ -249,6 +378,9 @@ int or3_context_destroy(or3_context *ctx) {
   }
   cudaFree(ctx->hits);
   cudaFree(ctx->pathL);
+  cudaFree(ctx->sorig);
+  cudaFree(ctx->sdir);
+  cudaFree(ctx->scontrib);
   cudaFree(ctx->counters);
   cudaFree(ctx->dstats);
   cudaFreeHost(ctx->host_counters);
@@ -457,6 +589,19 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     S.env_w = d->env_width;
     S.env_h = d->env_height;
   }
+  {
+    LightTables T;
+    build_light_tables(d, geom, T);
+    if ((rc = dev_upload(ctx, sg, T.lights, &S.lights))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, T.cdf, &S.light_cdf))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, T.pdf, &S.light_pdf))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, T.env_marg, &S.env_marg))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, T.env_cond, &S.env_cond))) { free_scene(sg); return rc; }
+    S.num_lights = (uint32_t)T.lights.size();
+    S.env_light = T.env_light;
+    S.env_prob = T.env_prob;
+    sg->info.num_lights = (int32_t)S.num_lights;
+  }
   if (d->num_textures) {
     std::vector<TextureDev> tex(d->num_textures);
     uint64_t total = 0;
@@ -571,6 +716,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const int variant = extend_variant(prm->tuning);
   const bool timek = (prm->flags & OR3_FLAG_TIME_KERNELS) != 0;
   const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
+  const bool shadows = prm->next_event_estimation && (sg->view.num_lights > 0 || sg->view.env_light != 0);
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
@@ -602,6 +748,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
+          if (shadows) launch_shadow(sg->view, q, grid_ext, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
           launch_reset_count(q, in, st);
           in ^= 1;

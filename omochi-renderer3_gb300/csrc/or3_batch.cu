@@ -159,6 +159,7 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   std::map<int32_t, uint32_t> scene_index;
   std::vector<DevScene> scenes;
   bool split = false;
+  bool shadows = false;  // some job samples lights: the bounce loop runs the shadow kernel
   std::vector<JobDev> jd(n);
   std::vector<JobPlan> jp(n);
   std::vector<BatchBuffers::JobOut> outs(n);
@@ -173,6 +174,8 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
       scenes.push_back(it->second->view);
       split = split || it->second->has_split;
     }
+    const DevScene &sv = it->second->view;
+    shadows = shadows || (job.params.next_event_estimation && (sv.num_lights > 0 || sv.env_light != 0));
     fill_render_const(&job.camera, &job.params, jd[j].rc);
     jd[j].scene = scene_index[job.scene];
     const uint64_t npix = (uint64_t)job.camera.width * job.camera.height;
@@ -239,6 +242,7 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
       const int in = k & 1;
       launch_extend_batch(b, q, in, grid_ext, count, st);
       launch_shade_batch(b, q, in, grid_sh, st);
+      if (shadows) launch_shadow_batch(b, q, grid_ext, st);
       launch_reset_count(q, in, st);
     }
   };

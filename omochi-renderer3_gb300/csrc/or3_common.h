@@ -96,6 +96,24 @@ struct MaterialDev {
   uint32_t pad;
 };
 
+// Next-event light: an in-BVH object with an emissive layer.
+//   kind kLightTriangle: p = v0, e1, e2 (the FP32 geometry the kernels test)
+//   kind kLightSphere:   p = centre, r
+// le = emission expected over the object's layer roulette.
+constexpr uint32_t kLightTriangle = 0u;
+constexpr uint32_t kLightSphere = 1u;
+struct LightDev {
+  float p[3];
+  uint32_t kind;
+  float e1[3];
+  float r;
+  float e2[3];
+  float pad0;
+  float le[3];
+  float pad1;
+};
+static_assert(sizeof(LightDev) == 64, "LightDev must be 64 bytes");
+
 struct LayerDev {
   uint32_t material;
   float rate;

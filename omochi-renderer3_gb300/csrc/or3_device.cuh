@@ -21,18 +21,16 @@ struct DevScene {
   const float *env;            // RGB, env_w * env_h
   const TextureDev *textures;
   const float *texels;
-  // NEE light list (emissive triangles and spheres), CDF over power
-  const uint32_t *light_rec;   // record index per light
-  const float *light_cdf;      // inclusive CDF, last = 1
-  const float *light_pdf;      // selection probability per light
-  const uint32_t *rec_light;   // record -> light index (0xffffffff = none)
-  const float *env_marg_cdf;   // [env_h] inclusive marginal CDF over rows
-  const float *env_cond_cdf;   // [env_h * env_w] inclusive conditional CDF per row
-  const float *env_row_sum;    // [env_h] (for pdf)
+  // next-event estimation: local lights chosen by power, and the environment
+  const LightDev *lights;      // [num_lights]
+  const float *light_cdf;      // [num_lights] inclusive CDF, last = 1
+  const float *light_pdf;      // [num_lights] selection probability among local lights
+  const float *env_marg;       // [env_h] inclusive marginal CDF over rows
+  const float *env_cond;       // [env_h * env_w] inclusive conditional CDF per row
   uint32_t num_nodes, num_prims, num_planes, num_lights;
-  uint32_t env_w, env_h, num_textures, pad0;
-  float env_total;             // sum of luminance*sin(theta) weights (0 = none)
-  float env_select_prob;       // probability of sampling the environment in NEE
+  uint32_t env_w, env_h, num_textures;
+  int32_t env_light;           // 0 none, 1 equirect map (CDF), 2 constant background
+  float env_prob;              // probability that a light sample goes to the environment
   float bg[3];
 };
 

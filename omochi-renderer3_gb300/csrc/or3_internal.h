@@ -43,6 +43,7 @@ struct or3_context {
   size_t cap_rays = 0, cap_paths = 0;
   float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
   float4 *hits = nullptr, *pathL = nullptr;
+  float4 *sorig = nullptr, *sdir = nullptr, *scontrib = nullptr;  // shadow queue (cap_rays entries)
   uint32_t *counters = nullptr;
   unsigned long long *dstats = nullptr;
   uint32_t *host_counters = nullptr;  // pinned

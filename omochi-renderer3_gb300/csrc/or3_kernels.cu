@@ -181,7 +181,7 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 template <bool COUNT, int VARIANT>
 __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
   __shared__ uint4 snodes[kSmemNodes * 4];
-  const uint32_t n = q.counters[in];
+  const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const uint32_t ns = stage_nodes(S, snodes, smem_nodes);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&q.stats[0], (unsigned long long)n);
@@ -216,10 +216,161 @@ struct NewRay {
   uint32_t meta;
 };
 
+struct ShadowRay {
+  V3 o, d, c;  // c: radiance the path gains if nothing lies on [o, o + d * tmax)
+  float tmax;
+};
+
+// orthonormal basis {t1, t2, a} about unit a (Duff et al., "Building an
+// Orthonormal Basis, Revisited", JCGT 2017)
+__device__ __forceinline__ V3 onb_t1(V3 a) {
+  const float sg = a.z >= 0.f ? 1.0f : -1.0f;
+  const float aa = -1.0f / (sg + a.z);
+  return v3(1.0f + sg * a.x * a.x * aa, sg * a.x * a.y * aa, -sg * a.x);
+}
+__device__ __forceinline__ V3 onb_t2(V3 a) {
+  const float sg = a.z >= 0.f ? 1.0f : -1.0f;
+  const float aa = -1.0f / (sg + a.z);
+  return v3(a.x * a.y * aa, sg + a.y * a.y * aa, -a.y);
+}
+
+// first index whose inclusive CDF value exceeds u (u < 1 = cdf[n - 1])
+__device__ __forceinline__ uint32_t cdf_find(const float *cdf, uint32_t n, float u) {
+  uint32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(cdf + mid) > u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+// BRDF times colour of the vertex: Lambert rho/pi, or the Phong lobe
+// rho (n+2)/(2 pi) cos^n about the mirror direction.
+struct Brdf {
+  V3 col, mirror;
+  float exponent;
+  bool phong;
+  __device__ __forceinline__ V3 eval(V3 d) const {
+    if (!phong) return col * (1.0f / kPi);
+    const float c = dot(d, mirror);
+    return col * ((exponent + 2.0f) / (2.0f * kPi) * (c > 0.f ? powf(c, exponent) : 0.f));
+  }
+};
+
+// One next-event light sample seen from x (oriented normal nl), with the
+// draws (rl.x select, rl.y / rl.z position).  The reference's
+// DirectRadiance_Lambert (src/renderer/PathTracer.cpp:239-323) picks a
+// SphereLight by TotalPower and samples its visible cap
+// (SphereLight::SampleOnePointWithTargetPoint, src/renderer/SphereLight.h:39-69),
+// but weights the sample by the receiver's emission, which is zero there.
+// This samples what it describes, with the light's own emission, and adds
+// emissive triangles (uniform by area) and the environment (marginal /
+// conditional CDF over the equirect map, or cosine-weighted directions about
+// nl for a constant background).  c = brdf * Le * cos * G / (pdf * p_select).
+__device__ __forceinline__ bool sample_light(const DevScene &S, uint4 rl, V3 x, V3 nl, const Brdf &b,
+                                             ShadowRay &sr) {
+  const float usel = u01(rl.x), u1 = u01(rl.y), u2 = u01(rl.z);
+  sr.o = x;
+  if (usel < S.env_prob) {
+    V3 d, le;
+    float pdf;
+    if (S.env_light == 1) {
+      const uint32_t W = S.env_w, H = S.env_h;
+      const uint32_t i = cdf_find(S.env_marg, H, u1);
+      const float prev = i ? __ldg(S.env_marg + i - 1) : 0.f, pr = __ldg(S.env_marg + i) - prev;
+      const float *row = S.env_cond + (size_t)i * W;
+      const uint32_t j = cdf_find(row, W, u2);
+      const float prevc = j ? __ldg(row + j - 1) : 0.f, pc = __ldg(row + j) - prevc;
+      const float u = ((float)j + (u2 - prevc) / pc) / (float)W;
+      const float v = ((float)i + (u1 - prev) / pr) / (float)H;
+      float sp, cp, st, ct;
+      sincospif(2.0f * u, &sp, &cp);
+      sincospif(v, &st, &ct);
+      if (!(st > 0.f)) return false;
+      d = v3(st * cp, ct, st * sp);
+      pdf = pr * pc * (float)W * (float)H / (2.0f * kPi * kPi * st);
+      const float *p = S.env + 3 * ((size_t)i * W + j);
+      le = v3(p[0], p[1], p[2]);
+    } else {
+      // constant background: cosine-weighted about the receiver's normal
+      const V3 t1 = onb_t1(nl), t2 = onb_t2(nl);
+      const float ct = sqrtf(u1), st = sqrtf(1.0f - u1);
+      float sp, cp;
+      sincospif(2.0f * u2, &sp, &cp);
+      d = t1 * (st * cp) + t2 * (st * sp) + nl * ct;
+      pdf = ct * (1.0f / kPi);
+      if (!(pdf > 0.f)) return false;
+      le = v3(S.bg[0], S.bg[1], S.bg[2]);
+    }
+    const float cs = dot(d, nl);
+    if (!(cs > 0.f)) return false;
+    sr.d = d;
+    sr.tmax = kInf;
+    sr.c = b.eval(d) * le * (cs / (pdf * S.env_prob));
+    return true;
+  }
+  if (S.num_lights == 0) return false;
+  const float ul = S.env_prob > 0.f ? (usel - S.env_prob) / (1.0f - S.env_prob) : usel;
+  const uint32_t k = cdf_find(S.light_cdf, S.num_lights, ul);
+  const float psel = (1.0f - S.env_prob) * __ldg(S.light_pdf + k);
+  if (!(psel > 0.f)) return false;
+  const float4 *lp = reinterpret_cast<const float4 *>(S.lights + k);
+  const float4 q0 = __ldg(lp), q1 = __ldg(lp + 1), q2 = __ldg(lp + 2), q3 = __ldg(lp + 3);
+  V3 p;
+  float pdf_a, cl;
+  V3 d;
+  float dist2;
+  if (__float_as_uint(q0.w) == kLightTriangle) {
+    // uniform over the triangle (sqrt warping of the barycentrics)
+    const V3 v0 = v3(q0.x, q0.y, q0.z), e1 = v3(q1.x, q1.y, q1.z), e2 = v3(q2.x, q2.y, q2.z);
+    const float su = sqrtf(u1);
+    p = v0 + e1 * (su * (1.0f - u2)) + e2 * (su * u2);
+    const V3 ng = cross(e1, e2);
+    const float ln = sqrtf(dot(ng, ng));
+    pdf_a = 2.0f / ln;
+    const V3 L = p - x;
+    dist2 = dot(L, L);
+    d = L * rsqrtf(dist2);
+    // the face is only ever hit from its front (Polygon::CheckIntersection's det > EPS)
+    const float det = -dot(d, ng);
+    if (!(det > kEps)) return false;
+    cl = det / ln;
+  } else {
+    // uniform over the cap of the sphere visible from x
+    const V3 c = v3(q0.x, q0.y, q0.z);
+    const float r = q1.w;
+    const V3 diff = x - c;
+    const float dd = sqrtf(dot(diff, diff)), cmax = r / dd;
+    if (!(cmax < 1.0f)) return false;  // x inside the light (the reference skips it too)
+    const V3 ax = diff * (1.0f / dd);
+    const V3 t1 = onb_t1(ax), t2 = onb_t2(ax);
+    const float ct = 1.0f - (1.0f - cmax) * u1, st = sqrtf(fmaxf(0.f, 1.0f - ct * ct));
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    const V3 nlight = ax * ct + t1 * (st * cp) + t2 * (st * sp);
+    p = c + nlight * r;
+    pdf_a = 1.0f / (2.0f * kPi * r * r * (1.0f - cmax));
+    const V3 L = p - x;
+    dist2 = dot(L, L);
+    d = L * rsqrtf(dist2);
+    cl = -dot(d, nlight);
+    if (!(cl > 0.f)) return false;
+  }
+  const float cs = dot(d, nl);
+  if (!(cs > 0.f)) return false;
+  sr.d = d;
+  sr.tmax = sqrtf(dist2) * (1.0f - 1e-3f);
+  sr.c = b.eval(d) * v3(q3.x, q3.y, q3.z) * (cs * cl / (dist2 * pdf_a * psel));
+  return true;
+}
+
 // One path vertex: PathTracer::Radiance_internal (src/renderer/PathTracer.cpp:349-442)
-// and the three BSDFs (:445-591).  Writes 0, 1 or 2 continuation rays.
+// and the three BSDFs (:445-591).  Writes 0, 1 or 2 continuation rays, and
+// with next-event estimation on, at most one shadow ray (has_sr).
 __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &rc, const Wave &w,
-                                         const Queues &q, int in, uint32_t i, NewRay &r0, NewRay &r1) {
+                                         const Queues &q, int in, uint32_t i, NewRay &r0, NewRay &r1,
+                                         ShadowRay &sr, bool &has_sr) {
   const float4 ro = q.orig[in][i], rd = q.dir[in][i], rb = q.beta[in][i], hh = q.hits[i];
   const V3 o = ld3(ro), d = ld3(rd);
   V3 beta = ld3(rb);
@@ -233,9 +384,14 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   h.rec = __float_as_uint(hh.y);
   h.u = hh.z;
   h.v = hh.w;
+  // With next-event estimation a vertex that sampled a light (Lambert,
+  // Phong) does not also count the emission its BSDF ray reaches; a camera
+  // or mirror/glass ray (depth 0 or kMetaSpec) still does.  The reference
+  // instead counts emission at the eye vertex only (PathTracer.cpp:433-439).
+  const bool after_light_sample = rc.nee && depth > 0 && !(meta & kMetaSpec);
   if (h.rec == kMissRec) {
     // miss: IBL::Sample(ray.dir) or Scene::Background() (PathTracer.cpp:357-364)
-    add_radiance(L, beta * env_lookup(S, d));
+    if (!after_light_sample) add_radiance(L, beta * env_lookup(S, d));
     return 0;
   }
   const Surface s = surface_at(S, h, o, d);
@@ -258,9 +414,11 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   V3 col = v3(m.color[0], m.color[1], m.color[2]);
   if (m.texture >= 0) col = col * texel(S, m.texture, s.uvx, s.uvy);  // GetTexturedColor (:327-346)
 
-  // emission is counted at every vertex when NEE is off, at the eye vertex
-  // only when NEE is on (PathTracer.cpp:404-411, :433-439)
-  if (m.emissive && (depth == 0 || !rc.nee))
+  // emission: at every vertex without NEE (PathTracer.cpp:404-411, :433-439);
+  // with NEE not where a light sample already covered it (in-BVH emitters
+  // are the lights; planes are not)
+  const bool is_light = !(h.rec & kPlaneBit) && (s.flags & kFlagEmissive);
+  if (m.emissive && !(after_light_sample && is_light))
     add_radiance(L, beta * v3(m.emission[0], m.emission[1], m.emission[2]));
 
   // Russian roulette (PathTracer.cpp:398-416)
@@ -277,6 +435,21 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   const uint32_t nmeta = (depth + 1u) | (leaf << 16);
   r0.o = s.p;
   r0.meta = nmeta;
+  // next-event estimation at a Lambert or Phong vertex that survived Russian
+  // roulette; the sample is weighted 1/p_rr like the reference's direct term
+  // (Radiance_Lambert, PathTracer.cpp:453-500)
+  if (rc.nee && ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG)) {
+    Brdf b;
+    b.col = col;
+    b.phong = m.type == OR3_PHONG;
+    b.exponent = m.phong_exponent;
+    b.mirror = normalize(d - nl * (2.0f * dot(d, nl)));
+    const uint4 rl = philox(path_counter(w.g_first + path, leaf, depth, 2u), rc.seed_lo, rc.seed_hi);
+    if (sample_light(S, rl, s.p, nl, b, sr)) {
+      sr.c = sr.c * beta * (1.0f / prr);
+      has_sr = sr.c.x > 0.f || sr.c.y > 0.f || sr.c.z > 0.f;
+    }
+  }
   switch (m.type) {
     case OR3_LAMBERT: {
       // Radiance_Lambert (PathTracer.cpp:445-500).  An emitter does not
@@ -299,10 +472,12 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
       // Radiance_Specular (PathTracer.cpp:503-520)
       r0.d = normalize(d - nl * (2.0f * dot(d, nl)));
       r0.beta = beta * col * (1.0f / prr);
+      r0.meta = nmeta | kMetaSpec;
       return 1;
     }
     case OR3_REFRACTION: {
       // Radiance_Refraction (PathTracer.cpp:523-591)
+      r0.meta = nmeta | kMetaSpec;
       const bool into = dot(s.n, nl) > 0.f;
       const V3 refl = normalize(d - nl * (2.0f * dot(d, nl)));
       const float nobj = m.ior;
@@ -339,7 +514,7 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
       r1.o = s.p;
       r1.d = refr;
       r1.beta = beta * col * (Tr / prr);
-      r1.meta = (depth + 1u) | ((leaf | (1u << depth)) << 16);
+      r1.meta = (depth + 1u) | ((leaf | (1u << depth)) << 16) | kMetaSpec;
       return 2;
     }
     default: {
@@ -352,13 +527,7 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
       const float sa = sqrtf(fmaxf(0.f, 1.0f - ca * ca));
       float sn, cs;
       sincospif(2.0f * u01(rn.w), &sn, &cs);
-      // orthonormal basis about r (Duff et al., "Building an Orthonormal Basis, Revisited", JCGT 2017)
-      const float sg = copysignf(1.0f, r.z);
-      const float aa = -1.0f / (sg + r.z);
-      const float bb = r.x * r.y * aa;
-      const V3 t1 = v3(1.0f + sg * r.x * r.x * aa, sg * bb, -sg * r.x);
-      const V3 t2 = v3(bb, sg + r.y * r.y * aa, -r.y);
-      const V3 wi = normalize(t1 * (sa * cs) + t2 * (sa * sn) + r * ca);
+      const V3 wi = normalize(onb_t1(r) * (sa * cs) + onb_t2(r) * (sa * sn) + r * ca);
       const float cosn = dot(wi, nl);
       if (cosn <= 0.f) return 0;
       r0.d = wi;
@@ -382,12 +551,14 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
 // RNG numbering; continuation rays inherit it.
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in, Batch b) {
-  const uint32_t n = q.counters[in];
+  const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const int out = in ^ 1;
   const uint32_t lane = threadIdx.x & 31u;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
     NewRay r0, r1;
+    ShadowRay sr;
+    bool has_sr = false;
     int cnt = 0;
     uint32_t tag = 0;
     if (i < n) {
@@ -397,9 +568,27 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wav
         const JobDev &job = b.jobs[sg.job];
         Wave w = w0;
         w.g_first = sg.g_first - sg.wave_first;
-        cnt = shade_one(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1);
+        cnt = shade_one(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1, sr, has_sr);
       } else {
-        cnt = shade_one(S0, rc0, w0, q, in, i, r0, r1);
+        cnt = shade_one(S0, rc0, w0, q, in, i, r0, r1, sr, has_sr);
+      }
+    }
+    // warp-aggregated append to the shadow queue
+    const unsigned sm = __ballot_sync(0xFFFFFFFFu, has_sr);
+    if (sm) {
+      const int leader = __ffs(sm) - 1;
+      uint32_t sbase = 0;
+      if ((int)lane == leader) sbase = atomicAdd(&q.counters[3], (uint32_t)__popc(sm));
+      sbase = __shfl_sync(0xFFFFFFFFu, sbase, leader);
+      if (has_sr) {
+        const uint32_t pos = sbase + (uint32_t)__popc(sm & ((1u << lane) - 1u));
+        if (pos < q.capacity) {
+          q.sorig[pos] = make_float4(sr.o.x, sr.o.y, sr.o.z, q.orig[in][i].w);
+          q.sdir[pos] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.tmax);
+          q.scontrib[pos] = make_float4(sr.c.x, sr.c.y, sr.c.z, __uint_as_float(tag));
+        } else {
+          atomicOr(&q.counters[2], kErrQueue);
+        }
       }
     }
     // warp-aggregated append to the output queue
@@ -428,10 +617,40 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wav
   }
 }
 
-// Clears a consumed queue's length and its extend fetch counter.
+// Clears a consumed queue's length and its extend fetch counter, and the
+// shadow queue's length and fetch counter.
 __global__ void k_reset_count(uint32_t *counters, int which) {
   counters[which] = 0;
   counters[4 + which] = 0;
+  counters[3] = 0;
+  counters[6] = 0;
+}
+
+struct ShadowSrc {
+  const float4 *orig, *dir;
+  __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d, float &tmax) const {
+    o = ld3(orig[i]);
+    const float4 dd = dir[i];
+    d = v3(dd.x, dd.y, dd.z);
+    tmax = dd.w;
+  }
+};
+
+struct ShadowSink {
+  const float4 *orig, *contrib;
+  float4 *pathL;
+  __device__ __forceinline__ void store(const DevScene &, uint32_t i, Hit h, V3, V3) const {
+    if (h.rec != kMissRec) return;
+    add_radiance(pathL + __float_as_uint(orig[i].w), ld3(contrib[i]));
+  }
+};
+
+// Any-hit test of every queued shadow ray (persistent, lane-refilled).
+__global__ void __launch_bounds__(256) k_shadow(DevScene S, Queues q) {
+  const uint32_t n = min(q.counters[3], q.capacity);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+  persistent_trace<true, false, 2>(S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir},
+                                   ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u, nullptr, &q.counters[2]);
 }
 
 // Per-pixel sums of the wave's path radiance: one warp per pixel, lanes over
@@ -577,15 +796,11 @@ __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
   q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// persistent_trace (STEP 2) with the scene chosen per ray by its segment.
-template <bool COUNT>
-__global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in) {
-  const uint32_t n = q.counters[in];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    atomicAdd(&q.stats[0], (unsigned long long)n);
-    if (n) atomicAdd(&q.stats[2], 1ull);
-  }
-  uint32_t cnt[3] = {0u, 0u, 0u};
+// persistent_trace (STEP 2) with the scene chosen per ray by its segment
+// (src.load also returns the ray's segment).
+template <bool ANY, bool COUNT, class Src, class Sink>
+__device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t *fetch, const Src &src,
+                                            const Sink &sink, uint32_t *cnt, uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
   TravState st;
@@ -593,7 +808,6 @@ __global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in)
   uint32_t r = kNoEntry;
   bool exhausted = false;
   const uint32_t lane = threadIdx.x & 31u;
-  uint32_t *fetch = &q.counters[4 + in];
   for (;;) {
     const bool need = (r == kNoEntry) && !exhausted;
     unsigned m = __ballot_sync(0xFFFFFFFFu, need);
@@ -606,9 +820,12 @@ __global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in)
       if (need) {
         const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
         if (idx < n) {
-          const uint32_t tag = __float_as_uint(q.beta[in][idx].w);
+          V3 o, d;
+          float tmax;
+          uint32_t tag;
+          src.load(idx, o, d, tmax, tag);
           sp = &b.scenes[b.jobs[b.segs[tag].job].scene];
-          trav_init(st, ld3(q.orig[in][idx]), ld3(q.dir[in][idx]), kInf, sp->num_nodes);
+          trav_init(st, o, d, tmax, sp->num_nodes);
           r = idx;
         } else {
           exhausted = true;
@@ -617,13 +834,42 @@ __global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in)
     }
     if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
-      if (trav_step_inline<false, COUNT>(*sp, st, stk_e, stk_t, nullptr, 0u, cnt, &q.counters[2])) {
-        const Hit h = trav_finish<false>(*sp, st);
-        q.hits[r] = make_float4(h.t, __uint_as_float(h.rec), h.u, h.v);
+      if (trav_step_inline<ANY, COUNT>(*sp, st, stk_e, stk_t, nullptr, 0u, cnt, err)) {
+        sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);
         r = kNoEntry;
       }
     }
   }
+}
+
+struct BatchQueueSrc {
+  const float4 *orig, *dir, *beta;
+  __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d, float &tmax, uint32_t &tag) const {
+    o = ld3(orig[i]);
+    d = ld3(dir[i]);
+    tmax = kInf;
+    tag = __float_as_uint(beta[i].w);
+  }
+};
+
+struct BatchShadowSrc {
+  const float4 *orig, *dir, *contrib;
+  __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d, float &tmax, uint32_t &tag) const {
+    ShadowSrc{orig, dir}.load(i, o, d, tmax);
+    tag = __float_as_uint(contrib[i].w);
+  }
+};
+
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in) {
+  const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+    if (n) atomicAdd(&q.stats[2], 1ull);
+  }
+  uint32_t cnt[3] = {0u, 0u, 0u};
+  batch_trace<false, COUNT>(b, n, &q.counters[4 + in], BatchQueueSrc{q.orig[in], q.dir[in], q.beta[in]},
+                            HitSink{q.hits}, cnt, &q.counters[2]);
   if (COUNT) {
     unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
 #pragma unroll
@@ -632,12 +878,19 @@ __global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in)
       c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, ofs);
       c2 += __shfl_xor_sync(0xFFFFFFFFu, c2, ofs);
     }
-    if (lane == 0) {
+    if ((threadIdx.x & 31u) == 0) {
       atomicAdd(&q.stats[3], c0);
       atomicAdd(&q.stats[4], c1);
       atomicAdd(&q.stats[5], c2);
     }
   }
+}
+
+__global__ void __launch_bounds__(256) k_shadow_batch(Batch b, Queues q) {
+  const uint32_t n = min(q.counters[3], q.capacity);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+  batch_trace<true, false>(b, n, &q.counters[6], BatchShadowSrc{q.sorig, q.sdir, q.scontrib},
+                           ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, &q.counters[2]);
 }
 
 // One thread per pixel-sample group (ss2 consecutive paths of one pixel and
@@ -699,6 +952,14 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
 
 void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
   k_reset_count<<<1, 1, 0, st>>>(q.counters, which);
+}
+
+void launch_shadow(const DevScene &S, const Queues &q, int grid, cudaStream_t st) {
+  k_shadow<<<grid, 256, 0, st>>>(S, q);
+}
+
+void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st) {
+  k_shadow_batch<<<grid, 256, 0, st>>>(b, q);
 }
 
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,

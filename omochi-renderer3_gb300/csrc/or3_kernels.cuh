@@ -40,19 +40,27 @@ struct Wave {
 };
 
 // Ray queues in HBM (structure of arrays, ping-pong).
-//   orig: (o.xyz, path index in wave)   dir: (d.xyz, depth | leaf << 16)
-//   beta: (throughput.xyz, -)           hits: (t, record, u, v)
+//   orig: (o.xyz, path index in wave)   dir: (d.xyz, depth | leaf << 16 | spec << 24)
+//   beta: (throughput.xyz, segment)     hits: (t, record, u, v)
+// Shadow queue (next-event estimation), filled by shade, drained by k_shadow:
+//   sorig: (o.xyz, path index)  sdir: (d.xyz, tmax)  scontrib: (radiance if unoccluded, segment)
 struct Queues {
   float4 *orig[2];
   float4 *dir[2];
   float4 *beta[2];
   float4 *hits;
   float4 *pathL;  // per camera path radiance of the wave
-  uint32_t *counters;         // [0],[1] queue lengths, [2] error bits
+  float4 *sorig, *sdir, *scontrib;
+  uint32_t *counters;         // [0],[1] queue lengths, [2] error bits, [3] shadow queue length,
+                              // [4],[5] extend fetch counters, [6] shadow fetch counter
   unsigned long long *stats;  // [0] extension rays [1] shadow rays [2] bounces [3] nodes [4] tris [5] spheres
-  uint32_t capacity;          // entries per queue
+  uint32_t capacity;          // entries per queue (the shadow queue too)
   uint32_t pad;
 };
+
+// dir.w bit: the ray leaves a mirror/glass vertex (no light sample was taken
+// there, so next-event estimation still counts the emission it reaches)
+constexpr uint32_t kMetaSpec = 1u << 24;
 
 constexpr uint32_t kErrStack = 1u;
 constexpr uint32_t kErrQueue = 2u;
@@ -120,6 +128,9 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                   int grid, int block, cudaStream_t st);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
+// any-hit test of the shadow queue; unoccluded samples add to their path's radiance
+void launch_shadow(const DevScene &S, const Queues &q, int grid, cudaStream_t st);
+void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st);
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st);
 void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,

@@ -29,11 +29,12 @@ struct Scratch {
   float4 beta[2][kMaxRays];
   float4 hits[kMaxRays];
   float4 pathL[kMaxPaths];
+  float4 sorig[kMaxRays], sdir[kMaxRays], scontrib[kMaxRays];  // shadow queue
   uint32_t counters[16];
   unsigned long long stats[8];
 };
 
-// Every GPU that loads libor3.so holds this array (about 3.7 MB) until exit.
+// Every GPU that loads libor3.so holds this array (about 5.3 MB) until exit.
 // All calls share it and it keeps the last call's contents.
 static __device__ __align__(256) Scratch g_scratch;
 
@@ -86,6 +87,9 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
   }
   q.hits = sc->hits;
   q.pathL = sc->pathL;
+  q.sorig = sc->sorig;
+  q.sdir = sc->sdir;
+  q.scontrib = sc->scontrib;
   q.counters = sc->counters;
   q.stats = sc->stats;
   q.capacity = kMaxRays;
@@ -102,9 +106,11 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
   launch_raygen(rc, w, q, 0, 0, 256, st);
   int in = 0;
   uint32_t count = num_paths, errbits = 0;
+  const bool shadows = rc.nee && (S.num_lights > 0 || S.env_light != 0);
   for (int bounce = 0; count > 0 && bounce < 1 << 20; bounce++) {
     launch_extend(S, q, in, grid_ext, 256, 0, false, extend_variant(0), st);
     launch_shade(S, rc, w, q, in, grid_sh, 256, st);
+    if (shadows) launch_shadow(S, q, grid_ext, st);
     launch_reset_count(q, in, st);
     in ^= 1;
     uint32_t hc[3] = {0, 0, 0};

@@ -412,10 +412,12 @@ int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_
   };
   // resident scenes
   std::vector<DevScene> scenes;
+  bool shadows = false;  // a resident scene has lights: NEE jobs queue shadow rays
   for (auto &kv : ctx->scenes) {
     S->scene_index[kv.first] = (uint32_t)scenes.size();
     scenes.push_back(kv.second->view);
     S->split = S->split || kv.second->has_split;
+    shadows = shadows || kv.second->view.num_lights > 0 || kv.second->view.env_light != 0;
   }
   if (scenes.empty()) return bail(fail(ctx, OR3_ERR_NOT_FOUND, "upload scenes before starting the server"));
   S->cap = S->p.wave_paths ? S->p.wave_paths : (S->split ? (1ull << 23) : (1ull << 24));
@@ -456,6 +458,7 @@ int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_
     const int in = k & 1;
     launch_extend_batch(b, q, in, ctx->num_sms * ctx->occ_extend, false, st);
     launch_shade_batch(b, q, in, ctx->num_sms * ctx->occ_shade, st);
+    if (shadows) launch_shadow_batch(b, q, ctx->num_sms * ctx->occ_extend, st);
     launch_reset_count(q, in, st);
   }
   if (cudaStreamEndCapture(st, &graph) != cudaSuccess || cudaGraphInstantiate(&S->graph, graph, 0) != cudaSuccess) {

@@ -9,11 +9,15 @@
   terrain_ibl()           1024x512-cell heightfield (1,048,576 triangles) with
                           fBm heights in [0, 50], 64 glass spheres, 2048x1024
                           float sky (gradient + 0.5 degree sun of 1e4 + log-normal
-                          background); 1920x1080, ss=32 (1024 spp), max depth 12
+                          background) sampled through its CDF (next-event
+                          estimation on); 1920x1080, ss=32 (1024 spp), max depth 12
   reference_cornell()     the reference's own built-in CornellBoxScene
                           (src/scenes/CornellBoxScene.cpp:10-36): axis floors,
                           a two-layer sphere, a SphereLight
-Each returns (SceneDesc, Camera, render settings dict).
+Each returns (SceneDesc, Camera, render settings dict).  Also:
+  sphere_light_box(), sky_floor()   small next-event-estimation scenes (SceneDesc, Camera)
+  batched_jobs()                    64 uneven render jobs for the batched form
+  served_pool(), served_request()   resident scenes and Poisson requests for the served form
 """
 import math
 
@@ -61,6 +65,52 @@ def cornell_box(width=256, height=256):
     sd.add_sphere((70.0, 16.5, 60.0), 16.5, sd.layers(glass))
     settings = dict(supersamples=8, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=3, max_depth=8)
     return sd, cornell_camera(width, height), settings
+
+
+def sphere_light_box(width=64, height=64):
+    """The Cornell walls lit only by an emissive sphere flagged as a SphereLight
+    (radius 6, radiance 40), with a Phong sphere (exponent 20) and a mirror
+    sphere: next-event estimation with a sphere light and a glossy lobe."""
+    sd = SceneDesc()
+    white = sd.material(abi.OR3_LAMBERT, (0.75, 0.75, 0.75))
+    red = sd.material(abi.OR3_LAMBERT, (0.75, 0.25, 0.25))
+    blue = sd.material(abi.OR3_LAMBERT, (0.25, 0.25, 0.75))
+    lamp = sd.material(abi.OR3_LAMBERT, (0.0, 0.0, 0.0), emission=(40.0, 40.0, 40.0))
+    glossy = sd.material(abi.OR3_PHONG, (0.7, 0.7, 0.7), phong_exponent=20.0)
+    mirror = sd.material(abi.OR3_SPECULAR, (0.95, 0.95, 0.95))
+    _box_walls(sd, white, red, blue)
+    sd.add_sphere((50.0, 80.0, 50.0), 6.0, sd.layers(lamp), light=True)
+    sd.add_sphere((32.0, 15.0, 45.0), 15.0, sd.layers(glossy))
+    sd.add_sphere((72.0, 12.0, 65.0), 12.0, sd.layers(mirror))
+    return sd, cornell_camera(width, height)
+
+
+def sky_floor(width=64, height=64, env=(256, 128), seed=3, constant=None):
+    """A Lambert floor and an axis-aligned Lambert box under the synthetic sky
+    (sun of radiance 1e4), or under a constant background when `constant` is an
+    RGB triple: next-event estimation of the environment."""
+    sd = SceneDesc()
+    white = sd.material(abi.OR3_LAMBERT, (0.7, 0.7, 0.7))
+    tan = sd.material(abi.OR3_LAMBERT, (0.6, 0.5, 0.35))
+    sd.add_triangles(quad([[-200, 0, -200], [200, 0, -200], [200, 0, 200], [-200, 0, 200]], (0, 1, 0)),
+                     sd.layers(white))
+    x0, x1, y1, z0, z1 = -20.0, 20.0, 30.0, -20.0, 20.0
+    box = [
+        ([[x0, y1, z0], [x1, y1, z0], [x1, y1, z1], [x0, y1, z1]], (0, 1, 0)),
+        ([[x0, 0, z1], [x1, 0, z1], [x1, y1, z1], [x0, y1, z1]], (0, 0, 1)),
+        ([[x0, 0, z0], [x1, 0, z0], [x1, y1, z0], [x0, y1, z0]], (0, 0, -1)),
+        ([[x1, 0, z0], [x1, y1, z0], [x1, y1, z1], [x1, 0, z1]], (1, 0, 0)),
+        ([[x0, 0, z0], [x0, y1, z0], [x0, y1, z1], [x0, 0, z1]], (-1, 0, 0)),
+    ]
+    for corners, facing in box:
+        sd.add_triangles(quad(corners, facing), sd.layers(tan))
+    if constant is None:
+        sky, _ = sky_image(env[0], env[1], seed=seed)
+        sd.set_env(sky)
+    else:
+        sd.background = tuple(float(c) for c in constant)
+    cam = Camera.from_fov(width, height, (60.0, 70.0, 140.0), (0.0, 10.0, 0.0), 45.0)
+    return sd, cam
 
 
 def icosphere_in_box(width=1024, height=768, level=6, seed=2):
@@ -145,7 +195,9 @@ def terrain_ibl(width=1920, height=1080, cells_x=1024, cells_z=512, seed=3, sphe
     sky, _ = sky_image(seed=seed)
     sd.set_env(sky)
     cam = Camera.from_fov(width, height, (0.0, 140.0, 520.0), (0.0, 20.0, 0.0), 45.0)
-    settings = dict(supersamples=32, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=12)
+    # the sky is importance-sampled: next-event estimation on
+    settings = dict(supersamples=32, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=12,
+                    next_event_estimation=True)
     return sd, cam, settings
 
 

@@ -83,6 +83,7 @@ typedef struct {
   int axis;
   double offset, nsign;
   v3 bmin, bmax, bcen;
+  int light;  /* in-BVH object with an emissive layer: a next-event light */
 } obj;
 
 typedef struct {
@@ -118,6 +119,18 @@ struct orc_scene {
   const float **tex;
   uint32_t *texw, *texh;
   int ntex;
+  /* next-event estimation: local lights (emissive triangles, then emissive
+     spheres, in description order) chosen by power, and the environment */
+  int nlights;
+  int *light_obj;
+  v3 *light_le;       /* emission expected over the layer roulette */
+  float *light_cdf;   /* inclusive, last = 1 */
+  float *light_pdf;
+  int env_light;      /* 0 none, 1 equirect map, 2 constant background */
+  float *env_marg;    /* [envh] inclusive marginal CDF over rows */
+  float *env_cond;    /* [envh * envw] inclusive conditional CDF per row */
+  double env_prob;    /* probability of sampling the environment */
+  int *order;         /* object index of description entry i (triangles, spheres, planes) */
 };
 
 typedef struct {
@@ -421,12 +434,249 @@ static int scene_closest(const orc_scene *s, v3 org, v3 dir, hitrec *best) {
   return best->t != INF;
 }
 
+/* ------------------------------------------------------------------ lights
+ * Next-event estimation has no working reference counterpart: the
+ * reference's DirectRadiance_Lambert (src/renderer/PathTracer.cpp:239-323)
+ * weights the light sample by the receiving surface's emission (always 0
+ * there), and its IBL importance map (src/renderer/IBL.h:104-189) is a stub.
+ * This restates the estimator the GPU implements:
+ *   - lights: every in-BVH object with an emissive layer (triangles by area,
+ *     spheres by SphereLight::SampleOnePointWithTargetPoint's visible-cap
+ *     sampling, src/renderer/SphereLight.h:39-69), chosen with probability
+ *     proportional to area * sum(p_layer * |emission|) (SphereLight::TotalPower,
+ *     :71-78), and the environment (equirect map by a piecewise-constant
+ *     marginal/conditional CDF over max(r,g,b) * sin(theta), or a constant
+ *     background by cosine-weighted directions about the receiver's normal);
+ *     when both kinds exist, each half;
+ *   - at a Lambert or Phong vertex that survived Russian roulette, one light
+ *     sample with an any-hit shadow ray, weighted like the reference's
+ *     direct term: brdf * Le * cos * G / (pdf * p_select) / p_rr;
+ *   - emission reached by a BSDF ray is counted only after the camera or a
+ *     mirror/glass vertex, or from an object that is not a light (planes).
+ */
+static double layer_prob(const orc_scene *s, const obj *o, uint32_t k) {
+  double lo = 0;
+  for (uint32_t j = 0; j < k; j++) lo += s->lrate[o->lb + j];
+  lo = lo < 0 ? 0 : lo > 1 ? 1 : lo;
+  double hi = k + 1 == o->lc ? 1.0 : lo + s->lrate[o->lb + k];
+  hi = hi < 0 ? 0 : hi > 1 ? 1 : hi;
+  return hi > lo ? hi - lo : 0.0;
+}
+
+static void build_lights(orc_scene *s) {
+  double *power = (double *)malloc(sizeof(double) * (s->n > 0 ? s->n : 1));
+  s->light_obj = (int *)malloc(sizeof(int) * (s->n > 0 ? s->n : 1));
+  s->light_le = (v3 *)malloc(sizeof(v3) * (s->n > 0 ? s->n : 1));
+  double total = 0;
+  /* description order: triangles, then spheres (object ids may be permuted) */
+  for (int pass = 0; pass < 2; pass++)
+    for (int i = 0; i < s->n; i++) {
+      obj *o = &s->o[s->order[i]];
+      if (!o->in_bvh || o->kind != (pass == 0 ? K_TRI : K_SPHERE)) continue;
+      o->light = 0;
+      for (uint32_t k = 0; k < o->lc; k++)
+        if (s->m[s->lmat[o->lb + k]].emissive) o->light = 1;
+      if (!o->light) continue;
+      v3 le = mk(0, 0, 0);
+      double mag = 0;
+      for (uint32_t k = 0; k < o->lc; k++) {
+        const double p = layer_prob(s, o, k);
+        const v3 e = s->m[s->lmat[o->lb + k]].emission;
+        le = add(le, mul(e, p));
+        mag += p * sqrt(dot(e, e));
+      }
+      const double area = o->kind == K_TRI ? 0.5 * sqrt(dot(cross(o->e1, o->e2), cross(o->e1, o->e2)))
+                                           : 4 * PI * o->r * o->r;
+      s->light_obj[s->nlights] = s->order[i];
+      s->light_le[s->nlights] = le;
+      power[s->nlights] = area * mag;
+      total += area * mag;
+      s->nlights++;
+    }
+  if (!(total > 0)) s->nlights = 0;
+  s->light_cdf = (float *)malloc(sizeof(float) * (s->nlights > 0 ? s->nlights : 1));
+  s->light_pdf = (float *)malloc(sizeof(float) * (s->nlights > 0 ? s->nlights : 1));
+  double run = 0;
+  for (int k = 0; k < s->nlights; k++) {
+    run += power[k];
+    s->light_cdf[k] = k + 1 == s->nlights ? 1.0f : (float)(run / total);
+    s->light_pdf[k] = (float)(power[k] / total);
+  }
+  free(power);
+  /* environment */
+  if (s->env) {
+    const int W = s->envw, H = s->envh;
+    double *rows = (double *)malloc(sizeof(double) * H);
+    s->env_cond = (float *)malloc(sizeof(float) * (size_t)W * H);
+    s->env_marg = (float *)malloc(sizeof(float) * H);
+    double etot = 0;
+    for (int i = 0; i < H; i++) {
+      const double st = sin(PI * (i + 0.5) / H);
+      double r = 0;
+      for (int j = 0; j < W; j++) {
+        const float *p = s->env + 3 * ((size_t)i * W + j);
+        const float mx = p[0] > p[1] ? (p[0] > p[2] ? p[0] : p[2]) : (p[1] > p[2] ? p[1] : p[2]);
+        r += (mx > 0 ? mx : 0) * st;
+        s->env_cond[(size_t)i * W + j] = (float)r; /* running sum, normalised below */
+      }
+      rows[i] = r;
+      etot += r;
+    }
+    for (int i = 0; i < H; i++) {
+      double r = 0;
+      for (int j = 0; j < W; j++) {
+        const float *p = s->env + 3 * ((size_t)i * W + j);
+        const float mx = p[0] > p[1] ? (p[0] > p[2] ? p[0] : p[2]) : (p[1] > p[2] ? p[1] : p[2]);
+        r += (mx > 0 ? mx : 0) * sin(PI * (i + 0.5) / H);
+        s->env_cond[(size_t)i * W + j] =
+            j + 1 == W ? 1.0f : rows[i] > 0 ? (float)(r / rows[i]) : (float)((j + 1.0) / W);
+      }
+    }
+    double run2 = 0;
+    for (int i = 0; i < H; i++) {
+      run2 += rows[i];
+      s->env_marg[i] = i + 1 == H ? 1.0f : etot > 0 ? (float)(run2 / etot) : (float)((i + 1.0) / H);
+    }
+    free(rows);
+    s->env_light = etot > 0 ? 1 : 0;
+  } else {
+    s->env_light = dot(s->bg, s->bg) != 0 ? 2 : 0;
+  }
+  s->env_prob = s->env_light ? (s->nlights ? 0.5 : 1.0) : 0.0;
+}
+
+/* first index whose inclusive CDF value exceeds u */
+static int cdf_find(const float *cdf, int n, double u) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((double)cdf[mid] > u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+/* orthonormal basis about unit a (Duff et al., JCGT 2017) */
+static void onb(v3 a, v3 *t1, v3 *t2) {
+  const double sg = a.z >= 0 ? 1.0 : -1.0;
+  const double aa = -1.0 / (sg + a.z), bb = a.x * a.y * aa;
+  *t1 = mk(1.0 + sg * a.x * a.x * aa, sg * bb, -sg * a.x);
+  *t2 = mk(bb, sg + a.y * a.y * aa, -a.y);
+}
+
+static v3 env_sample(const orc_scene *s, v3 d);
+static int scene_closest(const orc_scene *s, v3 org, v3 dir, hitrec *best);
+
+/* One light sample seen from x (oriented normal nl).  brdf(d) is the vertex's
+   BRDF times its colour; returns brdf * Le * cos * G / (pdf * p_select),
+   0 when the sample is occluded or faces away. */
+typedef struct {
+  int phong;
+  double exponent;
+  v3 col, mirror;
+} brdf_t;
+
+static v3 brdf_eval(const brdf_t *b, v3 d) {
+  if (!b->phong) return mul(b->col, 1.0 / PI);
+  const double c = dot(d, b->mirror);
+  return mul(b->col, (b->exponent + 2.0) / (2.0 * PI) * (c > 0 ? pow(c, b->exponent) : 0.0));
+}
+
+static v3 nee_direct(const orc_scene *s, const double r[4], v3 x, v3 nl, const brdf_t *b) {
+  const v3 zero = mk(0, 0, 0);
+  double usel = r[0];
+  v3 d, le;
+  double pdf_w, tmax;
+  double psel;
+  if (usel < s->env_prob) {
+    psel = s->env_prob;
+    if (s->env_light == 1) {
+      const int W = s->envw, H = s->envh;
+      const int i = cdf_find(s->env_marg, H, r[1]);
+      const double prev = i ? (double)s->env_marg[i - 1] : 0.0, pr = (double)s->env_marg[i] - prev;
+      const float *row = s->env_cond + (size_t)i * W;
+      const int j = cdf_find(row, W, r[2]);
+      const double prevc = j ? (double)row[j - 1] : 0.0, pc = (double)row[j] - prevc;
+      const double u = (j + (r[2] - prevc) / pc) / W, v = (i + (r[1] - prev) / pr) / H;
+      const double th = v * PI, ph = u * 2 * PI, st = sin(th);
+      if (!(st > 0)) return zero;
+      d = mk(st * cos(ph), cos(th), st * sin(ph));
+      pdf_w = pr * pc * W * H / (2 * PI * PI * st);
+      const float *p = s->env + 3 * ((size_t)i * W + j);
+      le = mk(p[0], p[1], p[2]);
+    } else {
+      /* constant background: cosine-weighted about the receiver's normal */
+      v3 t1, t2;
+      onb(nl, &t1, &t2);
+      const double ct = sqrt(r[1]), st = sqrt(1 - r[1]), ph = 2 * PI * r[2];
+      d = add(add(mul(t1, st * cos(ph)), mul(t2, st * sin(ph))), mul(nl, ct));
+      pdf_w = ct / PI;
+      if (!(pdf_w > 0)) return zero;
+      le = s->bg;
+    }
+    const double cs = dot(d, nl);
+    if (!(cs > 0)) return zero;
+    hitrec h;
+    if (scene_closest(s, x, d, &h)) return zero;
+    return mul(mulv(brdf_eval(b, d), le), cs / (pdf_w * psel));
+  }
+  if (s->nlights == 0) return zero;
+  const double ul = s->env_prob > 0 ? (usel - s->env_prob) / (1 - s->env_prob) : usel;
+  const int k = cdf_find(s->light_cdf, s->nlights, ul);
+  psel = (1 - s->env_prob) * (double)s->light_pdf[k];
+  const obj *o = &s->o[s->light_obj[k]];
+  v3 p;
+  double pdf_a, cl;
+  if (o->kind == K_TRI) {
+    const double su = sqrt(r[1]);
+    p = add(o->p0, add(mul(o->e1, su * (1 - r[2])), mul(o->e2, su * r[2])));
+    const v3 ng = cross(o->e1, o->e2);
+    const double ln = sqrt(dot(ng, ng));
+    pdf_a = 2.0 / ln;
+    const v3 L = sub(p, x);
+    const double dist2 = dot(L, L), dist = sqrt(dist2);
+    d = mul(L, 1.0 / dist);
+    const double det = -dot(d, ng); /* Polygon::CheckIntersection's det: the face must be hit from its front */
+    if (!(det > EPS)) return zero;
+    cl = det / ln;
+    tmax = dist * (1 - 1e-3);
+    const double cs = dot(d, nl);
+    if (!(cs > 0)) return zero;
+    hitrec h;
+    if (scene_closest(s, x, d, &h) && h.t < tmax) return zero;
+    return mul(mulv(brdf_eval(b, d), s->light_le[k]), cs * cl / (dist2 * pdf_a * psel));
+  }
+  /* sphere: uniform over the cap visible from x */
+  const v3 diff = sub(x, o->c);
+  const double dd = sqrt(dot(diff, diff)), cmax = o->r / dd;
+  if (!(cmax < 1)) return zero;
+  const v3 ax = mul(diff, 1.0 / dd);
+  v3 t1, t2;
+  onb(ax, &t1, &t2);
+  const double ct = 1 - (1 - cmax) * r[1], st = sqrt(fmax(0.0, 1 - ct * ct)), ph = 2 * PI * r[2];
+  const v3 nlight = add(mul(ax, ct), add(mul(t1, st * cos(ph)), mul(t2, st * sin(ph))));
+  p = add(o->c, mul(nlight, o->r));
+  pdf_a = 1.0 / (2 * PI * o->r * o->r * (1 - cmax));
+  const v3 L = sub(p, x);
+  const double dist2 = dot(L, L), dist = sqrt(dist2);
+  d = mul(L, 1.0 / dist);
+  cl = -dot(d, nlight);
+  if (!(cl > 0)) return zero;
+  tmax = dist * (1 - 1e-3);
+  const double cs = dot(d, nl);
+  if (!(cs > 0)) return zero;
+  hitrec h;
+  if (scene_closest(s, x, d, &h) && h.t < tmax) return zero;
+  return mul(mulv(brdf_eval(b, d), s->light_le[k]), cs * cl / (dist2 * pdf_a * psel));
+}
+
 /* ------------------------------------------------------------------ construction */
 orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
   orc_scene *s = (orc_scene *)calloc(1, sizeof(orc_scene));
   const int n = (int)(d->num_triangles + d->num_spheres + d->num_planes);
   s->n = n;
   s->o = (obj *)calloc(n > 0 ? n : 1, sizeof(obj));
+  s->order = (int *)calloc(n > 0 ? n : 1, sizeof(int));
   s->m = (mat *)calloc(d->num_materials, sizeof(mat));
   for (uint32_t i = 0; i < d->num_materials; i++) {
     const or3_material *a = &d->materials[i];
@@ -447,6 +697,7 @@ orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
   for (uint32_t i = 0; i < d->num_triangles; i++) {
     const uint32_t id = d->tri_ids ? d->tri_ids[i] : base + i;
     obj *o = &s->o[id];
+    s->order[base + i] = (int)id;
     const double *v = d->tri_vertices + 9 * (size_t)i;
     o->kind = K_TRI;
     o->in_bvh = 1;
@@ -481,6 +732,7 @@ orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
   for (uint32_t i = 0; i < d->num_spheres; i++) {
     const uint32_t id = d->sphere_ids ? d->sphere_ids[i] : base + i;
     obj *o = &s->o[id];
+    s->order[base + i] = (int)id;
     const double *sp = d->spheres + 4 * (size_t)i;
     o->kind = K_SPHERE;
     o->in_bvh = 1;
@@ -496,6 +748,7 @@ orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
   for (uint32_t i = 0; i < d->num_planes; i++) {
     const uint32_t id = d->plane_ids ? d->plane_ids[i] : base + i;
     obj *o = &s->o[id];
+    s->order[base + i] = (int)id;
     const double *p = d->planes + 4 * (size_t)i;
     o->kind = (int)p[0] == OR3_PLANE_INFINITE_FLOOR ? K_FLOOR : K_PLANE;
     o->in_bvh = 0;
@@ -546,6 +799,7 @@ orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
       s->tex[i] = t;
     }
   }
+  build_lights(s);
   return s;
 }
 
@@ -564,6 +818,13 @@ void orc_scene_destroy(orc_scene *s) {
   free(s->tex);
   free(s->texw);
   free(s->texh);
+  free(s->order);
+  free(s->light_obj);
+  free(s->light_le);
+  free(s->light_cdf);
+  free(s->light_pdf);
+  free(s->env_marg);
+  free(s->env_cond);
   free(s);
 }
 
@@ -623,12 +884,15 @@ typedef struct {
   uint64_t g;
 } pathctx;
 
-static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
+/* spec: the ray leaves the camera or a mirror/glass vertex (no light sample
+   was taken there, so next-event estimation counts the emission it reaches) */
+static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth, int spec) {
   const orc_scene *s = c->s;
   const orc_params *p = c->p;
+  const int nee = p->next_event_estimation != 0;
   if (p->max_depth > 0 && depth >= p->max_depth) return mk(0, 0, 0);
   hitrec h;
-  if (!scene_closest(s, org, dir, &h)) return env_sample(s, dir);
+  if (!scene_closest(s, org, dir, &h)) return (!nee || spec) ? env_sample(s, dir) : mk(0, 0, 0);
   const obj *o = &s->o[h.obj];
   const v3 normal = dot(h.normal, dir) < 0.0 ? h.normal : mul(h.normal, -1.0);
   double r[4];
@@ -643,16 +907,36 @@ static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
   const mat *m = &s->m[s->lmat[o->lb + sel]];
   v3 col = m->color;
   if (m->texture >= 0) col = mulv(col, texel(s, m->texture, h.u, h.v));
-  const int add_emission = depth == 0 || !p->next_event_estimation;
+  /* The reference counts emission at the eye vertex only when NEE is on
+     (PathTracer.cpp:433-439); with a working light sample the emission a
+     BSDF ray reaches is counted after the camera or a delta vertex, or from
+     an object that is not a light.  Without NEE this is every vertex. */
+  const int add_emission = !nee || spec || !o->light;
   double prr = fmax(col.x, fmax(col.y, col.z));
   if (depth > 64) prr *= pow(0.5, depth - 64);
   if (depth > p->rr_min_depth) {
-    if (r[1] >= prr) return add_emission ? m->emission : s->bg;
+    /* the reference returns Background() here when NEE is on (:405-411);
+       that term has no place in the NEE estimator and is left out */
+    if (r[1] >= prr) return add_emission ? m->emission : mk(0, 0, 0);
   } else {
     prr = 1.0;
   }
   v3 income = mk(0, 0, 0);
   const v3 pos = h.pos;
+  /* light sample at a Lambert or Phong vertex whose continuation would be traced */
+  const int sample_light = nee && (p->max_depth <= 0 || depth + 1 < p->max_depth) &&
+                           ((m->type == OR3_LAMBERT && !m->emissive) || m->type == OR3_PHONG);
+  v3 direct = mk(0, 0, 0);
+  if (sample_light) {
+    double rl[4];
+    path_rand(p->seed, c->g, leaf, (uint32_t)depth, 2, rl);
+    brdf_t b;
+    b.phong = m->type == OR3_PHONG;
+    b.exponent = m->phong;
+    b.col = col;
+    b.mirror = nrm(sub(dir, mul(normal, 2 * dot(dir, normal))));
+    direct = mul(nee_direct(s, rl, pos, normal, &b), 1.0 / prr);
+  }
   switch (m->type) {
     case OR3_LAMBERT: {
       if (!m->emissive) {
@@ -661,14 +945,14 @@ static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
         const v3 v = cross(w, u);
         const double r1 = 2 * PI * r[2], r2 = sqrt(r[3]), r3 = sqrt(1 - r[3]);
         const v3 nd = nrm(add(add(mul(u, r3 * cos(r1)), mul(v, r3 * sin(r1))), mul(w, r2)));
-        const v3 in = radiance(c, pos, nd, leaf, depth + 1);
-        income = mul(mulv(col, in), 1.0 / prr);
+        const v3 in = radiance(c, pos, nd, leaf, depth + 1, 0);
+        income = add(mul(mulv(col, in), 1.0 / prr), direct);
       }
       break;
     }
     case OR3_SPECULAR: {
       const v3 rd = nrm(sub(dir, mul(normal, 2 * dot(dir, normal))));
-      income = mulv(mul(col, 1.0 / prr), radiance(c, pos, rd, leaf, depth + 1));
+      income = mulv(mul(col, 1.0 / prr), radiance(c, pos, rd, leaf, depth + 1, 1));
       break;
     }
     case OR3_REFRACTION: {
@@ -679,7 +963,7 @@ static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
       const double dd = dot(dir, normal);
       const double cos2t = 1 - nratio * nratio * (1 - dd * dd);
       if (cos2t < 0) {
-        income = mulv(mul(m->color, 1.0 / prr), radiance(c, pos, refl, leaf, depth + 1));
+        income = mulv(mul(m->color, 1.0 / prr), radiance(c, pos, refl, leaf, depth + 1, 1));
         break;
       }
       const v3 refr = nrm(sub(mul(dir, nratio), mul(h.normal, (into ? 1.0 : -1.0) * (dd * nratio + sqrt(cos2t)))));
@@ -692,13 +976,13 @@ static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
         path_rand(p->seed, c->g, leaf, (uint32_t)depth, 1, r2);
         const double pr = 0.1 + 0.8 * Fr;
         if (r2[0] < pr) {
-          income = mulv(mul(col, Fr / (prr * pr)), radiance(c, pos, refl, leaf, depth + 1));
+          income = mulv(mul(col, Fr / (prr * pr)), radiance(c, pos, refl, leaf, depth + 1, 1));
         } else {
-          income = mulv(mul(col, Tr / (prr * (1 - pr))), radiance(c, pos, refr, leaf, depth + 1));
+          income = mulv(mul(col, Tr / (prr * (1 - pr))), radiance(c, pos, refr, leaf, depth + 1, 1));
         }
       } else {
-        const v3 a = mul(radiance(c, pos, refl, leaf, depth + 1), Fr);
-        const v3 b = mul(radiance(c, pos, refr, leaf | (1u << depth), depth + 1), Tr);
+        const v3 a = mul(radiance(c, pos, refl, leaf, depth + 1, 1), Fr);
+        const v3 b = mul(radiance(c, pos, refr, leaf | (1u << depth), depth + 1, 1), Tr);
         income = mulv(mul(col, 1.0 / prr), add(a, b));
       }
       break;
@@ -717,8 +1001,9 @@ static v3 radiance(const pathctx *c, v3 org, v3 dir, uint32_t leaf, int depth) {
       const v3 wi = nrm(add(add(mul(t1, sa * cos(ph)), mul(t2, sa * sin(ph))), mul(rr, ca)));
       const double cosn = dot(wi, normal);
       if (cosn > 0) {
-        income = mulv(mul(col, (e + 2.0) / (e + 1.0) * cosn / prr), radiance(c, pos, wi, leaf, depth + 1));
+        income = mulv(mul(col, (e + 2.0) / (e + 1.0) * cosn / prr), radiance(c, pos, wi, leaf, depth + 1, 0));
       }
+      income = add(income, direct);
       break;
     }
   }
@@ -796,7 +1081,7 @@ int orc_path_radiance(const orc_scene *s, const or3_camera *cam, const orc_param
     camera_ray(&k, p, x, y, (int)(subi % p->supersamples), (int)(subi / p->supersamples),
                (uint32_t)(pix * ss2 + subi), pass_first_of(p, sidx), &o, &d);
     pathctx c = {s, p, g};
-    const v3 L = radiance(&c, o, d, 0u, 0);
+    const v3 L = radiance(&c, o, d, 0u, 0, 1);
     out[3 * i] = L.x;
     out[3 * i + 1] = L.y;
     out[3 * i + 2] = L.z;
@@ -834,7 +1119,7 @@ int orc_render(const orc_scene *s, const or3_camera *cam, const orc_params *p, i
           camera_ray(&k, p, x, y, sx, sy, (uint32_t)(pix * ss2 + subi), (uint32_t)prev, &o, &d);
           for (int sidx = prev; sidx < next; sidx++) {
             pathctx c = {s, p, ((uint64_t)sidx * npix + (uint64_t)pix) * ss2 + subi};
-            const v3 L = radiance(&c, o, d, 0u, 0);
+            const v3 L = radiance(&c, o, d, 0u, 0, 1);
             S[0] += L.x; S[1] += L.y; S[2] += L.z;
             Q[0] += L.x * L.x; Q[1] += L.y * L.y; Q[2] += L.z * L.z;
           }

@@ -69,3 +69,25 @@ def test_noalloc_rejects_more_paths_than_its_scratch(pkg):
         ctx.release(sid)
     finally:
         ctx.close()
+
+
+def test_noalloc_with_light_sampling_matches_render(pkg):
+    # next-event estimation: the scratch's shadow queue is exercised too
+    torch = pytest.importorskip("torch")
+    ctx = pkg.Context(0)
+    try:
+        sd, cam = pkg.workloads.sphere_light_box(40, 32)
+        sid = ctx.upload(sd)
+        st = dict(SETTINGS, next_event_estimation=True)
+        ctx.render(sid, cam, flags=pkg.abi.OR3_FLAG_KEEP_PATHS, **st)
+        ref = ctx.path_radiance().astype(np.float64)
+        n = pkg.abi.OR3_NOALLOC_MAX_PATHS
+        out = torch.zeros(3 * n, dtype=torch.float32, device="cuda:0")
+        ctx.render_paths_noalloc(sid, cam, 4096, n, out.data_ptr(), **st)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().reshape(n, 3).astype(np.float64)
+        ok = _close(got, ref[4096:4096 + n]).all(axis=1)
+        assert ok.all(), np.nonzero(~ok)[0][:5]
+        ctx.release(sid)
+    finally:
+        ctx.close()

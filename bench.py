@@ -209,7 +209,7 @@ def run_batched(args, pkg):
     W = pkg.workloads
     ctx = pkg.Context(0)
     t0 = time.perf_counter()
-    jobs_sd = W.batched_jobs(n=args.jobs, scale=args.scale)
+    jobs_sd = W.batched_jobs(n=args.jobs, scale=args.scale, small=args.mix == "small")
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     sids = [ctx.upload(sd) for sd, _, _ in jobs_sd]
@@ -248,20 +248,49 @@ def run_batched(args, pkg):
     line = {"metric": METRIC, "form": "batched", "value": paths / bms / 1e3, "unit": "Mpaths/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
-            "config": {"workload": "batched_%d_scenes_1k-2M_tris_log_uniform_x%g_128-1024px_16-512spp" %
-                                   (len(jobs), args.scale),
+            "config": {"workload": ("batched_%d_scenes_1k-2M_tris_log_uniform_x%g_128-1024px_16-512spp" %
+                                    (len(jobs), args.scale)) if args.mix == "config" else
+                                   ("batched_%d_small_jobs_1k-2M_tris_x%g_64-256px_16-64spp" % (len(jobs), args.scale)),
                        "triangles_total": int(tris), "camera_paths": int(paths), "scene_gen_s": gen_s,
                        "scene_upload_s": upload_s, "tuning": best},
             "plain_form": {"value": paths / plain_ms / 1e3, "ms": plain_ms, "wall_s": plain_wall,
                            "what": "the same 64 renders, one or3_render call each, scenes resident"},
             "speedup_vs_plain": plain_ms / bms, "batch_wall_s": float(np.median(batch_wall)),
+            "speedup_vs_plain_wall": plain_wall / float(np.median(batch_wall)),
             "equal_images_max_rel_diff": maxdiff}
     print(json.dumps(line), flush=True)
     ctx.close()
 
 
+def _plain_fifo(ctx, sids, reqs):
+    """The same requests through the plain form, one or3_render after another
+    (progressive frames every 16 spp through the frame callback, as the server
+    delivers them).  Returns per-request device ms and paths."""
+    durs, paths = [], []
+    for t_arr, s, cam, st in reqs:
+        st = dict(st, min_samples=1, step_samples=1)  # one pass (16 spp) per frame
+        frames = []
+        w0 = time.perf_counter()
+        ctx.render(sids[s], cam, callback=lambda *a: frames.append(a[0]), **st)
+        durs.append(time.perf_counter() - w0)
+        paths.append(cam.width * cam.height * st["supersamples"] ** 2 * st["max_samples"])
+    return np.array(durs), np.array(paths, np.float64)
+
+
+def _fifo_latency(arrivals, durs):
+    """Latency of a single FIFO renderer that starts each request when it
+    arrives or when the previous one finishes."""
+    finish, lat = 0.0, []
+    for a, d in zip(arrivals, durs):
+        start = max(a, finish)
+        finish = start + d
+        lat.append(finish - a)
+    return np.array(lat)
+
+
 def run_served(args, pkg):
-    """Served workload: Poisson requests over a resident scene pool, continuous batching."""
+    """Served workload: Poisson requests over a resident scene pool, continuous
+    batching, against the plain form replaying the same request stream."""
     W = pkg.workloads
     ctx = pkg.Context(0)
     t0 = time.perf_counter()
@@ -273,44 +302,59 @@ def run_served(args, pkg):
     eyes = [e for _, e in pool]
     results = {}
     rng = np.random.default_rng(11)
-    mean_paths = np.mean([w * h for w, h in W.SERVED_RES]) * np.mean(W.SERVED_SPP)
+    mean_paths = np.mean([w * h for w, h in W.SERVED_RES]) * np.mean(W.SERVED_SPP) * 1.0
+    # warm both forms (context queues, graph capture, first-touch of every scene)
+    for k in range(len(sids)):
+        s, cam, st = W.served_request(np.random.default_rng(k), len(sids), lambda i: eyes[i])
+        ctx.render(sids[k], cam, **dict(st, max_samples=1, min_samples=1))
     for label, rate, secs in (("stated_rate", args.rate, args.seconds),
                               ("sustainable_rate", None, args.sustain_seconds)):
         if rate is None:
             cap = results["stated_rate"]["mpaths_per_s"] * 1e6
             rate = 0.6 * cap / mean_paths
-        ctx.server_start(frame_every_samples=1)
-        submitted = 0
-        tstart = time.perf_counter()
-        tnext = tstart
+        reqs, t = [], 0.0
         while True:
-            tnext += rng.exponential(1.0 / rate)
-            if tnext - tstart > secs:
+            t += rng.exponential(1.0 / rate)
+            if t > secs:
                 break
-            time.sleep(max(0.0, tnext - time.perf_counter()))
-            s, cam, st = W.served_request(rng, len(sids), lambda k: eyes[k])
+            reqs.append((t,) + tuple(W.served_request(rng, len(sids), lambda k: eyes[k])))
+        ctx.server_start(frame_every_samples=1)
+        tstart = time.perf_counter()
+        for t_arr, s, cam, st in reqs:
+            time.sleep(max(0.0, tstart + t_arr - time.perf_counter()))
             ctx.server_submit(sids[s], cam, **st)
-            submitted += 1
         ctx.server_drain(args.drain_timeout)
         wall = time.perf_counter() - tstart
         stt = ctx.server_stats()
         ctx.server_stop()
-        results[label] = {"rate_req_per_s": rate, "arrival_window_s": secs, "requests": submitted,
+        durs, paths = _plain_fifo(ctx, sids, reqs)
+        lat = _fifo_latency([r[0] for r in reqs], durs)
+        served_rate = stt["camera_paths"] / max(stt["busy_s"], 1e-9) / 1e6
+        plain_rate = paths.sum() / durs.sum() / 1e6
+        results[label] = {"rate_req_per_s": rate, "arrival_window_s": secs, "requests": len(reqs),
                           "latency_p50_s": stt["latency_p50_s"], "latency_p99_s": stt["latency_p99_s"],
                           "queue_p50_s": stt["queue_p50_s"], "queue_p99_s": stt["queue_p99_s"],
                           "first_frame_p50_s": stt["first_frame_p50_s"],
                           "mpaths_per_s": stt["camera_paths"] / (stt["device_ms"] / 1e3) / 1e6,
-                          "mpaths_per_s_wall": stt["camera_paths"] / max(stt["busy_s"], 1e-9) / 1e6,
+                          "mpaths_per_s_wall": served_rate,
                           "camera_paths": stt["camera_paths"], "wall_s": wall,
-                          "peak_active_jobs": stt["peak_active_jobs"]}
+                          "peak_active_jobs": stt["peak_active_jobs"],
+                          "plain_form": {"mpaths_per_s_wall": plain_rate,
+                                         "fifo_latency_p50_s": float(np.percentile(lat, 50)),
+                                         "fifo_latency_p99_s": float(np.percentile(lat, 99)),
+                                         "busy_s": float(durs.sum()),
+                                         "what": "same requests, one blocking or3_render each (frame per 16 spp), "
+                                                 "FIFO from the same arrival times"},
+                          "served_over_plain_wall": served_rate / plain_rate}
     sr = results["stated_rate"]
-    line = {"metric": METRIC, "form": "served", "value": sr["mpaths_per_s"], "unit": "Mpaths/s", "n_gpus": 1,
-            "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+    line = {"metric": METRIC, "form": "served", "value": sr["mpaths_per_s_wall"], "unit": "Mpaths/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, Poisson arrivals)",
             "config": {"workload": "served_%d_scenes_10k-4M_tris_x%g_env%dx%d" % (args.scenes, args.scale,
                                                                                 args.env_w, args.env_h),
                        "scene_gen_s": gen_s, "scene_upload_s": upload_s,
-                       "requests": "res {256^2,512^2,1280x720,1920x1080} x spp {16,64,256,1024}, frames every 16 spp"},
+                       "requests": "res {256^2,512^2,1280x720,1920x1080} x spp {16,64,256,1024}, frames every 16 spp",
+                       "value": "camera paths / server busy wall time at the stated rate"},
             "served": results}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -332,6 +376,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--mix", default="config", choices=["config", "small"],
+                    help="batched jobs: the stated mix, or small jobs (64-256 px, 16-64 spp)")
     ap.add_argument("--scenes", type=int, default=32)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--seconds", type=float, default=2.0)
@@ -383,7 +429,8 @@ def main():
     time.sleep(0.3)
     barrier(dist)
     torch.cuda.synchronize()
-    render_ms = ext_ms = 0.0
+    render_ms = ext_ms = shade_ms = 0.0
+    shadow_rays = 0
     ext_launches = paths = ext_rays = bounces = waves = passes = 0
     w0 = time.perf_counter()
     for i in range(args.steps):
@@ -391,6 +438,8 @@ def main():
         s = ctx.render(sid, cam, seed=i, flags=A.OR3_FLAG_TIME_KERNELS, **kw)
         render_ms += s["render_ms"]
         ext_ms += s["extend_ms"]
+        shade_ms += s["shade_ms"]
+        shadow_rays += s["shadow_rays"]
         ext_launches += s["extend_launches"]
         paths += s["camera_paths"]
         ext_rays += s["extension_rays"]
@@ -419,7 +468,8 @@ def main():
     e2e_s = max_over_ranks(dist, time.perf_counter() - e0)
     e2e_paths = sum_over_ranks(dist, float(paths / args.steps * e2e_steps))
 
-    launches = 2 * waves + 3 * bounces + passes
+    # per wave raygen + accumulate; per bounce extend, shade, reset (+ shadow with NEE); per pass frame
+    launches = 2 * waves + (4 if shadow_rays else 3) * ext_launches + passes
     avg_ext_ms = ext_ms / max(ext_launches, 1)
     achieved = alg_bytes_per_ray * ext_rays / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else None
     peak, peak_kind = load_peaks()
@@ -436,7 +486,10 @@ def main():
                        "wide_nodes": int(info["num_nodes"]), "scene_upload_ms": upload_s * 1000.0,
                        "bvh_build_ms": info["build_ms"], "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "wall_s_timed": wall_s, "mrays_per_s": ext_rays / (render_ms / 1000.0) / 1e6},
+                       "wall_s_timed": wall_s, "shadow_rays_per_step": shadow_rays // args.steps,
+                       "mrays_per_s": (ext_rays + shadow_rays) / (render_ms / 1000.0) / 1e6,
+                       "extend_ms_per_step": ext_ms / args.steps,
+                       "shade_and_shadow_ms_per_step": shade_ms / args.steps},
             "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": frame_bytes,
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},

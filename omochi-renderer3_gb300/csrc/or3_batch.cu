@@ -241,7 +241,7 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     for (int k = 0; k < unroll; k++) {
       const int in = k & 1;
       launch_extend_batch(b, q, in, grid_ext, count, st);
-      launch_shade_batch(b, q, in, grid_sh, st);
+      launch_shade_batch(b, q, in, grid_sh, shadows, st);
       if (shadows) launch_shadow_batch(b, q, grid_ext, st);
       launch_reset_count(q, in, st);
     }

@@ -367,7 +367,10 @@ __device__ __forceinline__ bool sample_light(const DevScene &S, uint4 rl, V3 x, 
 
 // One path vertex: PathTracer::Radiance_internal (src/renderer/PathTracer.cpp:349-442)
 // and the three BSDFs (:445-591).  Writes 0, 1 or 2 continuation rays, and
-// with next-event estimation on, at most one shadow ray (has_sr).
+// with next-event estimation on, at most one shadow ray (has_sr).  NEE
+// compiles the light-sampling code in (a separate instance keeps the
+// registers of the plain shade kernel at their NEE-free count).
+template <bool NEE>
 __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &rc, const Wave &w,
                                          const Queues &q, int in, uint32_t i, NewRay &r0, NewRay &r1,
                                          ShadowRay &sr, bool &has_sr) {
@@ -438,7 +441,7 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   // next-event estimation at a Lambert or Phong vertex that survived Russian
   // roulette; the sample is weighted 1/p_rr like the reference's direct term
   // (Radiance_Lambert, PathTracer.cpp:453-500)
-  if (rc.nee && ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG)) {
+  if (NEE && rc.nee && ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG)) {
     Brdf b;
     b.col = col;
     b.phong = m.type == OR3_PHONG;
@@ -549,8 +552,8 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
 
 // BATCH: the ray's segment (beta.w) selects the job's scene, constants and
 // RNG numbering; continuation rays inherit it.
-template <bool BATCH>
-__global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in, Batch b) {
+template <bool BATCH, bool NEE>
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in, Batch b) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const int out = in ^ 1;
   const uint32_t lane = threadIdx.x & 31u;
@@ -568,13 +571,13 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, RenderConst rc0, Wav
         const JobDev &job = b.jobs[sg.job];
         Wave w = w0;
         w.g_first = sg.g_first - sg.wave_first;
-        cnt = shade_one(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1, sr, has_sr);
+        cnt = shade_one<NEE>(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1, sr, has_sr);
       } else {
-        cnt = shade_one(S0, rc0, w0, q, in, i, r0, r1, sr, has_sr);
+        cnt = shade_one<NEE>(S0, rc0, w0, q, in, i, r0, r1, sr, has_sr);
       }
     }
     // warp-aggregated append to the shadow queue
-    const unsigned sm = __ballot_sync(0xFFFFFFFFu, has_sr);
+    const unsigned sm = NEE ? __ballot_sync(0xFFFFFFFFu, has_sr) : 0u;
     if (sm) {
       const int leader = __ffs(sm) - 1;
       uint32_t sbase = 0;
@@ -947,7 +950,10 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                   int grid, int block, cudaStream_t st) {
-  k_shade<false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+  if (rc.nee && (S.num_lights > 0 || S.env_light != 0))
+    k_shade<false, true><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+  else
+    k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
 }
 
 void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
@@ -1004,7 +1010,7 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
 }
 
 const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }
-const void *kernel_shade_ptr() { return (const void *)k_shade<false>; }
+const void *kernel_shade_ptr() { return (const void *)k_shade<false, false>; }
 
 // ---------------------------------------------------------------- batched form
 
@@ -1017,8 +1023,9 @@ void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool
   else k_extend_batch<false><<<grid, 256, 0, st>>>(b, q, in);
 }
 
-void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, cudaStream_t st) {
-  k_shade<true><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
+void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool nee, cudaStream_t st) {
+  if (nee) k_shade<true, true><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
+  else k_shade<true, false><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
 }
 
 void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st) {

@@ -105,7 +105,8 @@ struct Batch {
 
 void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, int out, cudaStream_t st);
 void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, cudaStream_t st);
-void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, cudaStream_t st);
+// nee: some job samples lights (the light-sampling instance of the kernel)
+void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool nee, cudaStream_t st);
 void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st);
 
 struct LaunchCfg {

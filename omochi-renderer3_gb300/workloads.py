@@ -309,11 +309,13 @@ def _mesh_scene(rng, tris, kind, env_size=(512, 256)):
     return sd, cam
 
 
-def batched_jobs(n=64, seed=4, scale=1.0):
+def batched_jobs(n=64, seed=4, scale=1.0, small=False):
     """Batched workload: n seeded scenes, triangle counts log-uniform in [1k, 2M] (x scale),
     alternating displaced icospheres and heightfields, mixed Lambert/mirror/glass,
     square images with sides uniform in [128, 1024], spp uniform in [16, 512]
-    (a 4x4 sub-pixel grid times spp/16 samples).  Returns [(SceneDesc, Camera, settings)]."""
+    (a 4x4 sub-pixel grid times spp/16 samples).  small: sides in [64, 256] and
+    spp in {16, 32, 48, 64} instead (the jobs a single render cannot fill the GPU
+    with).  Returns [(SceneDesc, Camera, settings)]."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -321,6 +323,9 @@ def batched_jobs(n=64, seed=4, scale=1.0):
         sd, eye = _mesh_scene(rng, tris, i % 2)
         side = int(rng.integers(128, 1025))
         spp = int(rng.integers(16, 513)) // 16 * 16 or 16
+        if small:
+            side = 64 + side * 192 // 1024
+            spp = 16 * (1 + spp * 4 // 528)
         if eye is None:
             cam = cornell_camera(side, side)
         else:

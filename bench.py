@@ -37,6 +37,11 @@ import __graft_entry__ as ge  # noqa: E402
 
 METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency when served"
 
+# DRAM bytes (read + write) per ray of the extend kernel, from one ncu capture
+# per workload (profiles/k_extend_<workload>_*.md); roofline.traffic is this
+# times the rays of an average launch.
+EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.0}
+
 
 def workload(pkg, name):
     W = pkg.workloads
@@ -123,7 +128,8 @@ def cpu_baseline(pkg, sd, cam, st, target_s=15.0, nthreads=None):
     ss2 = st["supersamples"] ** 2
     total = cam.width * cam.height * ss2 * st["max_samples"]
     kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
-              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"], seed=1)
+              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"], seed=1,
+              next_event_estimation=st.get("next_event_estimation", False))
     chunks = 64
     # calibrate
     probe = 4096
@@ -410,7 +416,8 @@ def main():
         desc += "_ss%d" % args.ss
     A = pkg.abi
     kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
-              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"])
+              step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"],
+              next_event_estimation=st.get("next_event_estimation", False))
     t0 = time.perf_counter()
     sid = ctx.upload(sd)
     upload_s = time.perf_counter() - t0
@@ -495,7 +502,11 @@ def main():
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None, "traffic": None,
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": (EXTEND_DRAM_BYTES_PER_RAY[args.workload] * ext_rays / max(ext_launches, 1)
+                                     if args.workload in EXTEND_DRAM_BYTES_PER_RAY else None),
+                         "traffic_unit": "bytes per launch",
+                         "alg_bytes_per_launch": alg_bytes_per_ray * ext_rays / max(ext_launches, 1),
                          "alg_bytes_per_ray": alg_bytes_per_ray, "avg_launch_ms": avg_ext_ms,
                          "launches": ext_launches},
             "cpu_baseline": cpu,

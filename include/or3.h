@@ -136,9 +136,8 @@ typedef struct or3_camera {
 #define OR3_LAYOUT_COMPACT 1   /* W x H doubles, rows top-down */
 
 #define OR3_FLAG_KEEP_PATHS 1u   /* keep per-path radiance of the last wave (testing) */
-#define OR3_FLAG_UNSORTED 2u     /* shade without partitioning rays by material */
-#define OR3_FLAG_NO_GRAPH 4u     /* launch the bounce loop without a CUDA graph */
-#define OR3_FLAG_NO_TAIL 8u      /* no single-launch tail for the last few rays */
+/* bits 2 and 8 are reserved */
+#define OR3_FLAG_NO_GRAPH 4u     /* batched/served forms: launch the bounce loop without a CUDA graph */
 #define OR3_FLAG_TIME_KERNELS 16u      /* CUDA events around every extend/shade launch */
 #define OR3_FLAG_COUNT_TRAVERSAL 32u   /* count nodes and primitives visited (slower) */
 

@@ -24,9 +24,7 @@ OR3_SPHERE_LIGHT = 1
 OR3_PLANE_AXIS_ALIGNED, OR3_PLANE_INFINITE_FLOOR = 0, 1
 OR3_LAYOUT_REFERENCE, OR3_LAYOUT_COMPACT = 0, 1
 OR3_FLAG_KEEP_PATHS = 1
-OR3_FLAG_UNSORTED = 2
 OR3_FLAG_NO_GRAPH = 4
-OR3_FLAG_NO_TAIL = 8
 OR3_FLAG_TIME_KERNELS = 16
 OR3_FLAG_COUNT_TRAVERSAL = 32
 

@@ -313,7 +313,8 @@ def batched_jobs(n=64, seed=4, scale=1.0, small=False):
     """Batched workload: n seeded scenes, triangle counts log-uniform in [1k, 2M] (x scale),
     alternating displaced icospheres and heightfields, mixed Lambert/mirror/glass,
     square images with sides uniform in [128, 1024], spp uniform in [16, 512]
-    (a 4x4 sub-pixel grid times spp/16 samples).  small: sides in [64, 256] and
+    (a 4x4 sub-pixel grid times spp/16 samples), next-event estimation on (the
+    box's light quad, or the sky through its CDF).  small: sides in [64, 256] and
     spp in {16, 32, 48, 64} instead (the jobs a single render cannot fill the GPU
     with).  Returns [(SceneDesc, Camera, settings)]."""
     rng = np.random.default_rng(seed)
@@ -331,7 +332,7 @@ def batched_jobs(n=64, seed=4, scale=1.0, small=False):
         else:
             cam = Camera.from_fov(side, side, eye, (0.0, 0.0, 0.0), 50.0)
         st = dict(supersamples=4, min_samples=spp // 16, max_samples=spp // 16, step_samples=1,
-                  rr_min_depth=5, max_depth=8, seed=1000 + i)
+                  rr_min_depth=5, max_depth=8, seed=1000 + i, next_event_estimation=True)
         out.append((sd, cam, st))
     return out
 
@@ -359,7 +360,8 @@ def served_request(rng, pool_size, eye_of):
     spp = SERVED_SPP[int(rng.integers(len(SERVED_SPP)))]
     cam = Camera.from_fov(w, h, eye_of(s), (0.0, 0.0, 0.0), 50.0)
     st = dict(supersamples=4, min_samples=spp // 16, max_samples=spp // 16, step_samples=1, rr_min_depth=5,
-              max_depth=8, seed=int(rng.integers(1 << 31)), layout=abi.OR3_LAYOUT_COMPACT)
+              max_depth=8, seed=int(rng.integers(1 << 31)), layout=abi.OR3_LAYOUT_COMPACT,
+              next_event_estimation=True)
     return s, cam, st
 
 

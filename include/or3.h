@@ -116,7 +116,17 @@ typedef struct or3_scene_desc {
   const uint32_t *texture_dims;    /* [n][2] width, height */
   const uint64_t *texture_offsets; /* [n] float offset into texture_rgb */
   const float *texture_rgb;
+
+  /* where the BVH is built (OR3_BUILD_*); zero-initialised = automatic */
+  uint32_t build;
 } or3_scene_desc;
+
+/* BVH build location.  Both build the same kind of tree (binned SAH, 16 bins,
+   leaves <= 4, 4-wide, 8-bit child boxes); closest hits are the same. */
+#define OR3_BUILD_AUTO 0u    /* device for >= OR3_BUILD_DEVICE_MIN_PRIMS in-BVH primitives, else host */
+#define OR3_BUILD_HOST 1u    /* host threads (bvh_build.cpp) */
+#define OR3_BUILD_DEVICE 2u  /* the GPU (bvh_build_gpu.cu), up to 2^26 primitives */
+#define OR3_BUILD_DEVICE_MIN_PRIMS 16384u
 
 /* ---- camera (src/renderer/Camera.h:12-43, :65-93; Aperture.h:23-35) ---- */
 typedef struct or3_camera {

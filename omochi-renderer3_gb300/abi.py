@@ -23,6 +23,8 @@ OR3_LAMBERT, OR3_SPECULAR, OR3_REFRACTION, OR3_PHONG = 0, 1, 2, 3
 OR3_SPHERE_LIGHT = 1
 OR3_PLANE_AXIS_ALIGNED, OR3_PLANE_INFINITE_FLOOR = 0, 1
 OR3_LAYOUT_REFERENCE, OR3_LAYOUT_COMPACT = 0, 1
+OR3_BUILD_AUTO, OR3_BUILD_HOST, OR3_BUILD_DEVICE = 0, 1, 2
+OR3_BUILD_DEVICE_MIN_PRIMS = 16384
 OR3_FLAG_KEEP_PATHS = 1
 OR3_FLAG_NO_GRAPH = 4
 OR3_FLAG_TIME_KERNELS = 16
@@ -54,7 +56,7 @@ class SceneDescC(ctypes.Structure):
         ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32), ("env_rgb", f32p),
         ("background", c_double3),
         ("num_textures", ctypes.c_uint32), ("texture_dims", u32p), ("texture_offsets", P(ctypes.c_uint64)),
-        ("texture_rgb", f32p),
+        ("texture_rgb", f32p), ("build", ctypes.c_uint32),
     ]
 
 

@@ -20,7 +20,8 @@ LIB_PATH = os.path.join(LIB_DIR, "libor3.so")
 CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["or3_kernels.cu", "or3_api.cu", "or3_batch.cu", "or3_server.cu", "or3_noalloc.cu", "bvh_build.cpp"]
+SOURCES = ["or3_kernels.cu", "or3_api.cu", "or3_batch.cu", "or3_server.cu", "or3_noalloc.cu", "bvh_build.cpp",
+           "bvh_build_gpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

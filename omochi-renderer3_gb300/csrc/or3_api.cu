@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "bvh_build_gpu.h"
 #include "or3.h"
 #include "or3_internal.h"
 #include "or3_kernels.cuh"
@@ -35,6 +36,34 @@ int dev_upload(or3_context *ctx, SceneGPU *sg, const std::vector<T> &v, const T 
   *out = static_cast<const T *>(p);
   return OR3_OK;
 }
+
+template <class T>
+int dev_alloc(or3_context *ctx, SceneGPU *sg, T **out, size_t n) {
+  *out = nullptr;
+  void *p = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  sg->allocs.push_back(p);
+  sg->info.device_bytes += n * sizeof(T);
+  *out = static_cast<T *>(p);
+  return OR3_OK;
+}
+
+// Device buffers that live only during one upload.
+struct DeviceTemps {
+  std::vector<void *> p;
+  template <class T>
+  int alloc(or3_context *ctx, T **out, size_t n) {
+    *out = nullptr;
+    void *q = nullptr;
+    OR3_CUDA(ctx, cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    p.push_back(q);
+    *out = static_cast<T *>(q);
+    return OR3_OK;
+  }
+  ~DeviceTemps() {
+    for (void *q : p) cudaFree(q);
+  }
+};
 
 void free_scene(SceneGPU *sg) {
   for (void *p : sg->allocs) cudaFree(p);
@@ -499,19 +528,53 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     pinfo[i] = PrimInfo{d->sphere_ids ? d->sphere_ids[j] : nt + j, lay[0], lay[1], kPrimSphere | (fl << 8)};
   }
 
-  WideBVH bvh;
-  std::string berr;
-  if (!build_wide_bvh(bp, 16, 4, bvh, &berr)) {
+  // ---- BVH: host threads, or the device for large scenes (same tree rules)
+  if (d->build > OR3_BUILD_DEVICE) {
     free_scene(sg);
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s", berr.c_str());
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "unknown build location %u", d->build);
+  }
+  const bool on_device = np > 0 && np <= (1u << 26) &&
+                         (d->build == OR3_BUILD_DEVICE ||
+                          (d->build == OR3_BUILD_AUTO && np >= OR3_BUILD_DEVICE_MIN_PRIMS));
+  WideBVH bvh;
+  DeviceBVH dbvh;
+  DeviceTemps tmp;  // freed when the upload returns (after its stream sync)
+  std::string berr;
+  if (!on_device) {
+    if (!build_wide_bvh(bp, 16, 4, bvh, &berr)) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s", berr.c_str());
+    }
+  } else {
+    for (const BuildPrim &b : bp)
+      for (int a = 0; a < 3; a++)
+        if (!(b.lo[a] <= b.hi[a]) || !std::isfinite(b.lo[a]) || !std::isfinite(b.hi[a])) {
+          free_scene(sg);
+          return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "build_wide_bvh: primitive with invalid or non-finite bounds");
+        }
+    BuildPrim *bp_dev = nullptr;
+    if (int rc = tmp.alloc(ctx, &bp_dev, np)) { free_scene(sg); return rc; }
+    const cudaError_t ce = cudaMemcpyAsync(bp_dev, bp.data(), np * sizeof(BuildPrim), cudaMemcpyHostToDevice,
+                                           ctx->stream);
+    if (ce != cudaSuccess) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(ce));
+    }
+    if (!build_wide_bvh_device(bp_dev, np, 4, ctx->stream, dbvh, &berr)) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_CUDA, "%s", berr.c_str());
+    }
+    sg->allocs.push_back(dbvh.nodes);
+    tmp.p.push_back(dbvh.order);
   }
   auto t1 = std::chrono::steady_clock::now();
 
-  // ---- records in leaf order
-  std::vector<float4> prims(3 * (size_t)np);
-  std::vector<PrimInfo> info(np);
-  std::vector<TriShade> shade(np);
-  for (uint32_t r = 0; r < np; r++) {
+  // ---- records in leaf order (the device build gathers them on the device)
+  const uint32_t nrec = on_device ? 0u : np;
+  std::vector<float4> prims(3 * (size_t)nrec);
+  std::vector<PrimInfo> info(nrec);
+  std::vector<TriShade> shade(nrec);
+  for (uint32_t r = 0; r < nrec; r++) {
     const uint32_t src = bvh.order[r];
     const float *g = &geom[12 * (size_t)src];
     if (src < nt) {
@@ -567,19 +630,55 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   sg->has_split = split;
 
   DevScene &S = sg->view;
-  S.num_nodes = (uint32_t)bvh.nodes.size();
+  S.num_nodes = on_device ? dbvh.num_nodes : (uint32_t)bvh.nodes.size();
   S.num_prims = np;
   S.num_planes = d->num_planes;
   S.bg[0] = (float)d->background[0];
   S.bg[1] = (float)d->background[1];
   S.bg[2] = (float)d->background[2];
   int rc = OR3_OK;
-  const WideNode *nodes_dev = nullptr;
-  if ((rc = dev_upload(ctx, sg, bvh.nodes, &nodes_dev))) { free_scene(sg); return rc; }
-  S.nodes = reinterpret_cast<const uint4 *>(nodes_dev);
-  if ((rc = dev_upload(ctx, sg, prims, &S.prims))) { free_scene(sg); return rc; }
-  if ((rc = dev_upload(ctx, sg, info, &S.info))) { free_scene(sg); return rc; }
-  if ((rc = dev_upload(ctx, sg, shade, &S.tri_shade))) { free_scene(sg); return rc; }
+  if (!on_device) {
+    const WideNode *nodes_dev = nullptr;
+    if ((rc = dev_upload(ctx, sg, bvh.nodes, &nodes_dev))) { free_scene(sg); return rc; }
+    S.nodes = reinterpret_cast<const uint4 *>(nodes_dev);
+    if ((rc = dev_upload(ctx, sg, prims, &S.prims))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, info, &S.info))) { free_scene(sg); return rc; }
+    if ((rc = dev_upload(ctx, sg, shade, &S.tri_shade))) { free_scene(sg); return rc; }
+  } else {
+    S.nodes = reinterpret_cast<const uint4 *>(dbvh.nodes);
+    sg->info.device_bytes += (size_t)dbvh.num_nodes * sizeof(WideNode);
+    // input-order records (temporary) gathered into leaf order
+    float4 *geom_in = nullptr;
+    PrimInfo *info_in = nullptr;
+    TriShade *shade_in = nullptr;
+    if ((rc = tmp.alloc(ctx, &geom_in, 3 * (size_t)np)) || (rc = tmp.alloc(ctx, &info_in, np)) ||
+        (rc = tmp.alloc(ctx, &shade_in, np))) {
+      free_scene(sg);
+      return rc;
+    }
+    cudaError_t ce = cudaMemcpyAsync(geom_in, geom.data(), 12 * sizeof(float) * (size_t)np, cudaMemcpyHostToDevice,
+                                     ctx->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(info_in, pinfo.data(), np * sizeof(PrimInfo), cudaMemcpyHostToDevice, ctx->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(shade_in, tshade.data(), np * sizeof(TriShade), cudaMemcpyHostToDevice, ctx->stream);
+    if (ce != cudaSuccess) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(ce));
+    }
+    float4 *prims_d = nullptr;
+    PrimInfo *info_d = nullptr;
+    TriShade *shade_d = nullptr;
+    if ((rc = dev_alloc(ctx, sg, &prims_d, 3 * (size_t)np)) || (rc = dev_alloc(ctx, sg, &info_d, np)) ||
+        (rc = dev_alloc(ctx, sg, &shade_d, np))) {
+      free_scene(sg);
+      return rc;
+    }
+    gather_leaf_order(np, dbvh.order, geom_in, info_in, shade_in, prims_d, info_d, shade_d, ctx->stream);
+    S.prims = prims_d;
+    S.info = info_d;
+    S.tri_shade = shade_d;
+  }
   if ((rc = dev_upload(ctx, sg, planes, &S.planes))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, mats, &S.materials))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, layers, &S.layers))) { free_scene(sg); return rc; }
@@ -623,10 +722,10 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   }
   auto t2 = std::chrono::steady_clock::now();
   sg->info.num_primitives = np + d->num_planes;
-  sg->info.num_nodes = bvh.nodes.size();
+  sg->info.num_nodes = S.num_nodes;
   sg->info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   sg->info.upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
-  sg->info.tree_depth = bvh.wide_depth;
+  sg->info.tree_depth = on_device ? dbvh.wide_depth : bvh.wide_depth;
   const int32_t id = ctx->next_scene++;
   ctx->scenes[id] = sg;
   *scene_out = id;

@@ -65,6 +65,7 @@ class SceneDesc:
     env: np.ndarray = None
     background: tuple = (0.0, 0.0, 0.0)
     textures: list = field(default_factory=list)
+    build: int = 0  # abi.OR3_BUILD_*
 
     # ---- materials
     def material(self, mtype=abi.OR3_LAMBERT, color=(0, 0, 0), emission=(0, 0, 0), ior=0.0,
@@ -256,6 +257,7 @@ class SceneDesc:
             d.texture_dims = _ptr(a["texture_dims"], ctypes.c_uint32)
             d.texture_offsets = _ptr(a["texture_offsets"], ctypes.c_uint64)
             d.texture_rgb = _ptr(a["texture_rgb"], ctypes.c_float)
+        d.build = self.build
         return d, keep
 
 

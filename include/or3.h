@@ -106,9 +106,12 @@ typedef struct or3_scene_desc {
   const uint32_t *plane_layers; /* [n][2] */
   const uint32_t *plane_ids;    /* [n] or NULL */
 
-  /* IBL equirect image (src/renderer/IBL.h:30-45), row-major RGB float */
+  /* IBL equirect image (src/renderer/IBL.h:30-45), row-major: RGB float, or
+     RGBE bytes (4 per texel, HDRImage's encoding, decoded on the device; see
+     or3_read_hdr).  Both NULL = no IBL: misses return `background`. */
   uint32_t env_width, env_height;
-  const float *env_rgb;  /* NULL = no IBL: misses return `background` */
+  const float *env_rgb;
+  const uint8_t *env_rgbe;
   double background[3];  /* Scene::Background() (src/scenes/Scene.h:40) */
 
   /* textures (src/tools/Image.h:20-31): RGB float, linear */
@@ -362,6 +365,38 @@ int or3_server_get_stats(or3_context *ctx, or3_server_stats *stats_out);
 int or3_server_get_moments(or3_context *ctx, uint64_t job_id, double *sum_host, double *sumsq_host,
                            size_t capacity, uint64_t *count_out);
 int or3_server_stop(or3_context *ctx);
+
+/* Served form with progressive frames encoded on the device to 8-bit RGB
+   (or3_encode_rgb8 with gamma: what the reference's PNG saver writes), 3
+   bytes per pixel in the job's layout, so a frame crosses to the host at an
+   eighth of the FP64 frame's size.  Jobs' frame_host buffers are not used. */
+typedef void (*or3_job_frame8_callback)(void *user, uint64_t job_id, int32_t samples, const uint8_t *rgb,
+                                        size_t width, size_t height, int32_t final_frame);
+int or3_server_start8(or3_context *ctx, const or3_server_params *params, or3_job_frame8_callback cb, void *user);
+
+/* ---- image output and input on the device (the reference's savers and HDR
+ * loader stay the file writers and readers; these replace their per-pixel
+ * conversions, src/tools/FileSaver.h:49-120, src/tools/HDRImage.h:10-38) ---- */
+
+/* 8-bit RGB as the reference's PNG/PPM savers produce it: clamp to [0, 1],
+   pow(x, 1/2.2) when gamma (FileSaver::CopyColorArrayToImage, Utils::GammaRev),
+   then (int)(v * 255 + 0.5) (Utils::ToRgb).  n pixels, 3 doubles each. */
+int or3_encode_rgb8(or3_context *ctx, const double *rgb, size_t n, int32_t gamma, uint8_t *out);
+/* HDRImage::Color2RGBE: 4 bytes per pixel. */
+int or3_encode_rgbe(or3_context *ctx, const double *rgb, size_t n, uint8_t *out);
+/* HDRImage::RGBE2Color: 3 floats per pixel. */
+int or3_decode_rgbe(or3_context *ctx, const uint8_t *rgbe, size_t n, float *out);
+/* The last frame of or3_render (the layout it was rendered in), encoded on
+   the device; capacity in bytes (3 or 4 per pixel). */
+int or3_get_frame_rgb8(or3_context *ctx, int32_t gamma, uint8_t *rgb, size_t capacity, int32_t *samples_out);
+int or3_get_frame_rgbe(or3_context *ctx, uint8_t *rgbe, size_t capacity, int32_t *samples_out);
+/* A Radiance .hdr file in memory (HDRImage::ReadFromRadianceFile,
+   src/tools/HDRImage.cpp:12-186: "#?" header, "-Y h +X w", run-length or flat
+   scanlines) to flat RGBE bytes, row-major, on the host.  rgbe NULL returns
+   the size only.  No context or GPU needed; decode with or3_decode_rgbe or
+   pass the bytes as or3_scene_desc.env_rgbe. */
+int or3_read_hdr(const uint8_t *file, size_t length, uint32_t *width_out, uint32_t *height_out, uint8_t *rgbe,
+                 size_t capacity);
 
 /* ---- rendering without allocating (no counterpart in the reference) ------
  * For callers that must not allocate device memory while they render: code

@@ -54,6 +54,7 @@ class SceneDescC(ctypes.Structure):
         ("sphere_ids", u32p),
         ("num_planes", ctypes.c_uint32), ("planes", f64p), ("plane_layers", u32p), ("plane_ids", u32p),
         ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32), ("env_rgb", f32p),
+        ("env_rgbe", P(ctypes.c_uint8)),
         ("background", c_double3),
         ("num_textures", ctypes.c_uint32), ("texture_dims", u32p), ("texture_offsets", P(ctypes.c_uint64)),
         ("texture_rgb", f32p), ("build", ctypes.c_uint32),
@@ -127,6 +128,8 @@ class ServerStatsC(ctypes.Structure):
                 ("peak_active_jobs", ctypes.c_uint64), ("peak_budget_bytes", ctypes.c_uint64)]
 
 
+JOB_FRAME8_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, P(ctypes.c_uint8),
+                                 ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32)
 JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, f64p, ctypes.c_size_t,
                                 ctypes.c_size_t, ctypes.c_int32)
 
@@ -168,6 +171,15 @@ PROTOTYPES = {
     "or3_autotune_batch": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), ctypes.c_size_t, ctypes.c_uint64,
                                           P(BatchParamsC), P(ctypes.c_double)]),
     "or3_server_start": (ctypes.c_int, [ctypes.c_void_p, P(ServerParamsC), JOB_FRAME_CB, ctypes.c_void_p]),
+    "or3_server_start8": (ctypes.c_int, [ctypes.c_void_p, P(ServerParamsC), JOB_FRAME8_CB, ctypes.c_void_p]),
+    "or3_encode_rgb8": (ctypes.c_int, [ctypes.c_void_p, f64p, ctypes.c_size_t, ctypes.c_int32, P(ctypes.c_uint8)]),
+    "or3_encode_rgbe": (ctypes.c_int, [ctypes.c_void_p, f64p, ctypes.c_size_t, P(ctypes.c_uint8)]),
+    "or3_decode_rgbe": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_uint8), ctypes.c_size_t, f32p]),
+    "or3_get_frame_rgb8": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_uint8), ctypes.c_size_t,
+                                          P(ctypes.c_int32)]),
+    "or3_get_frame_rgbe": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_uint8), ctypes.c_size_t, P(ctypes.c_int32)]),
+    "or3_read_hdr": (ctypes.c_int, [P(ctypes.c_uint8), ctypes.c_size_t, P(ctypes.c_uint32), P(ctypes.c_uint32),
+                                    P(ctypes.c_uint8), ctypes.c_size_t]),
     "or3_server_submit": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), P(ctypes.c_uint64)]),
     "or3_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, P(JobStatusC)]),
     "or3_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

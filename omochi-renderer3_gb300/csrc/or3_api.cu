@@ -117,11 +117,11 @@ constexpr double kPiD = 3.14159265358979323846264338327950288419716939;
 // measure of SphereLight::TotalPower, src/renderer/SphereLight.h:71-78).  The
 // environment is sampled through a piecewise-constant marginal/conditional CDF
 // over max(r, g, b) * sin(theta) per texel (the reference's importance map,
-// src/renderer/IBL.h:104-189, is a stub), or uniformly over directions when
-// it is a constant background.
+// src/renderer/IBL.h:104-189, is a stub; the CDF is built on the device), or
+// cosine-weighted about the receiver's normal when it is a constant background.
 struct LightTables {
   std::vector<LightDev> lights;
-  std::vector<float> cdf, pdf, env_marg, env_cond;
+  std::vector<float> cdf, pdf;
   int env_light = 0;
   float env_prob = 0.f;
 };
@@ -181,42 +181,12 @@ void build_light_tables(const or3_scene_desc *d, const std::vector<float> &geom,
     T.cdf[k] = k + 1 == nl ? 1.0f : (float)(run / total);
     T.pdf[k] = (float)(power[k] / total);
   }
-  if (d->env_rgb) {
-    const uint32_t W = d->env_width, H = d->env_height;
-    std::vector<double> rows(H);
-    T.env_cond.resize((size_t)W * H);
-    T.env_marg.resize(H);
-    auto weight = [&](uint32_t i, uint32_t j) {
-      const float *p = d->env_rgb + 3 * ((size_t)i * W + j);
-      const float mx = std::max(p[0], std::max(p[1], p[2]));
-      return (mx > 0 ? mx : 0) * std::sin(kPiD * (i + 0.5) / H);
-    };
-    double etot = 0;
-    for (uint32_t i = 0; i < H; i++) {
-      double r = 0;
-      for (uint32_t j = 0; j < W; j++) r += weight(i, j);
-      rows[i] = r;
-      etot += r;
-    }
-    for (uint32_t i = 0; i < H; i++) {
-      double r = 0;
-      for (uint32_t j = 0; j < W; j++) {
-        r += weight(i, j);
-        T.env_cond[(size_t)i * W + j] =
-            j + 1 == W ? 1.0f : rows[i] > 0 ? (float)(r / rows[i]) : (float)((j + 1.0) / W);
-      }
-    }
-    double run2 = 0;
-    for (uint32_t i = 0; i < H; i++) {
-      run2 += rows[i];
-      T.env_marg[i] = i + 1 == H ? 1.0f : etot > 0 ? (float)(run2 / etot) : (float)((i + 1.0) / H);
-    }
-    T.env_light = etot > 0 ? 1 : 0;
-  } else {
+  if (!d->env_rgb && !d->env_rgbe) {
     const double *b = d->background;
     T.env_light = (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) != 0 ? 2 : 0;
   }
-  T.env_prob = T.env_light ? (nl ? 0.5f : 1.0f) : 0.0f;
+  // an equirect map's CDF is built on the device (launch_env_cdf); the upload
+  // sets env_light = 1 there once the map's total weight is known
 }
 
 }  // namespace
@@ -452,8 +422,10 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "planes without data or layers");
   if ((uint64_t)d->num_triangles + d->num_spheres >= (uint64_t)kPlaneBit)
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "too many primitives");
-  if (d->env_rgb && (d->env_width == 0 || d->env_height == 0))
+  if ((d->env_rgb || d->env_rgbe) && (d->env_width == 0 || d->env_height == 0))
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "environment map with zero size");
+  if (d->env_rgb && d->env_rgbe)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "give the environment as env_rgb or env_rgbe, not both");
 
   auto t0 = std::chrono::steady_clock::now();
   SceneGPU *sg = new SceneGPU();
@@ -682,25 +654,45 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   if ((rc = dev_upload(ctx, sg, planes, &S.planes))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, mats, &S.materials))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, layers, &S.layers))) { free_scene(sg); return rc; }
-  if (d->env_rgb) {
-    std::vector<float> env(d->env_rgb, d->env_rgb + 3 * (size_t)d->env_width * d->env_height);
-    if ((rc = dev_upload(ctx, sg, env, &S.env))) { free_scene(sg); return rc; }
-    S.env_w = d->env_width;
-    S.env_h = d->env_height;
+  double *env_total = nullptr;  // device: [H] row totals, [H] the map's total
+  if (d->env_rgb || d->env_rgbe) {
+    const uint32_t W = d->env_width, H = d->env_height;
+    const size_t texels = (size_t)W * H;
+    float *env_d = nullptr, *marg_d = nullptr, *cond_d = nullptr;
+    if ((rc = dev_alloc(ctx, sg, &env_d, 3 * texels)) || (rc = dev_alloc(ctx, sg, &marg_d, H)) ||
+        (rc = dev_alloc(ctx, sg, &cond_d, texels)) || (rc = tmp.alloc(ctx, &env_total, (size_t)H + 1))) {
+      free_scene(sg);
+      return rc;
+    }
+    cudaError_t ce;
+    if (d->env_rgb) {
+      ce = cudaMemcpyAsync(env_d, d->env_rgb, 3 * texels * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    } else {
+      // RGBE bytes (a third of the float map's size) decoded on the device
+      uint8_t *rgbe_d = nullptr;
+      if ((rc = tmp.alloc(ctx, &rgbe_d, 4 * texels))) { free_scene(sg); return rc; }
+      ce = cudaMemcpyAsync(rgbe_d, d->env_rgbe, 4 * texels, cudaMemcpyHostToDevice, ctx->stream);
+      if (ce == cudaSuccess) launch_decode_rgbe(rgbe_d, texels, env_d, ctx->stream);
+    }
+    if (ce != cudaSuccess) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_CUDA, "environment upload: %s", cudaGetErrorString(ce));
+    }
+    launch_env_cdf(env_d, W, H, marg_d, cond_d, env_total, ctx->stream);
+    S.env = env_d;
+    S.env_marg = marg_d;
+    S.env_cond = cond_d;
+    S.env_w = W;
+    S.env_h = H;
   }
-  {
-    LightTables T;
-    build_light_tables(d, geom, T);
-    if ((rc = dev_upload(ctx, sg, T.lights, &S.lights))) { free_scene(sg); return rc; }
-    if ((rc = dev_upload(ctx, sg, T.cdf, &S.light_cdf))) { free_scene(sg); return rc; }
-    if ((rc = dev_upload(ctx, sg, T.pdf, &S.light_pdf))) { free_scene(sg); return rc; }
-    if ((rc = dev_upload(ctx, sg, T.env_marg, &S.env_marg))) { free_scene(sg); return rc; }
-    if ((rc = dev_upload(ctx, sg, T.env_cond, &S.env_cond))) { free_scene(sg); return rc; }
-    S.num_lights = (uint32_t)T.lights.size();
-    S.env_light = T.env_light;
-    S.env_prob = T.env_prob;
-    sg->info.num_lights = (int32_t)S.num_lights;
-  }
+  LightTables T;
+  build_light_tables(d, geom, T);
+  if ((rc = dev_upload(ctx, sg, T.lights, &S.lights))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, T.cdf, &S.light_cdf))) { free_scene(sg); return rc; }
+  if ((rc = dev_upload(ctx, sg, T.pdf, &S.light_pdf))) { free_scene(sg); return rc; }
+  S.num_lights = (uint32_t)T.lights.size();
+  S.env_light = T.env_light;
+  sg->info.num_lights = (int32_t)S.num_lights;
   if (d->num_textures) {
     std::vector<TextureDev> tex(d->num_textures);
     uint64_t total = 0;
@@ -715,11 +707,16 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     if ((rc = dev_upload(ctx, sg, texels, &S.texels))) { free_scene(sg); return rc; }
     S.num_textures = d->num_textures;
   }
+  double env_sum = 0.0;
+  if (env_total) cudaMemcpyAsync(&env_sum, env_total + S.env_h, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     free_scene(sg);
     return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(e));
   }
+  if (env_total) S.env_light = env_sum > 0 ? 1 : 0;
+  S.env_prob = S.env_light ? (S.num_lights ? 0.5f : 1.0f) : 0.0f;
   auto t2 = std::chrono::steady_clock::now();
   sg->info.num_primitives = np + d->num_planes;
   sg->info.num_nodes = S.num_nodes;

@@ -145,6 +145,15 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
                            const float *tmax, uint8_t *occ, uint32_t *counters, cudaStream_t st);
 void set_query_grid(int grid);
 
+// or3_image.cu: image output/input and the environment CDF
+int ensure_gamma_table(int device);  // per device, before launch_encode_rgb8 with gamma; 0 or a cudaError_t
+void launch_encode_rgb8(const double *in, size_t nvals, int gamma, uint8_t *out, cudaStream_t st);
+void launch_encode_rgbe(const double *in, size_t npix, uint8_t *out, cudaStream_t st);
+void launch_decode_rgbe(const uint8_t *in, size_t npix, float *out, cudaStream_t st);
+// rows: H + 1 doubles of scratch; rows[H] receives the map's total weight
+void launch_env_cdf(const float *env, uint32_t W, uint32_t H, float *marg, float *cond, double *rows,
+                    cudaStream_t st);
+
 // or3_noalloc.cu: the bounce loop on the static scratch array
 int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &rc, uint64_t first,
                          uint32_t num_paths, uint32_t pass_first, int device, int grid_ext, int grid_sh,

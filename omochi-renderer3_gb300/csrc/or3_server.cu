@@ -55,6 +55,7 @@ struct SJob {
 struct Server {
   or3_server_params p{};
   or3_job_frame_callback cb = nullptr;
+  or3_job_frame8_callback cb8 = nullptr;  // frames encoded to 8-bit on the device (or3_server_start8)
   void *user = nullptr;
   std::thread th;
   std::mutex mu;
@@ -84,6 +85,7 @@ struct Server {
   uint32_t cap_segs = 0;
   double *frame_dev = nullptr, *frame_pinned = nullptr;
   size_t cap_frame = 0;
+  uint8_t *frame8_dev = nullptr, *frame8_pinned = nullptr;  // 8-bit frames (3 bytes per pixel)
   cudaGraphExec_t graph = nullptr;
   int unroll = 8;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -126,24 +128,40 @@ int emit_frame(or3_context *ctx, Server &S, SJob &j, bool final) {
     OR3_CUDA(ctx, cudaStreamSynchronize(st));
     cudaFree(S.frame_dev);
     cudaFreeHost(S.frame_pinned);
+    cudaFree(S.frame8_dev);
+    cudaFreeHost(S.frame8_pinned);
     S.frame_dev = nullptr;
     S.frame_pinned = nullptr;
+    S.frame8_dev = nullptr;
+    S.frame8_pinned = nullptr;
     S.cap_frame = 0;
     OR3_CUDA(ctx, cudaMalloc(&S.frame_dev, nd * sizeof(double)));
-    OR3_CUDA(ctx, cudaMallocHost(&S.frame_pinned, nd * sizeof(double)));
+    if (S.cb8) {
+      OR3_CUDA(ctx, cudaMalloc(&S.frame8_dev, nd));
+      OR3_CUDA(ctx, cudaMallocHost(&S.frame8_pinned, nd));
+    } else {
+      OR3_CUDA(ctx, cudaMallocHost(&S.frame_pinned, nd * sizeof(double)));
+    }
     S.cap_frame = nd;
   }
   OR3_CUDA(ctx, cudaMemsetAsync(S.frame_dev, 0, nd * sizeof(double), st));
   launch_frame(j.sum, j.job.camera.width, j.job.camera.height, j.job.params.output_layout,
                1.0 / ((double)j.samples_done * j.ss2), S.frame_dev, st);
+  const size_t w = (j.job.params.output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * (size_t)j.job.camera.width;
+  if (S.cb8) {
+    // 8-bit on the device: 3 bytes per pixel cross to the host instead of 24
+    launch_encode_rgb8(S.frame_dev, nd, 1, S.frame8_dev, st);
+    OR3_CUDA(ctx, cudaMemcpyAsync(S.frame8_pinned, S.frame8_dev, nd, cudaMemcpyDeviceToHost, st));
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    if (j.t_first < 0) j.t_first = S.now();
+    S.cb8(S.user, j.id, j.samples_done, S.frame8_pinned, w, j.job.camera.height, final ? 1 : 0);
+    return OR3_OK;
+  }
   OR3_CUDA(ctx, cudaMemcpyAsync(S.frame_pinned, S.frame_dev, nd * sizeof(double), cudaMemcpyDeviceToHost, st));
   OR3_CUDA(ctx, cudaStreamSynchronize(st));
   if (j.t_first < 0) j.t_first = S.now();
   if (j.job.frame_host && j.job.frame_capacity >= nd) std::memcpy(j.job.frame_host, S.frame_pinned, nd * sizeof(double));
-  if (S.cb)
-    S.cb(S.user, j.id, j.samples_done, S.frame_pinned,
-         (j.job.params.output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * (size_t)j.job.camera.width,
-         j.job.camera.height, final ? 1 : 0);
+  if (S.cb) S.cb(S.user, j.id, j.samples_done, S.frame_pinned, w, j.job.camera.height, final ? 1 : 0);
   return OR3_OK;
 }
 
@@ -384,6 +402,8 @@ void destroy_server_state(or3_context *ctx) {
   cudaFreeHost(S->info_host);
   cudaFree(S->frame_dev);
   cudaFreeHost(S->frame_pinned);
+  cudaFree(S->frame8_dev);
+  cudaFreeHost(S->frame8_pinned);
   if (S->e0) cudaEventDestroy(S->e0);
   if (S->e1) cudaEventDestroy(S->e1);
   delete S;
@@ -396,14 +416,20 @@ using namespace or3;
 
 extern "C" {
 
-int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_frame_callback cb, void *user) {
+static int server_start(or3_context *ctx, const or3_server_params *params, or3_job_frame_callback cb,
+                        or3_job_frame8_callback cb8, void *user) {
   if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
   if (ctx->server) return fail(ctx, OR3_ERR_BUSY, "server already running");
   cudaSetDevice(ctx->device);
+  if (cb8) {
+    if (int e = ensure_gamma_table(ctx->device))
+      return fail(ctx, OR3_ERR_CUDA, "gamma table: %s", cudaGetErrorString((cudaError_t)e));
+  }
   Server *S = new Server();
   ctx->server = S;
   if (params) S->p = *params;
   S->cb = cb;
+  S->cb8 = cb8;
   S->user = user;
   S->t0 = Clock::now();
   auto bail = [&](int rc) {
@@ -469,6 +495,15 @@ int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_
   if (cudaStreamSynchronize(st) != cudaSuccess) return bail(fail(ctx, OR3_ERR_CUDA, "server start"));
   S->th = std::thread(worker, ctx);
   return OR3_OK;
+}
+
+int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_frame_callback cb, void *user) {
+  return server_start(ctx, params, cb, nullptr, user);
+}
+
+int or3_server_start8(or3_context *ctx, const or3_server_params *params, or3_job_frame8_callback cb, void *user) {
+  if (!cb) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "or3_server_start8 needs a frame callback");
+  return server_start(ctx, params, nullptr, cb, user);
 }
 
 int or3_server_submit(or3_context *ctx, const or3_batch_job *job, uint64_t *id_out) {

@@ -125,6 +125,45 @@ class Context:
         self._check(self.lib.or3_get_frame(self.h, out.ctypes.data_as(abi.f64p), out.size, ctypes.byref(s)))
         return out, s.value
 
+    # ---- image output / input on the device
+    def encode_rgb8(self, rgb, gamma=True):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 3), np.uint8)
+        self._check(self.lib.or3_encode_rgb8(self.h, c.ctypes.data_as(abi.f64p), c.shape[0], 1 if gamma else 0,
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out
+
+    def encode_rgbe(self, rgb):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 4), np.uint8)
+        self._check(self.lib.or3_encode_rgbe(self.h, c.ctypes.data_as(abi.f64p), c.shape[0],
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out
+
+    def decode_rgbe(self, rgbe):
+        b = np.ascontiguousarray(rgbe, np.uint8).reshape(-1, 4)
+        out = np.zeros((b.shape[0], 3), np.float32)
+        self._check(self.lib.or3_decode_rgbe(self.h, b.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), b.shape[0],
+                                             out.ctypes.data_as(abi.f32p)))
+        return out
+
+    def frame_rgb8(self, width, height, layout=abi.OR3_LAYOUT_REFERENCE, gamma=True):
+        w = width * (2 if layout == abi.OR3_LAYOUT_REFERENCE else 1)
+        out = np.zeros((height, w, 3), np.uint8)
+        s = ctypes.c_int32()
+        self._check(self.lib.or3_get_frame_rgb8(self.h, 1 if gamma else 0,
+                                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), out.size,
+                                                ctypes.byref(s)))
+        return out, s.value
+
+    def frame_rgbe(self, width, height, layout=abi.OR3_LAYOUT_REFERENCE):
+        w = width * (2 if layout == abi.OR3_LAYOUT_REFERENCE else 1)
+        out = np.zeros((height, w, 4), np.uint8)
+        s = ctypes.c_int32()
+        self._check(self.lib.or3_get_frame_rgbe(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), out.size,
+                                                ctypes.byref(s)))
+        return out, s.value
+
     def moments(self, width, height):
         s = np.zeros((height, width, 3), np.float64)
         q = np.zeros_like(s)
@@ -189,9 +228,18 @@ class Context:
 
     # ---- served form
     def server_start(self, *, wave_paths=0, hbm_budget_bytes=0, max_active_jobs=0, frame_every_samples=0,
-                     graph_bounces=0, keep_moments=False, on_frame=None):
+                     graph_bounces=0, keep_moments=False, on_frame=None, rgb8=False):
+        """rgb8: frames encoded to 8-bit on the device (or3_server_start8); on_frame then
+        receives uint8 images."""
         p = abi.ServerParamsC(wave_paths, hbm_budget_bytes, max_active_jobs, frame_every_samples, graph_bounces,
                               abi.OR3_SERVER_KEEP_MOMENTS if keep_moments else 0)
+        if rgb8:
+            def _cb8(user, job_id, samples, rgb, w, h, final):
+                if on_frame is not None:
+                    on_frame(job_id, samples, np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy(), bool(final))
+            self._server_cb = abi.JOB_FRAME8_CB(_cb8)
+            self._check(self.lib.or3_server_start8(self.h, ctypes.byref(p), self._server_cb, None))
+            return
         if on_frame is not None:
             def _cb(user, job_id, samples, rgb, w, h, final):
                 on_frame(job_id, samples, np.ctypeslib.as_array(rgb, shape=(h, w, 3)).copy(), bool(final))
@@ -336,3 +384,20 @@ class GpuPathTracer:
 
     def StopRendering(self):
         self.ctx.stop()
+
+
+def read_hdr(data):
+    """Radiance .hdr file contents (bytes) -> (H, W, 4) uint8 RGBE (or3_read_hdr; host only)."""
+    lib = abi.load_library()
+    buf = np.frombuffer(bytes(data), np.uint8)
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    ptr = buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    rc = lib.or3_read_hdr(ptr, buf.size, ctypes.byref(w), ctypes.byref(h), None, 0)
+    if rc != abi.OR3_OK:
+        raise Or3Error(rc, "or3_read_hdr: not a readable Radiance file")
+    out = np.zeros((h.value, w.value, 4), np.uint8)
+    rc = lib.or3_read_hdr(ptr, buf.size, ctypes.byref(w), ctypes.byref(h),
+                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), out.size)
+    if rc != abi.OR3_OK:
+        raise Or3Error(rc, "or3_read_hdr: truncated or malformed pixel data")
+    return out

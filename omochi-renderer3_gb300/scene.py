@@ -63,6 +63,7 @@ class SceneDesc:
     spheres: list = field(default_factory=list)   # (cx,cy,cz,r, layer_begin, layer_count, flags, id)
     planes: list = field(default_factory=list)    # (kind, axis, offset, flip, layer_begin, layer_count, id)
     env: np.ndarray = None
+    env_rgbe: np.ndarray = None  # (H, W, 4) uint8, decoded on the device (alternative to env)
     background: tuple = (0.0, 0.0, 0.0)
     textures: list = field(default_factory=list)
     build: int = 0  # abi.OR3_BUILD_*
@@ -122,6 +123,12 @@ class SceneDesc:
 
     def set_env(self, rgb):
         self.env = np.ascontiguousarray(rgb, dtype=np.float32)
+        self.env_rgbe = None
+
+    def set_env_rgbe(self, rgbe):
+        """Environment as RGBE bytes (H, W, 4), e.g. from renderer.read_hdr."""
+        self.env_rgbe = np.ascontiguousarray(rgbe, dtype=np.uint8)
+        self.env = None
 
     @property
     def num_objects(self):
@@ -151,6 +158,8 @@ class SceneDesc:
             h.update(np.ascontiguousarray(a[k]).tobytes())
         if self.env is not None:
             h.update(self.env.tobytes())
+        if self.env_rgbe is not None:
+            h.update(self.env_rgbe.tobytes())
         return h.hexdigest()
 
     # ---- flattened arrays
@@ -251,6 +260,10 @@ class SceneDesc:
             d.env_height, d.env_width = self.env.shape[0], self.env.shape[1]
             d.env_rgb = _ptr(self.env, ctypes.c_float)
             keep.append(self.env)
+        elif self.env_rgbe is not None:
+            d.env_height, d.env_width = self.env_rgbe.shape[0], self.env_rgbe.shape[1]
+            d.env_rgbe = _ptr(self.env_rgbe, ctypes.c_uint8)
+            keep.append(self.env_rgbe)
         d.background = abi.c_double3(*self.background)
         if self.textures:
             d.num_textures = len(self.textures)

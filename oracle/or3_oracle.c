@@ -14,6 +14,11 @@
  *   radiance           PathTracer::Radiance/_internal/_Lambert/_Specular/_Refraction
  *                                                       src/renderer/PathTracer.cpp:180-591
  *   env_sample         IBL::Sample(dir)                 src/renderer/IBL.h:30-45
+ *   orc_encode_rgb8    FileSaver::CopyColorArrayToImage + Utils::ToRgb
+ *                                                       src/tools/FileSaver.h:49-120,
+ *                                                       src/tools/Utils.h:93-109
+ *   orc_encode_rgbe    HDRImage::Color2RGBE             src/tools/HDRImage.h:10-25
+ *   orc_decode_rgbe    HDRImage::RGBE2Color             src/tools/HDRImage.h:27-38
  * The random numbers are the GPU's counter-based Philox draws (not the
  * reference's per-row xorshift), so a path can be replayed exactly; the
  * estimator and its expectation are the reference's.
@@ -1133,4 +1138,48 @@ int orc_render(const orc_scene *s, const or3_camera *cam, const orc_params *p, i
   if (seconds) *seconds = (double)(clock() - t0) / CLOCKS_PER_SEC;
 #endif
   return 0;
+}
+
+/* ------------------------------------------------------------------ image conversions */
+static double clamp01(double x) { return x < 0.0 ? 0.0 : x > 1.0 ? 1.0 : x; }
+
+void orc_encode_rgb8(size_t n, const double *rgb, int gamma, uint8_t *out) {
+  for (size_t i = 0; i < 3 * n; i++) {
+    double v = clamp01(rgb[i]);
+    if (gamma) v = pow(clamp01(v), 1.0 / 2.2);
+    out[i] = (uint8_t)(int)(v * 255 + 0.5);
+  }
+}
+
+void orc_encode_rgbe(size_t n, const double *rgb, uint8_t *out) {
+  for (size_t i = 0; i < n; i++) {
+    const double *c = rgb + 3 * i;
+    uint8_t *b = out + 4 * i;
+    const double mx = fmax(fmax(c[0], c[1]), c[2]);
+    float v = (float)mx;
+    if (v < 1e-32) {
+      b[0] = b[1] = b[2] = b[3] = 0;
+    } else {
+      int e;
+      v = frexpf(v, &e) * 256.0f / v;
+      b[0] = (uint8_t)(c[0] * v);
+      b[1] = (uint8_t)(c[1] * v);
+      b[2] = (uint8_t)(c[2] * v);
+      b[3] = (uint8_t)(e + 128);
+    }
+  }
+}
+
+void orc_decode_rgbe(size_t n, const uint8_t *rgbe, double *out) {
+  for (size_t i = 0; i < n; i++) {
+    const uint8_t *b = rgbe + 4 * i;
+    if (b[3]) {
+      const float f = (float)ldexp(1.0, (int)b[3] - (128 + 8));
+      out[3 * i] = (double)(b[0] * f);
+      out[3 * i + 1] = (double)(b[1] * f);
+      out[3 * i + 2] = (double)(b[2] * f);
+    } else {
+      out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = 0.0;
+    }
+  }
 }

@@ -60,6 +60,13 @@ int orc_path_radiance(const orc_scene *s, const or3_camera *cam, const orc_param
 int orc_render(const orc_scene *s, const or3_camera *cam, const orc_params *p, int nthreads, double *sum,
                double *sumsq, double *seconds);
 
+/* Image conversions of the reference's savers and HDR loader:
+   8-bit: FileSaver::CopyColorArrayToImage + Utils::ToRgb (gamma 1/2.2 or none);
+   RGBE: HDRImage::Color2RGBE / RGBE2Color.  n pixels, RGB doubles. */
+void orc_encode_rgb8(size_t n, const double *rgb, int gamma, uint8_t *out);
+void orc_encode_rgbe(size_t n, const double *rgb, uint8_t *out);
+void orc_decode_rgbe(size_t n, const uint8_t *rgbe, double *out);
+
 /* Philox4x32-10 as the kernels use it (for the RNG known-answer test). */
 void orc_philox(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
 

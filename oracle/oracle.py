@@ -67,11 +67,33 @@ class CRestatement:
         lib.orc_object_distance.argtypes = [ctypes.c_void_p, ctypes.c_size_t, i32p, f64p, f64p, f64p]
         lib.orc_path_radiance.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(OrcParams),
                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, f64p]
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        lib.orc_encode_rgb8.argtypes = [ctypes.c_size_t, f64p, ctypes.c_int, u8p]
+        lib.orc_encode_rgbe.argtypes = [ctypes.c_size_t, f64p, u8p]
+        lib.orc_decode_rgbe.argtypes = [ctypes.c_size_t, u8p, f64p]
         lib.orc_render.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(OrcParams), ctypes.c_int,
                                    f64p, f64p, f64p]
         lib.orc_philox.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.POINTER(ctypes.c_uint32)]
         self.lib = lib
+
+    def encode_rgb8(self, rgb, gamma=True):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 3), np.uint8)
+        self.lib.orc_encode_rgb8(c.shape[0], _np(c, ctypes.c_double), 1 if gamma else 0, _np(out, ctypes.c_uint8))
+        return out
+
+    def encode_rgbe(self, rgb):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 4), np.uint8)
+        self.lib.orc_encode_rgbe(c.shape[0], _np(c, ctypes.c_double), _np(out, ctypes.c_uint8))
+        return out
+
+    def decode_rgbe(self, rgbe):
+        b = np.ascontiguousarray(rgbe, np.uint8).reshape(-1, 4)
+        out = np.zeros((b.shape[0], 3), np.float64)
+        self.lib.orc_decode_rgbe(b.shape[0], _np(b, ctypes.c_uint8), _np(out, ctypes.c_double))
+        return out
 
     def philox(self, ctr, k0, k1):
         c = (ctypes.c_uint32 * 4)(*ctr)
@@ -154,8 +176,47 @@ class Reference:
         lib.orref_render_scene.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6 + [f64p, f64p]
         if cfg:
             lib.orref_set_depth_limits.argtypes = [ctypes.c_int, ctypes.c_int]
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        lib.orref_encode_rgb8.argtypes = [ctypes.c_size_t, f64p, ctypes.c_int, u8p]
+        lib.orref_encode_rgbe.argtypes = [ctypes.c_size_t, f64p, u8p]
+        lib.orref_decode_rgbe.argtypes = [ctypes.c_size_t, u8p, f64p]
+        lib.orref_write_hdr.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, f64p]
+        lib.orref_read_hdr.argtypes = [ctypes.c_char_p, i32p, i32p, f64p, ctypes.c_size_t]
         self.lib = lib
         self.cfg = cfg
+
+    # ---- the reference's image conversions (src/tools/FileSaver.h, HDRImage.h/.cpp)
+    def encode_rgb8(self, rgb, gamma=True):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 3), np.uint8)
+        self.lib.orref_encode_rgb8(c.shape[0], _np(c, ctypes.c_double), 1 if gamma else 0, _np(out, ctypes.c_uint8))
+        return out
+
+    def encode_rgbe(self, rgb):
+        c = np.ascontiguousarray(rgb, np.float64).reshape(-1, 3)
+        out = np.zeros((c.shape[0], 4), np.uint8)
+        self.lib.orref_encode_rgbe(c.shape[0], _np(c, ctypes.c_double), _np(out, ctypes.c_uint8))
+        return out
+
+    def decode_rgbe(self, rgbe):
+        b = np.ascontiguousarray(rgbe, np.uint8).reshape(-1, 4)
+        out = np.zeros((b.shape[0], 3), np.float64)
+        self.lib.orref_decode_rgbe(b.shape[0], _np(b, ctypes.c_uint8), _np(out, ctypes.c_double))
+        return out
+
+    def write_hdr(self, path, rgb):
+        c = np.ascontiguousarray(rgb, np.float64)
+        h, w = c.shape[:2]
+        if self.lib.orref_write_hdr(path.encode(), w, h, _np(c, ctypes.c_double)) != 0:
+            raise IOError(path)
+
+    def read_hdr(self, path):
+        w, h = ctypes.c_int32(), ctypes.c_int32()
+        if self.lib.orref_read_hdr(path.encode(), ctypes.byref(w), ctypes.byref(h), None, 0) != 0:
+            raise IOError(path)
+        out = np.zeros((h.value, w.value, 3), np.float64)
+        self.lib.orref_read_hdr(path.encode(), ctypes.byref(w), ctypes.byref(h), _np(out, ctypes.c_double), out.size)
+        return out
 
     def set_depth_limits(self, rr_min_depth, max_depth):
         if not self.cfg:

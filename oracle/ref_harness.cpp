@@ -55,6 +55,8 @@
 #include "renderer/Sphere.h"
 #include "renderer/SphereLight.h"
 #include "scenes/Scene.h"
+#include "tools/FileSaver.h"
+#include "tools/HDRImage.h"
 #include "tools/ImageHandler.h"
 #undef private
 #undef protected
@@ -315,6 +317,63 @@ int orref_render_scene(void *p, const or3_camera *c, int min_s, int max_s, int s
   delete pt->m_result;
   pt->m_result = nullptr;
   delete pt;
+  return 0;
+}
+
+// ---- image output and input (the savers' 8-bit conversion, RGBE)
+
+// FileSaver::CopyColorArrayToImage (src/tools/FileSaver.h:49-120, gamma on or
+// off) followed by ImageHandler::SaveToPngFile's Utils::ToRgb
+// (src/tools/ImageHandler.cpp:133-155): the bytes the reference writes.
+void orref_encode_rgb8(size_t n, const double *rgb, int gamma, uint8_t *out) {
+  std::vector<Color> img(n), conv;
+  for (size_t i = 0; i < n; i++) img[i] = Color(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+  FileSaver::CopyColorArrayToImage(img.data(), conv, static_cast<int>(n), 1, gamma != 0);
+  for (size_t i = 0; i < n; i++) {
+    out[3 * i] = static_cast<unsigned char>(Utils::ToRgb(conv[i].x));
+    out[3 * i + 1] = static_cast<unsigned char>(Utils::ToRgb(conv[i].y));
+    out[3 * i + 2] = static_cast<unsigned char>(Utils::ToRgb(conv[i].z));
+  }
+}
+
+// HDRImage::Color2RGBE / RGBE2Color (src/tools/HDRImage.h:10-38).
+void orref_encode_rgbe(size_t n, const double *rgb, uint8_t *out) {
+  for (size_t i = 0; i < n; i++) HDRImage::Color2RGBE(out + 4 * i, Color(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]));
+}
+
+void orref_decode_rgbe(size_t n, const uint8_t *rgbe, double *out) {
+  for (size_t i = 0; i < n; i++) {
+    unsigned char b[4] = {rgbe[4 * i], rgbe[4 * i + 1], rgbe[4 * i + 2], rgbe[4 * i + 3]};
+    Color c;
+    HDRImage::RGBE2Color(b, c);
+    out[3 * i] = c.x;
+    out[3 * i + 1] = c.y;
+    out[3 * i + 2] = c.z;
+  }
+}
+
+// HDRImage::WriteToRadianceFile / ReadFromRadianceFile (src/tools/HDRImage.cpp).
+int orref_write_hdr(const char *path, int w, int h, const double *rgb) {
+  HDRImage img;
+  img.m_width = w;
+  img.m_height = h;
+  img.m_image.resize((size_t)w * h);
+  for (size_t i = 0; i < (size_t)w * h; i++) img.m_image[i] = Color(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+  return img.WriteToRadianceFile(path) ? 0 : -1;
+}
+
+int orref_read_hdr(const char *path, int *w, int *h, double *out, size_t capacity) {
+  HDRImage img;
+  if (!img.ReadFromRadianceFile(path)) return -1;
+  *w = static_cast<int>(img.GetWidth());
+  *h = static_cast<int>(img.GetHeight());
+  if (!out) return 0;
+  if (capacity < 3 * img.m_image.size()) return -2;
+  for (size_t i = 0; i < img.m_image.size(); i++) {
+    out[3 * i] = img.m_image[i].x;
+    out[3 * i + 1] = img.m_image[i].y;
+    out[3 * i + 2] = img.m_image[i].z;
+  }
   return 0;
 }
 

@@ -14,6 +14,10 @@ committed and are all the GPU tests need.
                         PathTracer::Radiance estimator (float16), sample counts
   rmse_cornell_cfg.npz  (--rmse) 16384-spp reference render of the Cornell
                         workload, the RMSE target
+  image_codec.npz       the reference's 8-bit conversion (gamma on and off),
+                        Color2RGBE and RGBE2Color on seeded colours and bytes,
+                        and two .hdr files its writer produced (one run-length
+                        encoded, one flat) with what its reader decodes
 Each fixture stores a digest of the flattened scene it was made from.
 """
 import argparse
@@ -130,6 +134,35 @@ def make_rmse():
     print("%s: %d spp, %.0fs" % (path, n, sec))
 
 
+def make_image_codec():
+    import tempfile
+    ref = O.Reference()
+    rng = np.random.default_rng(21)
+    n = 20000
+    ldr = rng.uniform(-0.1, 1.2, (n, 3))
+    ldr[:8] = [[0, 0, 0], [1, 1, 1], [0.5, 0.5, 0.5], [2, -1, 0.999999], [1e-9, 1e-5, 0.0039215],
+               [0.99, 0.001, 0.2], [np.nextafter(1.0, 0), 0.25, 0.75], [0.0, 1.0, 0.5]]
+    hdr = np.exp(rng.uniform(np.log(1e-6), np.log(1e6), (n, 3)))
+    hdr[rng.random(n) < 0.05] = 0.0
+    hdr[:6] = [[0, 0, 0], [1e-33, 1e-33, 1e-33], [1, 1, 1], [255.99, 0.5, 1e-3], [1e30, 1e29, 1], [0.5, 0.5, 0.5]]
+    rgbe_in = rng.integers(0, 256, (n, 4), dtype=np.uint8)
+    rgbe_in[:4, 3] = [0, 1, 128, 255]
+    out = dict(ldr=ldr, rgb8_gamma=ref.encode_rgb8(ldr, True), rgb8_linear=ref.encode_rgb8(ldr, False),
+               hdr=hdr, rgbe=ref.encode_rgbe(hdr), rgbe_in=rgbe_in, rgbe_decoded=ref.decode_rgbe(rgbe_in))
+    with tempfile.TemporaryDirectory() as td:
+        for name, (h, w) in (("rle", (23, 37)), ("flat", (4, 5))):
+            img = np.exp(rng.uniform(np.log(1e-3), np.log(1e3), (h, w, 3)))
+            img[::3] = img[::3, :1]  # constant rows: runs for the run-length encoder
+            path = os.path.join(td, name + ".hdr")
+            ref.write_hdr(path, img)
+            out["hdr_%s_file" % name] = np.frombuffer(open(path, "rb").read(), np.uint8)
+            out["hdr_%s_image" % name] = img
+            out["hdr_%s_decoded" % name] = ref.read_hdr(path)
+    path = os.path.join(HERE, "image_codec.npz")
+    np.savez_compressed(path, **out)
+    print(path)
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--rmse", action="store_true")
@@ -140,6 +173,10 @@ if __name__ == "__main__":
     if a.rmse:
         make_rmse()
         sys.exit(0)
+    if a.only == "image_codec":
+        make_image_codec()
+        sys.exit(0)
+    make_image_codec()
     for nm in CLOSEST_SCENES:
         if not a.only or a.only == nm:
             make_closest(nm)

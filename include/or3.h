@@ -398,6 +398,31 @@ int or3_get_frame_rgbe(or3_context *ctx, uint8_t *rgbe, size_t capacity, int32_t
 int or3_read_hdr(const uint8_t *file, size_t length, uint32_t *width_out, uint32_t *height_out, uint8_t *rgbe,
                  size_t capacity);
 
+/* ---- mesh ingest: Wavefront .obj/.mtl to arrays (Model::ReadFromObj,
+ * src/renderer/Model.cpp:50-182; Model::LoadMaterialFile, :184-292), without
+ * a per-triangle object; the arrays plug into or3_scene_desc's triangle
+ * fields.  Material 0 is the reference's default (Lambert, colour 0.99); the
+ * rest come from the .mtl files in order.  Triangles are in file order. */
+typedef struct or3_mesh {
+  uint32_t num_triangles;
+  double *vertices;        /* [n][3][3] */
+  double *normals;         /* [n][3][3]; the face normal where the file gives none */
+  double *uvs;             /* [n][3][2] */
+  uint32_t *material;      /* [n] index into materials */
+  uint32_t num_materials;
+  or3_material *materials; /* texture = -1: textures are listed by path */
+  char **material_names;   /* [num_materials] */
+  char **texture_paths;    /* [num_materials] map_Kd path, or NULL */
+} or3_mesh;
+/* threads 0 = all host threads.  OR3_ERR_NOT_FOUND for a missing .obj/.mtl,
+   OR3_ERR_INVALID_ARGUMENT for a malformed line or index. */
+int or3_mesh_load_obj(const char *path, int32_t flip_v, uint32_t threads, or3_mesh **mesh_out);
+/* Model::Transform as SceneFromExternalFile::ReadMesh applies it (rotation in
+   radians, Rz * Ry * Rx; per-axis scale; then translation; normals rotated). */
+int or3_mesh_transform(or3_mesh *mesh, const double position[3], const double scaling[3],
+                       const double rotation[3]);
+void or3_mesh_free(or3_mesh *mesh);
+
 /* ---- rendering without allocating (no counterpart in the reference) ------
  * For callers that must not allocate device memory while they render: code
  * running in a host callback enqueued on a CUDA stream (CUDA calls that

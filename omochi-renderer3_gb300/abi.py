@@ -128,6 +128,12 @@ class ServerStatsC(ctypes.Structure):
                 ("peak_active_jobs", ctypes.c_uint64), ("peak_budget_bytes", ctypes.c_uint64)]
 
 
+class MeshC(ctypes.Structure):
+    _fields_ = [("num_triangles", ctypes.c_uint32), ("vertices", f64p), ("normals", f64p), ("uvs", f64p),
+                ("material", u32p), ("num_materials", ctypes.c_uint32), ("materials", P(Material)),
+                ("material_names", P(ctypes.c_char_p)), ("texture_paths", P(ctypes.c_char_p))]
+
+
 JOB_FRAME8_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, P(ctypes.c_uint8),
                                  ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32)
 JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, f64p, ctypes.c_size_t,
@@ -178,6 +184,9 @@ PROTOTYPES = {
     "or3_get_frame_rgb8": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_uint8), ctypes.c_size_t,
                                           P(ctypes.c_int32)]),
     "or3_get_frame_rgbe": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_uint8), ctypes.c_size_t, P(ctypes.c_int32)]),
+    "or3_mesh_load_obj": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_uint32, P(P(MeshC))]),
+    "or3_mesh_transform": (ctypes.c_int, [P(MeshC), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
+    "or3_mesh_free": (None, [P(MeshC)]),
     "or3_read_hdr": (ctypes.c_int, [P(ctypes.c_uint8), ctypes.c_size_t, P(ctypes.c_uint32), P(ctypes.c_uint32),
                                     P(ctypes.c_uint8), ctypes.c_size_t]),
     "or3_server_submit": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), P(ctypes.c_uint64)]),

@@ -401,3 +401,36 @@ def read_hdr(data):
     if rc != abi.OR3_OK:
         raise Or3Error(rc, "or3_read_hdr: truncated or malformed pixel data")
     return out
+
+
+def load_obj(path, flip_v=False, threads=0, position=None, scaling=(1.0, 1.0, 1.0), rotation=(0.0, 0.0, 0.0)):
+    """or3_mesh_load_obj (+ or3_mesh_transform when position is given); host only.
+    Returns dict: vertices [n,3,3], normals [n,3,3], uvs [n,3,2], material [n],
+    materials [(type, colour, ior)], names, textures."""
+    lib = abi.load_library()
+    mp = ctypes.POINTER(abi.MeshC)()
+    rc = lib.or3_mesh_load_obj(str(path).encode(), 1 if flip_v else 0, threads, ctypes.byref(mp))
+    if rc != abi.OR3_OK:
+        raise Or3Error(rc, "or3_mesh_load_obj(%s) failed" % path)
+    try:
+        if position is not None:
+            d3 = ctypes.c_double * 3
+            rc = lib.or3_mesh_transform(mp, d3(*position), d3(*scaling), d3(*rotation))
+            if rc != abi.OR3_OK:
+                raise Or3Error(rc, "or3_mesh_transform failed")
+        m = mp.contents
+        n = m.num_triangles
+        out = {
+            "vertices": np.ctypeslib.as_array(m.vertices, shape=(n, 3, 3)).copy() if n else np.zeros((0, 3, 3)),
+            "normals": np.ctypeslib.as_array(m.normals, shape=(n, 3, 3)).copy() if n else np.zeros((0, 3, 3)),
+            "uvs": np.ctypeslib.as_array(m.uvs, shape=(n, 3, 2)).copy() if n else np.zeros((0, 3, 2)),
+            "material": np.ctypeslib.as_array(m.material, shape=(n,)).copy() if n else np.zeros(0, np.uint32),
+            "materials": [(m.materials[i].type, tuple(m.materials[i].color), m.materials[i].ior)
+                          for i in range(m.num_materials)],
+            "names": [m.material_names[i].decode() for i in range(m.num_materials)],
+            "textures": [(m.texture_paths[i].decode() if m.texture_paths[i] else None)
+                         for i in range(m.num_materials)],
+        }
+    finally:
+        lib.or3_mesh_free(mp)
+    return out

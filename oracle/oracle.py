@@ -182,6 +182,9 @@ class Reference:
         lib.orref_decode_rgbe.argtypes = [ctypes.c_size_t, u8p, f64p]
         lib.orref_write_hdr.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, f64p]
         lib.orref_read_hdr.argtypes = [ctypes.c_char_p, i32p, i32p, f64p, ctypes.c_size_t]
+        lib.orref_load_obj.restype = ctypes.c_long
+        lib.orref_load_obj.argtypes = [ctypes.c_char_p, ctypes.c_int, f64p, f64p, f64p, f64p, f64p, f64p, f64p,
+                                       ctypes.c_long]
         self.lib = lib
         self.cfg = cfg
 
@@ -209,6 +212,22 @@ class Reference:
         h, w = c.shape[:2]
         if self.lib.orref_write_hdr(path.encode(), w, h, _np(c, ctypes.c_double)) != 0:
             raise IOError(path)
+
+    def load_obj(self, path, flip_v=False, position=(0, 0, 0), scaling=(1, 1, 1), rotation=(0, 0, 0)):
+        """Model::ReadFromObj + Transform: (tri [n,3,3], normals [n,3,3], uvs [n,3,2], mat [n,5])."""
+        args = [np.ascontiguousarray(x, np.float64) for x in (position, scaling, rotation)]
+        z = np.zeros(1)
+        n = self.lib.orref_load_obj(path.encode(), 1 if flip_v else 0, *[_np(a, ctypes.c_double) for a in args],
+                                    _np(z, ctypes.c_double), _np(z, ctypes.c_double), _np(z, ctypes.c_double),
+                                    _np(z, ctypes.c_double), 0)
+        if n < 0:
+            raise IOError(path)
+        tri, nrm = np.zeros((n, 3, 3)), np.zeros((n, 3, 3))
+        uv, mat = np.zeros((n, 3, 2)), np.zeros((n, 5))
+        self.lib.orref_load_obj(path.encode(), 1 if flip_v else 0, *[_np(a, ctypes.c_double) for a in args],
+                                _np(tri, ctypes.c_double), _np(nrm, ctypes.c_double), _np(uv, ctypes.c_double),
+                                _np(mat, ctypes.c_double), n)
+        return tri, nrm, uv, mat
 
     def read_hdr(self, path):
         w, h = ctypes.c_int32(), ctypes.c_int32()

@@ -54,8 +54,10 @@
 #include "renderer/Polygon.h"
 #include "renderer/Sphere.h"
 #include "renderer/SphereLight.h"
+#include "renderer/Model.h"
 #include "scenes/Scene.h"
 #include "tools/FileSaver.h"
+#include "tools/Matrix.h"
 #include "tools/HDRImage.h"
 #include "tools/ImageHandler.h"
 #undef private
@@ -375,6 +377,48 @@ int orref_read_hdr(const char *path, int *w, int *h, double *out, size_t capacit
     out[3 * i + 2] = img.m_image[i].z;
   }
   return 0;
+}
+
+// Model::ReadFromObj (src/renderer/Model.cpp:50-182) and the Transform that
+// SceneFromExternalFile::ReadMesh applies (src/scenes/SceneFromExternalFile.cpp:518-527);
+// every polygon of every material list, as Scene::AddModel would add them.
+// tri: [n][3][3] world vertices, nrm: [n][3][3], uv: [n][3][2], mat: [n][5]
+// (type, r, g, b, ior).  Returns the triangle count (or -1), filling at most cap.
+long orref_load_obj(const char *path, int flip_v, const double *pos, const double *scale, const double *rot,
+                    double *tri, double *nrm, double *uv, double *mat, long cap) {
+  Model model;
+  std::streambuf *old = std::cerr.rdbuf(nullptr);
+  const bool ok = model.ReadFromObj(path, flip_v != 0);
+  std::cerr.rdbuf(old);
+  if (!ok) return -1;
+  model.Transform(Vector3(pos[0], pos[1], pos[2]), Vector3(scale[0], scale[1], scale[2]),
+                  Matrix::RotateAroundVector(Vector3(0, 0, 1), rot[2]) *
+                      Matrix::RotateAroundVector(Vector3(0, 1, 0), rot[1]) *
+                      Matrix::RotateAroundVector(Vector3(1, 0, 0), rot[0]));
+  long n = 0;
+  for (size_t i = 0; i < model.GetMaterialCount(); i++) {
+    const Material &m = model.GetMaterial(i);
+    const Model::PolygonList &pl = model.GetPolygonList(m);
+    for (size_t j = 0; j < pl.size(); j++, n++) {
+      if (n >= cap) continue;
+      const Polygon *p = pl[j];
+      const Vector3 v0 = p->m_posAndEdges[0] + p->position_;
+      const Vector3 v[3] = {v0, v0 + p->m_posAndEdges[1], v0 + p->m_posAndEdges[2]};
+      const Vector3 n0 = p->m_normalAndDiffs[0];
+      const Vector3 nn[3] = {n0, n0 + p->m_normalAndDiffs[1], n0 + p->m_normalAndDiffs[2]};
+      const Vector3 u0 = p->m_uvOrigAndEdges[0];
+      const Vector3 uu[3] = {u0, u0 + p->m_uvOrigAndEdges[1], u0 + p->m_uvOrigAndEdges[2]};
+      for (int k = 0; k < 3; k++) {
+        tri[9 * n + 3 * k] = v[k].x; tri[9 * n + 3 * k + 1] = v[k].y; tri[9 * n + 3 * k + 2] = v[k].z;
+        nrm[9 * n + 3 * k] = nn[k].x; nrm[9 * n + 3 * k + 1] = nn[k].y; nrm[9 * n + 3 * k + 2] = nn[k].z;
+        uv[6 * n + 2 * k] = uu[k].x; uv[6 * n + 2 * k + 1] = uu[k].y;
+      }
+      mat[5 * n] = (double)m.reflection_type;
+      mat[5 * n + 1] = m.color.x; mat[5 * n + 2] = m.color.y; mat[5 * n + 3] = m.color.z;
+      mat[5 * n + 4] = m.refraction_rate;
+    }
+  }
+  return n;
 }
 
 }  // extern "C"

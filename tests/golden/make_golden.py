@@ -14,6 +14,8 @@ committed and are all the GPU tests need.
                         PathTracer::Radiance estimator (float16), sample counts
   rmse_cornell_cfg.npz  (--rmse) 16384-spp reference render of the Cornell
                         workload, the RMSE target
+  obj_ref.npz           the reference's Model::ReadFromObj + Transform of
+                        tests/golden/obj/mesh.obj (with and without the v flip)
   image_codec.npz       the reference's 8-bit conversion (gamma on and off),
                         Color2RGBE and RGBE2Color on seeded colours and bytes,
                         and two .hdr files its writer produced (one run-length
@@ -134,6 +136,21 @@ def make_rmse():
     print("%s: %d spp, %.0fs" % (path, n, sec))
 
 
+OBJ_TRANSFORM = dict(position=(10.0, -5.0, 3.0), scaling=(2.0, 1.0, 0.5), rotation=(0.3, -0.2, 0.7))
+
+
+def make_obj():
+    ref = O.Reference()
+    path = os.path.join(HERE, "obj", "mesh.obj")
+    out = {}
+    for flip in (0, 1):
+        tri, nrm, uv, mat = ref.load_obj(path, flip_v=bool(flip), **OBJ_TRANSFORM)
+        out.update({"tri_%d" % flip: tri, "nrm_%d" % flip: nrm, "uv_%d" % flip: uv, "mat_%d" % flip: mat})
+    dest = os.path.join(HERE, "obj_ref.npz")
+    np.savez_compressed(dest, **out)
+    print(dest, out["tri_0"].shape)
+
+
 def make_image_codec():
     import tempfile
     ref = O.Reference()
@@ -176,7 +193,11 @@ if __name__ == "__main__":
     if a.only == "image_codec":
         make_image_codec()
         sys.exit(0)
+    if a.only == "obj":
+        make_obj()
+        sys.exit(0)
     make_image_codec()
+    make_obj()
     for nm in CLOSEST_SCENES:
         if not a.only or a.only == nm:
             make_closest(nm)

@@ -436,7 +436,7 @@ def main():
     time.sleep(0.3)
     barrier(dist)
     torch.cuda.synchronize()
-    render_ms = ext_ms = shade_ms = 0.0
+    render_ms = ext_ms = shade_ms = shadow_ms = 0.0
     shadow_rays = 0
     ext_launches = paths = ext_rays = bounces = waves = passes = 0
     w0 = time.perf_counter()
@@ -446,6 +446,7 @@ def main():
         render_ms += s["render_ms"]
         ext_ms += s["extend_ms"]
         shade_ms += s["shade_ms"]
+        shadow_ms += s["shadow_ms"]
         shadow_rays += s["shadow_rays"]
         ext_launches += s["extend_launches"]
         paths += s["camera_paths"]
@@ -495,8 +496,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "wall_s_timed": wall_s, "shadow_rays_per_step": shadow_rays // args.steps,
                        "mrays_per_s": (ext_rays + shadow_rays) / (render_ms / 1000.0) / 1e6,
-                       "extend_ms_per_step": ext_ms / args.steps,
-                       "shade_and_shadow_ms_per_step": shade_ms / args.steps},
+                       "extend_ms_per_step": ext_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps,
+                       "shadow_ms_per_step": shadow_ms / args.steps},
             "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": frame_bytes,
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},

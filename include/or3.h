@@ -197,13 +197,16 @@ typedef struct or3_render_stats {
   int32_t passes;
   /* OR3_FLAG_TIME_KERNELS: summed device time and launch counts */
   double extend_ms;
-  double shade_ms;
+  double shade_ms;         /* the shade kernel (shadow rays are in shadow_ms) */
   uint64_t extend_launches;
   uint64_t shade_launches;
   /* OR3_FLAG_COUNT_TRAVERSAL: totals over all extension rays */
   uint64_t nodes_visited;  /* 64-byte wide nodes fetched */
   uint64_t tris_tested;    /* 48-byte triangle records tested */
   uint64_t spheres_tested; /* sphere records tested */
+  /* OR3_FLAG_TIME_KERNELS: the shadow-ray (any-hit) kernel, next-event estimation only */
+  double shadow_ms;
+  uint64_t shadow_launches;
 } or3_render_stats;
 
 typedef struct or3_scene_info {

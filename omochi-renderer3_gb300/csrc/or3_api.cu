@@ -357,7 +357,7 @@ int or3_context_create(int device, or3_context **out) {
   cudaMemset(ctx->dstats, 0, 8 * sizeof(unsigned long long));
   cudaEventCreate(&ctx->ev0);
   cudaEventCreate(&ctx->ev1);
-  for (int k = 0; k < 3; k++) cudaEventCreate(&ctx->kev[k]);
+  for (int k = 0; k < 4; k++) cudaEventCreate(&ctx->kev[k]);
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(OR3_ERR_CUDA);
   *out = ctx;
   return OR3_OK;
@@ -389,7 +389,7 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFreeHost(ctx->frame_pinned);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  for (int k = 0; k < 3; k++)
+  for (int k = 0; k < 4; k++)
     if (ctx->kev[k]) cudaEventDestroy(ctx->kev[k]);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -844,8 +844,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
-          if (shadows) launch_shadow(sg->view, q, grid_ext, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
+          if (shadows) launch_shadow(sg->view, q, grid_ext, st);
+          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[3], st));
           launch_reset_count(q, in, st);
           in ^= 1;
           OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t),
@@ -853,13 +854,18 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
           count = ctx->host_counters[in];
           if (timek) {
-            float e = 0.f, s2 = 0.f;
+            float e = 0.f, s2 = 0.f, s3 = 0.f;
             cudaEventElapsedTime(&e, ctx->kev[0], ctx->kev[1]);
             cudaEventElapsedTime(&s2, ctx->kev[1], ctx->kev[2]);
+            cudaEventElapsedTime(&s3, ctx->kev[2], ctx->kev[3]);
             stats.extend_ms += e;
             stats.shade_ms += s2;
             stats.extend_launches++;
             stats.shade_launches++;
+            if (shadows) {
+              stats.shadow_ms += s3;
+              stats.shadow_launches++;
+            }
           }
           if (ctx->host_counters[2]) break;
           if (bounce > 100000) break;

@@ -65,7 +65,7 @@ struct or3_context {
   uint64_t last_wave_paths = 0;
   bool last_kept_paths = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t kev[4] = {nullptr, nullptr, nullptr, nullptr};
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

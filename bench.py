@@ -379,6 +379,7 @@ def main():
     ap.add_argument("--res", default="", help="WxH override (smaller case for profiling)")
     ap.add_argument("--ss", type=int, default=0, help="sub-pixel grid override")
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"])
+    ap.add_argument("--tuning", type=int, default=0, help="or3_render_params.tuning (kernel variant A/B)")
     ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
@@ -417,7 +418,9 @@ def main():
     A = pkg.abi
     kw = dict(supersamples=st["supersamples"], min_samples=st["min_samples"], max_samples=st["max_samples"],
               step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"],
-              next_event_estimation=st.get("next_event_estimation", False))
+              next_event_estimation=st.get("next_event_estimation", False), tuning=args.tuning)
+    if args.tuning:
+        desc += "_tuning%d" % args.tuning
     t0 = time.perf_counter()
     sid = ctx.upload(sd)
     upload_s = time.perf_counter() - t0

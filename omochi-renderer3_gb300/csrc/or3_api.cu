@@ -810,6 +810,36 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const int smem_nodes =
       (prm->tuning & OR3_TUNE_SMEM_NODES) ? (int)std::min<uint64_t>(256, sg->view.num_nodes) : 0;
   const int variant = extend_variant(prm->tuning);
+  // L2 persisting window over the BVH nodes (a context setting, restored below)
+  const bool l2win = (prm->tuning & OR3_TUNE_L2_PERSIST) != 0;
+  if (l2win) {
+    int maxp = 0, maxw = 0;
+    cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, ctx->device);
+    cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device);
+    const size_t bytes = std::min<size_t>((size_t)sg->view.num_nodes * sizeof(WideNode), (size_t)maxw);
+    if (maxp > 0 && bytes > 0) {
+      cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min<size_t>(bytes, (size_t)maxp));
+      cudaStreamAttrValue a{};
+      a.accessPolicyWindow.base_ptr = (void *)sg->view.nodes;
+      a.accessPolicyWindow.num_bytes = bytes;
+      a.accessPolicyWindow.hitRatio = std::min(1.0f, (float)maxp / (float)bytes);
+      a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+      a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+      cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &a);
+    }
+  }
+  struct L2Restore {
+    bool on;
+    cudaStream_t st;
+    ~L2Restore() {
+      if (!on) return;
+      cudaStreamAttrValue a{};
+      a.accessPolicyWindow.num_bytes = 0;
+      cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &a);
+      cudaCtxResetPersistingL2Cache();
+      cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
+  } l2restore{l2win, st};
   const bool timek = (prm->flags & OR3_FLAG_TIME_KERNELS) != 0;
   const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
   const bool shadows = prm->next_event_estimation && (sg->view.num_lights > 0 || sg->view.env_light != 0);
@@ -845,7 +875,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
-          if (shadows) launch_shadow(sg->view, q, grid_ext, st);
+          if (shadows) launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[3], st));
           launch_reset_count(q, in, st);
           in ^= 1;

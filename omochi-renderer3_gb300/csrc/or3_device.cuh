@@ -204,6 +204,55 @@ __device__ __forceinline__ void trav_init(TravState &s, V3 o, V3 d, float tmax, 
   s.sp = 0;
 }
 
+// Traversal stacks for trav_step_inline: put(i, entry, key), ent(i), key(i).
+// LocalStack: the thread's arrays (local memory).  SplitStack<KS>: entries
+// [0, KS) in shared memory, one column per thread of the block (stride =
+// blockDim.x, so a warp's accesses fall in distinct banks), deeper ones in
+// local memory; most traversals never leave the shared part.
+struct LocalStack {
+  uint32_t *e;
+  float *t;
+  __device__ __forceinline__ void put(int i, uint32_t ee, float tt) {
+    e[i] = ee;
+    t[i] = tt;
+  }
+  __device__ __forceinline__ uint32_t ent(int i) const { return e[i]; }
+  __device__ __forceinline__ float key(int i) const { return t[i]; }
+};
+
+template <int KS>
+struct SplitStack {
+  uint32_t *se;  // shared, this thread's column
+  float *st;
+  uint32_t stride;
+  uint32_t le[kStackSize - KS];
+  float lt[kStackSize - KS];
+  __device__ __forceinline__ void put(int i, uint32_t ee, float tt) {
+    if (i < KS) {
+      se[i * stride] = ee;
+      st[i * stride] = tt;
+    } else {
+      le[i - KS] = ee;
+      lt[i - KS] = tt;
+    }
+  }
+  __device__ __forceinline__ uint32_t ent(int i) const { return i < KS ? se[i * stride] : le[i - KS]; }
+  __device__ __forceinline__ float key(int i) const { return i < KS ? st[i * stride] : lt[i - KS]; }
+};
+
+template <class STK>
+__device__ __forceinline__ bool trav_pop_stk(TravState &s, const STK &stk) {
+  while (s.sp > 0) {
+    s.sp--;
+    if (stk.key(s.sp) <= s.tmax * 1.0000010f) {
+      s.entry = stk.ent(s.sp);
+      return true;
+    }
+  }
+  s.entry = kNoEntry;
+  return false;
+}
+
 // Pops the nearest pending entry that can still hold a closer hit; false when none.
 __device__ __forceinline__ bool trav_pop(TravState &s, const uint32_t *stk_e, const float *stk_t) {
   while (s.sp > 0) {
@@ -360,8 +409,10 @@ __device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint3
 
 // One node per step; the node's hit leaf children are tested right away and
 // only internal children go through the stack (stack entries are node indices).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, uint32_t *stk_e, float *stk_t,
+// SORT: visit internal children nearest first (closest hit); an any-hit
+// query may take them in slot order.
+template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack>
+__device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, STK &stk,
                                                  const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
   const uint32_t e = s.entry;
   if (e == kNoEntry) return true;
@@ -416,6 +467,29 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
     trav_leaf<COUNT>(S, s, first, (counts >> (8 * i)) & 0xFFu, cnt);
   }
   if (ANY && s.rec != kMissRec) return true;
+  const float inf2 = kInf * 2.f;
+  if (!SORT) {
+    // slot order: the first internal child hit is next, the others go on the stack
+    uint32_t nxt = kNoEntry;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (key[j] < inf2) {
+        if (nxt == kNoEntry) {
+          nxt = kid[j];
+        } else if (s.sp < kStackSize) {
+          stk.put(s.sp, kid[j], key[j]);
+          s.sp++;
+        } else {
+          atomicOr(err, 1u);
+        }
+      }
+    }
+    if (nxt != kNoEntry) {
+      s.entry = nxt;
+      return false;
+    }
+    return !trav_pop_stk(s, stk);
+  }
 #define OR3_CSWAP(a, b)                                       \
   if (key[b] < key[a]) {                                      \
     const float tk = key[a]; key[a] = key[b]; key[b] = tk;     \
@@ -423,15 +497,13 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
   }
   OR3_CSWAP(0, 1) OR3_CSWAP(2, 3) OR3_CSWAP(0, 2) OR3_CSWAP(1, 3) OR3_CSWAP(1, 2)
 #undef OR3_CSWAP
-  const float inf2 = kInf * 2.f;
   const float tl2 = s.tmax * 1.0000010f;
   if (key[0] < inf2 && key[0] <= tl2) {
 #pragma unroll
     for (int j = 3; j >= 1; j--) {
       if (key[j] < inf2 && key[j] <= tl2) {
         if (s.sp < kStackSize) {
-          stk_e[s.sp] = kid[j];
-          stk_t[s.sp] = key[j];
+          stk.put(s.sp, kid[j], key[j]);
           s.sp++;
         } else {
           atomicOr(err, 1u);
@@ -441,7 +513,7 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
     s.entry = kid[0];
     return false;
   }
-  return !trav_pop(s, stk_e, stk_t);
+  return !trav_pop_stk(s, stk);
 }
 
 // After the BVH: the not-in-BVH objects, strictly closer only (Scene.cpp:73-83).

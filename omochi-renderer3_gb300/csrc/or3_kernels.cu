@@ -89,12 +89,36 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 //         any idle lane every step;
 // STEP 2: one node per step with its hit leaves tested in place, refill only
 //         once at least half of the warp is idle (amortises the atomic).
-template <bool ANY, bool COUNT, int STEP, class Src, class Sink>
+// The STEP 2 stack: local arrays (KS = 0) or the first KS entries in shared
+// memory (one static allocation of KS x 256 entries per kernel that uses it;
+// blocks of at most 256 threads).
+template <int KS>
+struct StackOf {
+  __device__ __forceinline__ static SplitStack<KS> make(uint32_t *, float *) {
+    __shared__ uint32_t sh_e[KS * 256];
+    __shared__ float sh_t[KS * 256];
+    SplitStack<KS> s;
+    s.se = sh_e + threadIdx.x;
+    s.st = sh_t + threadIdx.x;
+    s.stride = blockDim.x;
+    return s;
+  }
+};
+template <>
+struct StackOf<0> {
+  __device__ __forceinline__ static LocalStack make(uint32_t *e, float *t) { return LocalStack{e, t}; }
+};
+
+// REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
+// nearest-first child order (off only for any-hit queries).  KS: stack
+// entries kept in shared memory (STEP 2).
+template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, int KS = 0>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
+  auto stk = StackOf<STEP == 2 ? KS : 0>::make(stk_e, stk_t);
   TravState st;
   uint32_t r = kNoEntry;
   bool exhausted = false;
@@ -102,7 +126,7 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
   for (;;) {
     const bool need = (r == kNoEntry) && !exhausted;
     unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    if (STEP == 2 && __popc(m) < 16 && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
+    if (STEP == 2 && __popc(m) < REFILL && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
     if (m) {
       const int leader = __ffs(m) - 1;
       uint32_t base = 0;
@@ -124,7 +148,7 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
     if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
       const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                  : trav_step_inline<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err);
+                                  : trav_step_inline<ANY, COUNT, SORT>(S, st, stk, snodes, ns, cnt, err);
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;
@@ -178,9 +202,22 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 // Closest hit for every queued ray.  COUNT adds the nodes, triangles and
 // spheres each ray touched to stats[3..5] (the algorithmic byte count).
 // VARIANT 0: gridstride_trace; 1, 2: persistent_trace<STEP = VARIANT>.
+// VARIANT 0: gridstride_trace; 1: persistent_trace STEP 1; 2, 4, 5: STEP 2
+// refilling at 16, 8 or 24 idle lanes; 6, 7: STEP 2 with the top 16 / 8
+// stack entries in shared memory.
+template <bool COUNT, int VARIANT>
+__device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, int in, int smem_nodes,
+                                            uint4 *snodes);
+
 template <bool COUNT, int VARIANT>
 __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
   __shared__ uint4 snodes[kSmemNodes * 4];
+  extend_body<COUNT, VARIANT>(S, q, in, smem_nodes, snodes);
+}
+
+template <bool COUNT, int VARIANT>
+__device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, int in, int smem_nodes,
+                                            uint4 *snodes) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const uint32_t ns = stage_nodes(S, snodes, smem_nodes);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -192,8 +229,12 @@ __global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, in
     gridstride_trace<false, COUNT>(S, n, QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
                                    &q.counters[2]);
   } else {
-    persistent_trace<false, COUNT, VARIANT == 1 ? 1 : 2>(S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]},
-                                                         HitSink{q.hits}, snodes, ns, cnt, &q.counters[2]);
+    constexpr int kStep = VARIANT == 1 ? 1 : 2;
+    constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
+    constexpr int kShared = VARIANT == 6 ? 16 : VARIANT == 7 ? 8 : 0;
+    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, true, kShared>(
+        S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
+        &q.counters[2]);
   }
   if (COUNT) {
     unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
@@ -649,11 +690,14 @@ struct ShadowSink {
 };
 
 // Any-hit test of every queued shadow ray (persistent, lane-refilled).
+// SORT false: children in slot order (no distance sort).
+template <bool SORT>
 __global__ void __launch_bounds__(256) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  persistent_trace<true, false, 2>(S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir},
-                                   ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u, nullptr, &q.counters[2]);
+  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT>(
+      S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir}, ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u,
+      nullptr, &q.counters[2]);
 }
 
 // Per-pixel sums of the wave's path radiance: one warp per pixel, lanes over
@@ -806,6 +850,7 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
                                             const Sink &sink, uint32_t *cnt, uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
+  LocalStack stk{stk_e, stk_t};
   TravState st;
   const DevScene *sp = nullptr;
   uint32_t r = kNoEntry;
@@ -837,7 +882,7 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
     }
     if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
-      if (trav_step_inline<ANY, COUNT>(*sp, st, stk_e, stk_t, nullptr, 0u, cnt, err)) {
+      if (trav_step_inline<ANY, COUNT>(*sp, st, stk, nullptr, 0u, cnt, err)) {
         sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);
         r = kNoEntry;
       }
@@ -941,9 +986,14 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
   switch ((count ? 8 : 0) | (variant & 7)) {
     case 1: k_extend<false, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 4: k_extend<false, 4><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 5: k_extend<false, 5><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 6: k_extend<false, 6><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 7: k_extend<false, 7><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 8: k_extend<true, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 9: k_extend<true, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 10: k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 10: case 12: case 13: case 14: case 15:  // counting runs use the default traversal
+      k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
     default: k_extend<false, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
   }
 }
@@ -960,8 +1010,9 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
   k_reset_count<<<1, 1, 0, st>>>(q.counters, which);
 }
 
-void launch_shadow(const DevScene &S, const Queues &q, int grid, cudaStream_t st) {
-  k_shadow<<<grid, 256, 0, st>>>(S, q);
+void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, cudaStream_t st) {
+  if (unsorted) k_shadow<false><<<grid, 256, 0, st>>>(S, q);
+  else k_shadow<true><<<grid, 256, 0, st>>>(S, q);
 }
 
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st) {

@@ -178,8 +178,7 @@ typedef struct or3_render_params {
 #define OR3_TUNE_EXTEND_MASK 0x7u  /* extend kernel: 0 default (= 2); 1 persistent, one node or leaf per step;
                                       2 persistent, node steps with leaves in place, lanes refilled once
                                       16 are idle; 3 one ray per thread; 4, 5 as 2 refilling at 8 / 24
-                                      idle lanes; 6, 7 as 2 with the top 16 / 8 stack entries in
-                                      shared memory */
+                                      idle lanes; 6, 7 = 2 */
 #define OR3_TUNE_SMEM_NODES 0x10u  /* stage the top BVH nodes in shared memory */
 #define OR3_TUNE_SHADOW_UNSORTED 0x20u /* shadow rays take children in slot order (no distance sort) */
 #define OR3_TUNE_L2_PERSIST 0x40u      /* or3_render: L2 persisting access window over the BVH nodes */

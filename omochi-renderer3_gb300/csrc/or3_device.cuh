@@ -204,11 +204,8 @@ __device__ __forceinline__ void trav_init(TravState &s, V3 o, V3 d, float tmax, 
   s.sp = 0;
 }
 
-// Traversal stacks for trav_step_inline: put(i, entry, key), ent(i), key(i).
-// LocalStack: the thread's arrays (local memory).  SplitStack<KS>: entries
-// [0, KS) in shared memory, one column per thread of the block (stride =
-// blockDim.x, so a warp's accesses fall in distinct banks), deeper ones in
-// local memory; most traversals never leave the shared part.
+// Traversal stack for trav_step_inline: put(i, entry, key), ent(i), key(i)
+// over the thread's arrays (local memory).
 struct LocalStack {
   uint32_t *e;
   float *t;
@@ -218,26 +215,6 @@ struct LocalStack {
   }
   __device__ __forceinline__ uint32_t ent(int i) const { return e[i]; }
   __device__ __forceinline__ float key(int i) const { return t[i]; }
-};
-
-template <int KS>
-struct SplitStack {
-  uint32_t *se;  // shared, this thread's column
-  float *st;
-  uint32_t stride;
-  uint32_t le[kStackSize - KS];
-  float lt[kStackSize - KS];
-  __device__ __forceinline__ void put(int i, uint32_t ee, float tt) {
-    if (i < KS) {
-      se[i * stride] = ee;
-      st[i * stride] = tt;
-    } else {
-      le[i - KS] = ee;
-      lt[i - KS] = tt;
-    }
-  }
-  __device__ __forceinline__ uint32_t ent(int i) const { return i < KS ? se[i * stride] : le[i - KS]; }
-  __device__ __forceinline__ float key(int i) const { return i < KS ? st[i * stride] : lt[i - KS]; }
 };
 
 template <class STK>

@@ -89,36 +89,15 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 //         any idle lane every step;
 // STEP 2: one node per step with its hit leaves tested in place, refill only
 //         once at least half of the warp is idle (amortises the atomic).
-// The STEP 2 stack: local arrays (KS = 0) or the first KS entries in shared
-// memory (one static allocation of KS x 256 entries per kernel that uses it;
-// blocks of at most 256 threads).
-template <int KS>
-struct StackOf {
-  __device__ __forceinline__ static SplitStack<KS> make(uint32_t *, float *) {
-    __shared__ uint32_t sh_e[KS * 256];
-    __shared__ float sh_t[KS * 256];
-    SplitStack<KS> s;
-    s.se = sh_e + threadIdx.x;
-    s.st = sh_t + threadIdx.x;
-    s.stride = blockDim.x;
-    return s;
-  }
-};
-template <>
-struct StackOf<0> {
-  __device__ __forceinline__ static LocalStack make(uint32_t *e, float *t) { return LocalStack{e, t}; }
-};
-
 // REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
-// nearest-first child order (off only for any-hit queries).  KS: stack
-// entries kept in shared memory (STEP 2).
-template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, int KS = 0>
+// nearest-first child order (off only for any-hit queries).
+template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
-  auto stk = StackOf<STEP == 2 ? KS : 0>::make(stk_e, stk_t);
+  LocalStack stk{stk_e, stk_t};
   TravState st;
   uint32_t r = kNoEntry;
   bool exhausted = false;
@@ -132,8 +111,8 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
       uint32_t base = 0;
       if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
       if (need) {
-        const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
         if (idx < n) {
           V3 o, d;
           float tmax;
@@ -203,8 +182,7 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 // spheres each ray touched to stats[3..5] (the algorithmic byte count).
 // VARIANT 0: gridstride_trace; 1, 2: persistent_trace<STEP = VARIANT>.
 // VARIANT 0: gridstride_trace; 1: persistent_trace STEP 1; 2, 4, 5: STEP 2
-// refilling at 16, 8 or 24 idle lanes; 6, 7: STEP 2 with the top 16 / 8
-// stack entries in shared memory.
+// refilling at 16, 8 or 24 idle lanes.
 template <bool COUNT, int VARIANT>
 __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, int in, int smem_nodes,
                                             uint4 *snodes);
@@ -231,8 +209,7 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
   } else {
     constexpr int kStep = VARIANT == 1 ? 1 : 2;
     constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
-    constexpr int kShared = VARIANT == 6 ? 16 : VARIANT == 7 ? 8 : 0;
-    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, true, kShared>(
+    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill>(
         S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
         &q.counters[2]);
   }
@@ -988,8 +965,6 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
     case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 4: k_extend<false, 4><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 5: k_extend<false, 5><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 6: k_extend<false, 6><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 7: k_extend<false, 7><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 8: k_extend<true, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 9: k_extend<true, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 10: case 12: case 13: case 14: case 15:  // counting runs use the default traversal

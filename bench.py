@@ -380,6 +380,8 @@ def main():
     ap.add_argument("--ss", type=int, default=0, help="sub-pixel grid override")
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"])
     ap.add_argument("--tuning", type=int, default=0, help="or3_render_params.tuning (kernel variant A/B)")
+    ap.add_argument("--leaf-max", type=int, default=0, help="BVH leaf size bound (0 = library default)")
+    ap.add_argument("--trav-cost", type=float, default=0.0, help="BVH SAH node cost (0 = library default)")
     ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
@@ -421,6 +423,9 @@ def main():
               next_event_estimation=st.get("next_event_estimation", False), tuning=args.tuning)
     if args.tuning:
         desc += "_tuning%d" % args.tuning
+    if args.leaf_max or args.trav_cost:
+        sd.leaf_max, sd.traversal_cost = args.leaf_max, args.trav_cost
+        desc += "_leaf%d_ct%g" % (args.leaf_max, args.trav_cost)
     t0 = time.perf_counter()
     sid = ctx.upload(sd)
     upload_s = time.perf_counter() - t0

@@ -122,6 +122,10 @@ typedef struct or3_scene_desc {
 
   /* where the BVH is built (OR3_BUILD_*); zero-initialised = automatic */
   uint32_t build;
+  /* BVH build: primitives per leaf at most (0 = 4, up to 8); SAH cost of a
+     node visit relative to a primitive test (0 = 1, the reference's) */
+  uint32_t leaf_max;
+  double traversal_cost;
 } or3_scene_desc;
 
 /* BVH build location.  Both build the same kind of tree (binned SAH, 16 bins,

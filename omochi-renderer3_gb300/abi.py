@@ -57,7 +57,8 @@ class SceneDescC(ctypes.Structure):
         ("env_rgbe", P(ctypes.c_uint8)),
         ("background", c_double3),
         ("num_textures", ctypes.c_uint32), ("texture_dims", u32p), ("texture_offsets", P(ctypes.c_uint64)),
-        ("texture_rgb", f32p), ("build", ctypes.c_uint32),
+        ("texture_rgb", f32p), ("build", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32),
+        ("traversal_cost", ctypes.c_double),
     ]
 
 

@@ -2,8 +2,9 @@
 //
 // Design (own, not the reference's):
 //   * binned SAH over centroids (bins per axis configurable, 16 by default),
-//     traversal cost 1, primitive cost 1 -- the same unit costs the reference's
-//     sweep uses (T_aabb = T_tri = 1, src/renderer/BVH.cpp:235-236);
+//     primitive cost 1 and a node cost (1 by default -- the same unit costs
+//     the reference's sweep uses, T_aabb = T_tri = 1,
+//     src/renderer/BVH.cpp:235-236);
 //   * leaves of at most `leaf_max` primitives; a node of <= leaf_max
 //     primitives becomes a leaf when that is not costlier than its best split;
 //   * a hard binary depth bound (kMaxBinaryDepth) enforced by switching to
@@ -59,12 +60,13 @@ struct BNode {
 struct Builder {
   const std::vector<BuildPrim> &prims;
   int bins, leaf_max;
+  double trav_cost = 1.0;  // SAH cost of a node relative to one primitive test
   std::vector<uint32_t> idx;
   std::vector<float> cent;  // 3 per prim
   std::vector<BNode> nodes;
   int max_depth = 0;
 
-  Builder(const std::vector<BuildPrim> &p, int b, int l) : prims(p), bins(b), leaf_max(l) {}
+  Builder(const std::vector<BuildPrim> &p, int b, int l, double ct) : prims(p), bins(b), leaf_max(l), trav_cost(ct) {}
 
   AABB prim_box(uint32_t i) const {
     AABB b;
@@ -321,7 +323,7 @@ struct Builder {
             acc.grow(bb[b]);
             cnt += bc[b];
             if (cnt == 0 || rightCnt[b + 1] == 0) continue;
-            const double cost = 1.0 + (acc.area() * cnt + rightArea[b + 1] * rightCnt[b + 1]) /
+            const double cost = trav_cost + (acc.area() * cnt + rightArea[b + 1] * rightCnt[b + 1]) /
                                           std::max(parentArea, 1e-30);
             if (cost < bestCost) { bestCost = cost; bestAxis = a; bestBin = b; }
           }
@@ -496,10 +498,10 @@ void decode_child_box(const WideNode &n, int c, float lo[3], float hi[3]) {
 }
 
 bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max, WideBVH &out,
-                    std::string *err) {
+                    std::string *err, double trav_cost) {
   out = WideBVH();
-  if (bins < 2 || bins > 256 || leaf_max < 1 || leaf_max > 4) {
-    if (err) *err = "build_wide_bvh: bins must be in [2,256] and leaf_max in [1,4]";
+  if (bins < 2 || bins > 256 || leaf_max < 1 || leaf_max > 8 || !(trav_cost > 0)) {
+    if (err) *err = "build_wide_bvh: bins must be in [2,256], leaf_max in [1,8], traversal cost > 0";
     return false;
   }
   for (const BuildPrim &p : prims)
@@ -510,7 +512,7 @@ bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max,
       }
   if (prims.empty()) return true;
 
-  Builder b(prims, bins, leaf_max);
+  Builder b(prims, bins, leaf_max, trav_cost);
   b.build();
   out.binary_depth = b.max_depth;
   out.binary_nodes = b.nodes.size();

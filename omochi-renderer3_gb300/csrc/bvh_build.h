@@ -29,8 +29,9 @@ struct WideBVH {
 
 // Returns false (with *err) on invalid input.  An empty prim list yields an
 // empty node array.
+// trav_cost: SAH cost of visiting a node, relative to one primitive test.
 bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max, WideBVH &out,
-                    std::string *err);
+                    std::string *err, double trav_cost = 1.0);
 
 // Decoded child box of a quantised node, exactly as the kernels compute it.
 void decode_child_box(const WideNode &n, int child, float lo[3], float hi[3]);

@@ -3,7 +3,8 @@
 // Replaces the host build (itself replacing the reference's full-sweep SAH,
 // src/renderer/BVH.cpp:164-312, and its 4-wide collapse,
 // src/renderer/QBVH.cpp:208-272) for large scenes, with the same tree rules:
-// binned SAH over centroids with 16 bins and unit costs; leaves of at most
+// binned SAH over centroids with 16 bins (node cost trav_cost, primitive
+// cost 1); leaves of at most
 // leaf_max primitives when a leaf is not costlier than the best split; the
 // binary depth bound kMaxBinaryDepth kept by median splits; the greedy 4-wide
 // collapse by largest child area, breadth first when that tree would be too
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(256) k_bin(uint32_t n, const uint32_t *idx, co
 
 // One thread per large node: node record, split choice, children.
 __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbox, const uint32_t *bins,
-                         int leaf_max, DNode *nodes, Decision *dec, Task *next, Task *small, Counters *ctr) {
+                         int leaf_max, double ct, DNode *nodes, Decision *dec, Task *next, Task *small, Counters *ctr) {
   const uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
   if (ti >= ntasks) return;
   const Task t = tasks[ti];
@@ -290,7 +291,7 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
         }
         cnt += w[6];
         if (cnt == 0 || rcnt[b + 1] == 0) continue;
-        const double cost = 1.0 + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
+        const double cost = ct + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
         if (cost < best) {
           best = cost;
           d.axis = a;
@@ -485,7 +486,7 @@ __device__ __forceinline__ float warp_max(float v) {
 // buffer); lane 0 evaluates the SAH and owns the stack.
 __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, const Task *small,
                                                             const BuildPrim *prims, uint32_t *idx, int leaf_max,
-                                                            DNode *nodes, Counters *ctr) {
+                                                            double ct, DNode *nodes, Counters *ctr) {
   __shared__ SmallShared sh_all[kSmallWarps];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t si = blockIdx.x * kSmallWarps + (threadIdx.x >> 5);
@@ -601,7 +602,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
             cnt += w[6];
             if (cnt == 0 || rcnt[b + 1] == 0) continue;
             const double cost =
-                1.0 + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
+                ct + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
             if (cost < best) {
               best = cost;
               axis = a;
@@ -803,7 +804,7 @@ __global__ void k_leaf_kinds(uint32_t nw, WideNode *wn, uint32_t *order, const B
     const uint32_t cnt = w.count[k];
     if (cnt == 0) continue;
     uint32_t *b = order + w.child[k];
-    uint32_t tri[4], sph[4], nt = 0, ns = 0;
+    uint32_t tri[15], sph[15], nt = 0, ns = 0;
     for (uint32_t j = 0; j < cnt; j++) {
       if (prims[b[j]].kind == kPrimTriangle) tri[nt++] = b[j];
       else sph[ns++] = b[j];
@@ -828,14 +829,14 @@ cudaError_t grow(T **p, size_t &cap, size_t n) {
 }  // namespace
 
 bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cudaStream_t st, DeviceBVH &out,
-                           std::string *err) {
+                           std::string *err, double trav_cost) {
   out = DeviceBVH();
   auto fail = [&](const char *what, cudaError_t e) {
     if (err) *err = std::string("device BVH build: ") + what + ": " + cudaGetErrorString(e);
     return false;
   };
-  if (n == 0 || n > (1u << 26) || leaf_max < 1 || leaf_max > 4) {
-    if (err) *err = "device BVH build: 1 <= primitives <= 2^26 and leaf_max in [1,4] required";
+  if (n == 0 || n > (1u << 26) || leaf_max < 1 || leaf_max > 8 || !(trav_cost > 0)) {
+    if (err) *err = "device BVH build: 1 <= primitives <= 2^26, leaf_max in [1,8], traversal cost > 0";
     return false;
   }
   uint32_t *idx = nullptr, *idx2 = nullptr, *pt = nullptr, *pt2 = nullptr, *flags = nullptr, *scan = nullptr,
@@ -888,7 +889,7 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
       k_bounds<<<nblk, 256, 0, st>>>(n, idx, pt, prims, tbox);
       k_bin<<<nblk, 256, 0, st>>>(n, idx, pt, prims, tbox, bins);
       cudaMemsetAsync(&ctr->next_tasks, 0, sizeof(uint32_t), st);
-      k_decide<<<(ntasks + 127) / 128, 128, 0, st>>>(ntasks, tasks, tbox, bins, leaf_max, nodes, dec, next, small, ctr);
+      k_decide<<<(ntasks + 127) / 128, 128, 0, st>>>(ntasks, tasks, tbox, bins, leaf_max, trav_cost, nodes, dec, next, small, ctr);
       k_flags<<<(n + 255) / 256, 256, 0, st>>>(n, idx, pt, tasks, dec, prims, flags);
       k_scan_blocks<<<nsb, 256, 0, st>>>(n, flags, scan, sums);
       k_scan_sums<<<1, 1024, 0, st>>>(nsb, sums);
@@ -913,7 +914,7 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
     }
     if (hc.small)
       k_small<<<(hc.small + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, 0, st>>>(hc.small, small, prims, idx,
-                                                                                       leaf_max, nodes, ctr);
+                                                                                       leaf_max, trav_cost, nodes, ctr);
     // phase 3: greedy collapse, breadth first if that is deeper than the stack allows
     for (int pass = 0; pass < 2; pass++) {
       const uint32_t one = 1, zero = 0;

@@ -25,7 +25,7 @@ struct DeviceBVH {
 // prims: device array of n primitive bounds (input order).  Blocks on `st`.
 // Returns false (with *err) on invalid input or a CUDA error.
 bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cudaStream_t st, DeviceBVH &out,
-                           std::string *err);
+                           std::string *err, double trav_cost = 1.0);
 
 // Records, PrimInfo and TriShade from input order into leaf order.
 void gather_leaf_order(uint32_t n, const uint32_t *order, const float4 *prims_in, const PrimInfo *info_in,

@@ -505,6 +505,12 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     free_scene(sg);
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "unknown build location %u", d->build);
   }
+  const int leaf_max = d->leaf_max ? (int)d->leaf_max : 4;
+  const double trav_cost = d->traversal_cost > 0 ? d->traversal_cost : 1.0;
+  if (leaf_max > 8) {
+    free_scene(sg);
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "leaf_max %d: at most 8", leaf_max);
+  }
   const bool on_device = np > 0 && np <= (1u << 26) &&
                          (d->build == OR3_BUILD_DEVICE ||
                           (d->build == OR3_BUILD_AUTO && np >= OR3_BUILD_DEVICE_MIN_PRIMS));
@@ -513,7 +519,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   DeviceTemps tmp;  // freed when the upload returns (after its stream sync)
   std::string berr;
   if (!on_device) {
-    if (!build_wide_bvh(bp, 16, 4, bvh, &berr)) {
+    if (!build_wide_bvh(bp, 16, leaf_max, bvh, &berr, trav_cost)) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s", berr.c_str());
     }
@@ -532,7 +538,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(ce));
     }
-    if (!build_wide_bvh_device(bp_dev, np, 4, ctx->stream, dbvh, &berr)) {
+    if (!build_wide_bvh_device(bp_dev, np, leaf_max, ctx->stream, dbvh, &berr, trav_cost)) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "%s", berr.c_str());
     }

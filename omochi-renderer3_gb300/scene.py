@@ -67,6 +67,8 @@ class SceneDesc:
     background: tuple = (0.0, 0.0, 0.0)
     textures: list = field(default_factory=list)
     build: int = 0  # abi.OR3_BUILD_*
+    leaf_max: int = 0          # BVH leaf size bound (0 = 4)
+    traversal_cost: float = 0.0  # SAH node cost (0 = 1)
 
     # ---- materials
     def material(self, mtype=abi.OR3_LAMBERT, color=(0, 0, 0), emission=(0, 0, 0), ior=0.0,
@@ -271,6 +273,8 @@ class SceneDesc:
             d.texture_offsets = _ptr(a["texture_offsets"], ctypes.c_uint64)
             d.texture_rgb = _ptr(a["texture_rgb"], ctypes.c_float)
         d.build = self.build
+        d.leaf_max = self.leaf_max
+        d.traversal_cost = self.traversal_cost
         return d, keep
 
 

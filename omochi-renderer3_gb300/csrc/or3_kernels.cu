@@ -571,7 +571,8 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
 // BATCH: the ray's segment (beta.w) selects the job's scene, constants and
 // RNG numbering; continuation rays inherit it.
 template <bool BATCH, bool NEE>
-__global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in, Batch b) {
+__global__ void __launch_bounds__(256, NEE ? 3 : 4) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in,
+                                                            Batch b) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const int out = in ^ 1;
   const uint32_t lane = threadIdx.x & 31u;

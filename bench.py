@@ -12,8 +12,9 @@ value      camera paths / device time of the passes (CUDA events on the
            library's stream, scene resident in HBM), Mpaths/s
 e2e        the same through the C ABI from host buffers: scene upload
            (flatten + BVH build + H2D), render, frame D2H, per step
-roofline   extend (closest-hit) kernel: algorithmic bytes (64 B per wide node
-           fetched, 48 B per triangle record, 16 B per sphere record, counted
+roofline   extend (closest-hit) kernel: algorithmic bytes (128 B per wide node
+           fetched -- FP32 child boxes; 64 B for the quantised variants 1, 3, 6
+           --, 48 B per triangle record, 16 B per sphere record, counted
            by an instrumented run of the same render) / its event-timed
            duration, against the measured HBM copy bandwidth
 cpu_baseline  the C oracle (FP64 restatement of the reference path, its BVH)
@@ -38,9 +39,11 @@ import __graft_entry__ as ge  # noqa: E402
 METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency when served"
 
 # DRAM bytes (read + write) per ray of the extend kernel, from one ncu capture
-# per workload (profiles/k_extend_<workload>_*.md); roofline.traffic is this
-# times the rays of an average launch.
-EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.0}
+# per workload on a smaller image of the same scene (camera rays: queue bytes
+# grow with the rays; profiles/k_extend_mesh_512x384.md,
+# profiles/k_traversal_terrain_480x270.md); roofline.traffic is this times
+# the rays of an average launch.
+EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.2, "terrain": 52.0}
 
 
 def workload(pkg, name):
@@ -433,7 +436,8 @@ def main():
 
     # algorithmic bytes per extension ray (instrumented run, untimed)
     c = ctx.render(sid, cam, seed=99, flags=A.OR3_FLAG_COUNT_TRAVERSAL, **kw)
-    alg_bytes_per_ray = (64.0 * c["nodes_visited"] + 48.0 * c["tris_tested"] + 16.0 * c["spheres_tested"]) / \
+    node_bytes = 64.0 if (args.tuning & 7) in (1, 3, 6) else 128.0  # quantised or FP32 child boxes
+    alg_bytes_per_ray = (node_bytes * c["nodes_visited"] + 48.0 * c["tris_tested"] + 16.0 * c["spheres_tested"]) / \
         max(c["extension_rays"], 1)
 
     for i in range(args.warmup):
@@ -505,7 +509,9 @@ def main():
                        "wall_s_timed": wall_s, "shadow_rays_per_step": shadow_rays // args.steps,
                        "mrays_per_s": (ext_rays + shadow_rays) / (render_ms / 1000.0) / 1e6,
                        "extend_ms_per_step": ext_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps,
-                       "shadow_ms_per_step": shadow_ms / args.steps},
+                       "shadow_ms_per_step": shadow_ms / args.steps,
+                       "per_extension_ray": {k: c[k] / max(c["extension_rays"], 1)
+                                             for k in ("nodes_visited", "tris_tested", "spheres_tested")}},
             "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": frame_bytes,
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},

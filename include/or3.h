@@ -182,8 +182,10 @@ typedef struct or3_render_params {
 #define OR3_TUNE_EXTEND_MASK 0x7u  /* extend kernel: 0 default (= 2); 1 persistent, one node or leaf per step;
                                       2 persistent, node steps with leaves in place, lanes refilled once
                                       16 are idle; 3 one ray per thread; 4, 5 as 2 refilling at 8 / 24
-                                      idle lanes; 6, 7 = 2 */
-#define OR3_TUNE_SMEM_NODES 0x10u  /* stage the top BVH nodes in shared memory */
+                                      idle lanes; 6 as 2 over the 8-bit quantised child boxes (shadow
+                                      rays too); 7 = 2.  2, 4, 5 test FP32 child boxes; 1, 3, 6 the
+                                      quantised ones */
+#define OR3_TUNE_SMEM_NODES 0x10u  /* stage the top quantised BVH nodes in shared memory (variants 1, 3, 6) */
 #define OR3_TUNE_SHADOW_UNSORTED 0x20u /* shadow rays take children in slot order (no distance sort) */
 #define OR3_TUNE_L2_PERSIST 0x40u      /* or3_render: L2 persisting access window over the BVH nodes */
 
@@ -209,7 +211,7 @@ typedef struct or3_render_stats {
   uint64_t extend_launches;
   uint64_t shade_launches;
   /* OR3_FLAG_COUNT_TRAVERSAL: totals over all extension rays */
-  uint64_t nodes_visited;  /* 64-byte wide nodes fetched */
+  uint64_t nodes_visited;  /* wide nodes fetched (128 bytes with FP32 child boxes, 64 quantised) */
   uint64_t tris_tested;    /* 48-byte triangle records tested */
   uint64_t spheres_tested; /* sphere records tested */
   /* OR3_FLAG_TIME_KERNELS: the shadow-ray (any-hit) kernel, next-event estimation only */
@@ -219,7 +221,7 @@ typedef struct or3_render_stats {
 
 typedef struct or3_scene_info {
   uint64_t num_primitives;
-  uint64_t num_nodes;      /* 64-byte wide nodes */
+  uint64_t num_nodes;      /* wide nodes */
   uint64_t device_bytes;
   double build_ms;         /* host BVH build */
   double upload_ms;        /* H2D copies */

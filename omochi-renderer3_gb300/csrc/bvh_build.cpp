@@ -22,6 +22,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <thread>
 
 namespace or3 {
@@ -392,14 +393,26 @@ void quantise(WideNode &w, const AABB &nodeBox, const AABB *childBox, int nchild
   }
 }
 
+// Child boxes of one wide node in WideNodeF::b order (empty slots +inf / -inf).
+void set_boxes(float *dst, const AABB &parent, const AABB *boxes, int nchild) {
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 4; c++) {
+      float lo = INFINITY, hi = -INFINITY;
+      if (c < nchild) fnode_slab(parent.lo[a], parent.hi[a], boxes[c].lo[a], boxes[c].hi[a], &lo, &hi);
+      dst[(2 * a) * 4 + c] = lo;
+      dst[(2 * a + 1) * 4 + c] = hi;
+    }
+}
+
 struct Collapser {
   const std::vector<BNode> &bn;
   std::vector<WideNode> &out;
+  std::vector<float> &fbox;
   bool breadth_first;
   int max_depth = 0;
 
-  Collapser(const std::vector<BNode> &b, std::vector<WideNode> &o, bool bf)
-      : bn(b), out(o), breadth_first(bf) {}
+  Collapser(const std::vector<BNode> &b, std::vector<WideNode> &o, std::vector<float> &f, bool bf)
+      : bn(b), out(o), fbox(f), breadth_first(bf) {}
 
   void gather(int root, std::vector<int> &kids) const {
     kids.clear();
@@ -464,6 +477,7 @@ struct Collapser {
       }
       out[slot] = w;
     }
+    fbox.assign(24 * out.size(), 0.f);
     // quantised boxes (independent per node): all host threads
     unsigned threads = std::thread::hardware_concurrency();
     threads = std::max(1u, std::min(threads, 64u));
@@ -477,6 +491,7 @@ struct Collapser {
           AABB boxes[4];
           for (int k = 0; k < it.nkids; k++) boxes[k] = bn[it.kids[k]].box;
           quantise(out[it.slot], bn[it.root].box, boxes, it.nkids);
+          set_boxes(&fbox[24 * (size_t)it.slot], bn[it.root].box, boxes, it.nkids);
         }
       }
     };
@@ -488,6 +503,21 @@ struct Collapser {
 };
 
 }  // namespace
+
+void make_float_nodes(const WideBVH &bvh, std::vector<WideNodeF> &out) {
+  out.resize(bvh.nodes.size());
+  for (size_t i = 0; i < bvh.nodes.size(); i++) {
+    const WideNode &w = bvh.nodes[i];
+    WideNodeF &f = out[i];
+    std::memset(&f, 0, sizeof(f));
+    std::memcpy(f.b, &bvh.boxes[24 * i], 24 * sizeof(float));
+    for (int c = 0; c < 4; c++) {
+      f.child[c] = w.child[c];
+      f.count[c] = w.count[c];
+    }
+    f.imask = w.imask;
+  }
+}
 
 void decode_child_box(const WideNode &n, int c, float lo[3], float hi[3]) {
   for (int a = 0; a < 3; a++) {
@@ -532,7 +562,7 @@ bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max,
   for (int pass = 0; pass < 2; pass++) {
     out.nodes.clear();
     out.nodes.push_back(WideNode());
-    Collapser c(bn, out.nodes, pass == 1);
+    Collapser c(bn, out.nodes, out.boxes, pass == 1);
     if (bn[0].right < 0) {
       // single leaf child under the root
       WideNode w;
@@ -542,6 +572,8 @@ bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max,
       w.child[0] = bn[1].first;
       w.count[0] = (uint8_t)bn[1].count;
       out.nodes[0] = w;
+      out.boxes.assign(24, 0.f);
+      set_boxes(out.boxes.data(), bn[0].box, &box, 1);
       c.max_depth = 1;
     } else {
       c.emit_all();

@@ -21,6 +21,7 @@ struct BuildPrim {
 
 struct WideBVH {
   std::vector<WideNode> nodes;   // node 0 is the root
+  std::vector<float> boxes;      // per node 24 floats: the children's exact boxes as WideNodeF::b
   std::vector<uint32_t> order;   // leaf order: record i holds input prim order[i]
   int binary_depth = 0;
   int wide_depth = 0;
@@ -32,6 +33,9 @@ struct WideBVH {
 // trav_cost: SAH cost of visiting a node, relative to one primitive test.
 bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max, WideBVH &out,
                     std::string *err, double trav_cost = 1.0);
+
+// FP32-box nodes (WideNodeF) from a built tree's topology and exact child boxes.
+void make_float_nodes(const WideBVH &bvh, std::vector<WideNodeF> &out);
 
 // Decoded child box of a quantised node, exactly as the kernels compute it.
 void decode_child_box(const WideNode &n, int child, float lo[3], float hi[3]);

@@ -724,8 +724,9 @@ __device__ void quantise(WideNode &w, const float *nlo, const float *nhi, const 
 
 __device__ __forceinline__ double node_area(const DNode &n) { return box_area(n.lo, n.hi); }
 
+// wbox: per wide node the 24 FP32 child bounds in WideNodeF::b order.
 __global__ void k_collapse(uint32_t nin, const WItem *in, const DNode *bn, int breadth_first, WideNode *wn,
-                           WItem *out, Counters *ctr) {
+                           float *wbox, WItem *out, Counters *ctr) {
   const uint32_t ii = blockIdx.x * blockDim.x + threadIdx.x;
   if (ii >= nin) return;
   const WItem it = in[ii];
@@ -791,7 +792,31 @@ __global__ void k_collapse(uint32_t nin, const WItem *in, const DNode *bn, int b
   }
   quantise(w, r.lo, r.hi, clo, chi, nk);
   wn[it.slot] = w;
+  float *fb = wbox + 24 * (size_t)it.slot;
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 4; k++) {
+      float lo = INFINITY, hi = -INFINITY;
+      if (k < nk) fnode_slab(r.lo[a], r.hi[a], clo[k][a], chi[k][a], &lo, &hi);
+      fb[(2 * a) * 4 + k] = lo;
+      fb[(2 * a + 1) * 4 + k] = hi;
+    }
   atomicMax(&ctr->wide_depth, it.depth);
+}
+
+// FP32-box nodes: the child bounds with the final child / count / imask.
+__global__ void k_make_fnodes(uint32_t nw, const WideNode *wn, const float *wbox, WideNodeF *fn) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nw) return;
+  const WideNode w = wn[i];
+  WideNodeF f;
+  for (int k = 0; k < 24; k++) f.b[k / 4][k % 4] = wbox[24 * (size_t)i + k];
+  for (int c = 0; c < 4; c++) {
+    f.child[c] = w.child[c];
+    f.count[c] = w.count[c];
+  }
+  f.imask = w.imask;
+  f.pad[0] = f.pad[1] = 0u;
+  fn[i] = f;
 }
 
 // Leaves: triangles before spheres, count = ntri | nsph << 4.
@@ -846,6 +871,7 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
   DNode *nodes = nullptr;
   WItem *wa = nullptr, *wb = nullptr;
   WideNode *wide = nullptr;
+  float *wbox = nullptr;
   Counters *ctr = nullptr;
   Counters hc{};
   const uint32_t ntmax = n / (kSmallTask + 1) + 2;  // large tasks of one level
@@ -864,7 +890,8 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
       fail("allocation", e);
       break;
     }
-    if ((e = cudaMalloc(&wide, (size_t)n * sizeof(WideNode)))) {
+    if ((e = cudaMalloc(&wide, (size_t)n * sizeof(WideNode))) ||
+        (e = cudaMalloc(&wbox, (size_t)n * 24 * sizeof(float)))) {
       fail("allocation", e);
       break;
     }
@@ -927,7 +954,7 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
       WItem *a = wa, *b = wb;
       while (nin > 0) {
         cudaMemcpyAsync(&ctr->items, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-        k_collapse<<<(nin + 127) / 128, 128, 0, st>>>(nin, a, nodes, pass, wide, b, ctr);
+        k_collapse<<<(nin + 127) / 128, 128, 0, st>>>(nin, a, nodes, pass, wide, wbox, b, ctr);
         if ((e = cudaMemcpyAsync(&hc, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st)) ||
             (e = cudaStreamSynchronize(st))) {
           fail("collapse", e);
@@ -947,10 +974,12 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
     k_leaf_kinds<<<(hc.wide + 127) / 128, 128, 0, st>>>(hc.wide, wide, idx, prims);
     // exact-size outputs
     if ((e = cudaMalloc(&out.nodes, (size_t)hc.wide * sizeof(WideNode))) ||
-        (e = cudaMemcpyAsync(out.nodes, wide, (size_t)hc.wide * sizeof(WideNode), cudaMemcpyDeviceToDevice, st))) {
+        (e = cudaMemcpyAsync(out.nodes, wide, (size_t)hc.wide * sizeof(WideNode), cudaMemcpyDeviceToDevice, st)) ||
+        (e = cudaMalloc(&out.fnodes, (size_t)hc.wide * sizeof(WideNodeF)))) {
       fail("output", e);
       break;
     }
+    k_make_fnodes<<<(hc.wide + 127) / 128, 128, 0, st>>>(hc.wide, wide, wbox, out.fnodes);
     out.order = idx;
     idx = nullptr;  // handed to the caller
     out.num_nodes = hc.wide;
@@ -981,9 +1010,11 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
   cudaFree(wa);
   cudaFree(wb);
   cudaFree(wide);
+  cudaFree(wbox);
   cudaFree(ctr);
   if (!ok) {
     cudaFree(out.nodes);
+    cudaFree(out.fnodes);
     cudaFree(out.order);
     out = DeviceBVH();
   }

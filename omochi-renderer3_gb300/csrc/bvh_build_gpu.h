@@ -1,4 +1,4 @@
-// bvh_build_gpu.h -- device build of the 4-wide quantised BVH (bvh_build_gpu.cu).
+// bvh_build_gpu.h -- device build of the 4-wide BVH (bvh_build_gpu.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,11 +10,12 @@
 
 namespace or3 {
 
-// Device-resident result: nodes[num_nodes] (root at 0) and the leaf order
-// (record r holds input primitive order[r]), both cudaMalloc'd and owned by
-// the caller.
+// Device-resident result: nodes[num_nodes] (root at 0), the same tree with
+// FP32 child boxes (fnodes) and the leaf order (record r holds input
+// primitive order[r]), all cudaMalloc'd and owned by the caller.
 struct DeviceBVH {
   WideNode *nodes = nullptr;
+  WideNodeF *fnodes = nullptr;
   uint32_t *order = nullptr;
   uint32_t num_nodes = 0;
   int binary_depth = 0;

@@ -346,9 +346,18 @@ int or3_context_create(int device, or3_context **out) {
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(OR3_ERR_CUDA);
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_extend, kernel_extend_ptr(), 256, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_shade, kernel_shade_ptr(), 256, 0);
   ctx->occ_extend = std::max(ctx->occ_extend, 1);
-  ctx->occ_shade = std::max(ctx->occ_shade, 1);
+  // the shade instances differ in registers (the light sample): a grid sized
+  // for the wrong one leaves a tail of blocks that wait for a free slot
+  for (int nee = 0; nee < 2; nee++) {
+    int o = 64;
+    for (int batch = 0; batch < 2; batch++) {
+      int ob = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, kernel_shade_ptr(batch, nee), 256, 0);
+      o = std::min(o, ob);
+    }
+    (nee ? ctx->occ_shade_nee : ctx->occ_shade) = std::max(o, 1);
+  }
   set_query_grid(ctx->num_sms * ctx->occ_extend);
   if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
@@ -543,6 +552,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       return fail(ctx, OR3_ERR_CUDA, "%s", berr.c_str());
     }
     sg->allocs.push_back(dbvh.nodes);
+    sg->allocs.push_back(dbvh.fnodes);
     tmp.p.push_back(dbvh.order);
   }
   auto t1 = std::chrono::steady_clock::now();
@@ -619,12 +629,18 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     const WideNode *nodes_dev = nullptr;
     if ((rc = dev_upload(ctx, sg, bvh.nodes, &nodes_dev))) { free_scene(sg); return rc; }
     S.nodes = reinterpret_cast<const uint4 *>(nodes_dev);
+    std::vector<WideNodeF> fnodes;
+    make_float_nodes(bvh, fnodes);
+    const WideNodeF *fnodes_dev = nullptr;
+    if ((rc = dev_upload(ctx, sg, fnodes, &fnodes_dev))) { free_scene(sg); return rc; }
+    S.fnodes = reinterpret_cast<const float4 *>(fnodes_dev);
     if ((rc = dev_upload(ctx, sg, prims, &S.prims))) { free_scene(sg); return rc; }
     if ((rc = dev_upload(ctx, sg, info, &S.info))) { free_scene(sg); return rc; }
     if ((rc = dev_upload(ctx, sg, shade, &S.tri_shade))) { free_scene(sg); return rc; }
   } else {
     S.nodes = reinterpret_cast<const uint4 *>(dbvh.nodes);
-    sg->info.device_bytes += (size_t)dbvh.num_nodes * sizeof(WideNode);
+    S.fnodes = reinterpret_cast<const float4 *>(dbvh.fnodes);
+    sg->info.device_bytes += (size_t)dbvh.num_nodes * (sizeof(WideNode) + sizeof(WideNodeF));
     // input-order records (temporary) gathered into leaf order
     float4 *geom_in = nullptr;
     PrimInfo *info_in = nullptr;
@@ -812,7 +828,6 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const Queues q = make_queues(ctx);
   const int block = 256;
   const int grid_ext = ctx->num_sms * ctx->occ_extend;
-  const int grid_sh = ctx->num_sms * ctx->occ_shade;
   const int smem_nodes =
       (prm->tuning & OR3_TUNE_SMEM_NODES) ? (int)std::min<uint64_t>(256, sg->view.num_nodes) : 0;
   const int variant = extend_variant(prm->tuning);
@@ -822,11 +837,13 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     int maxp = 0, maxw = 0;
     cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, ctx->device);
     cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device);
-    const size_t bytes = std::min<size_t>((size_t)sg->view.num_nodes * sizeof(WideNode), (size_t)maxw);
+    const bool fn = variant == 2 || variant == 4 || variant == 5;
+    const size_t bytes =
+        std::min<size_t>((size_t)sg->view.num_nodes * (fn ? sizeof(WideNodeF) : sizeof(WideNode)), (size_t)maxw);
     if (maxp > 0 && bytes > 0) {
       cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min<size_t>(bytes, (size_t)maxp));
       cudaStreamAttrValue a{};
-      a.accessPolicyWindow.base_ptr = (void *)sg->view.nodes;
+      a.accessPolicyWindow.base_ptr = fn ? (void *)sg->view.fnodes : (void *)sg->view.nodes;
       a.accessPolicyWindow.num_bytes = bytes;
       a.accessPolicyWindow.hitRatio = std::min(1.0f, (float)maxp / (float)bytes);
       a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
@@ -849,6 +866,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const bool timek = (prm->flags & OR3_FLAG_TIME_KERNELS) != 0;
   const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
   const bool shadows = prm->next_event_estimation && (sg->view.num_lights > 0 || sg->view.env_light != 0);
+  // sized for the shade instance launch_shade picks
+  const int grid_sh = ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade);
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
@@ -881,7 +900,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
           launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
-          if (shadows) launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, st);
+          if (shadows)
+            launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, st);
           if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[3], st));
           launch_reset_count(q, in, st);
           in ^= 1;
@@ -1105,7 +1125,7 @@ int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *
   std::string err;
   const int rcode = render_paths_noalloc(it->second->view, it->second->has_split, rc, first, num_paths,
                                          (uint32_t)prev, ctx->device, ctx->num_sms * ctx->occ_extend,
-                                         ctx->num_sms * ctx->occ_shade, radiance_dev,
+                                         ctx->num_sms * (rc.nee ? ctx->occ_shade_nee : ctx->occ_shade), radiance_dev,
                                          stream ? (cudaStream_t)stream : ctx->stream, &err);
   if (rcode != OR3_OK) return fail(ctx, rcode, "%s", err.c_str());
   return OR3_OK;

@@ -226,7 +226,8 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   Batch b{B.scenes, B.jobs, B.segs, B.info};
   const Queues q = make_queues(ctx);
   const int bps_ext = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, ctx->occ_extend) : ctx->occ_extend;
-  const int bps_sh = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, ctx->occ_shade) : ctx->occ_shade;
+  const int occ_sh = shadows ? ctx->occ_shade_nee : ctx->occ_shade;  // the instance launch_shade_batch picks
+  const int bps_sh = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, occ_sh) : occ_sh;
   const int grid_ext = ctx->num_sms * std::max(bps_ext, 1);
   const int grid_sh = ctx->num_sms * std::max(bps_sh, 1);
   const bool count = (bp->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;

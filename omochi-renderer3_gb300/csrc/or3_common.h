@@ -12,6 +12,7 @@
 // src/renderer/QBVH.h:45-52).
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 
 #ifdef __CUDACC__
@@ -47,6 +48,38 @@ struct alignas(64) WideNode {
   uint32_t pad;
 };
 static_assert(sizeof(WideNode) == 64, "WideNode must be 64 bytes");
+
+// Wide node with FP32 child boxes (128 bytes): b[2a] are the lower and
+// b[2a+1] the upper bounds of the 4 children on axis a (empty slots +inf /
+// -inf), so a ray picks its near and far planes by which of the two it loads;
+// child / count / imask as in WideNode.  Twice the bytes of WideNode, no
+// dequantisation in the node test.
+struct alignas(16) WideNodeF {
+  float b[6][4];
+  uint32_t child[4];
+  uint8_t count[4];
+  uint32_t imask;
+  uint32_t pad[2];
+};
+static_assert(sizeof(WideNodeF) == 128, "WideNodeF must be 128 bytes");
+
+// One child slab of a WideNodeF: the exact bound [lo, hi] widened by 2^-18
+// of the parent's extent on that axis and then two ulps, so that the
+// rounding of the slab distances cannot drop a ray that grazes a box face.
+// Host and device builds give the same bits (round-to-nearest float ops).
+OR3_HD void fnode_slab(float plo, float phi, float lo, float hi, float *olo, float *ohi) {
+#ifdef __CUDA_ARCH__
+  const float pad = __fmul_rn(__fsub_rn(phi, plo), 0x1p-18f);
+  lo = __fsub_rn(lo, pad);
+  hi = __fadd_rn(hi, pad);
+#else
+  const float pad = (phi - plo) * 0x1p-18f;
+  lo = lo - pad;
+  hi = hi + pad;
+#endif
+  *olo = nextafterf(nextafterf(lo, -INFINITY), -INFINITY);
+  *ohi = nextafterf(nextafterf(hi, INFINITY), INFINITY);
+}
 
 enum PrimKind : uint32_t { kPrimTriangle = 0, kPrimSphere = 1, kPrimPlane = 2, kPrimFloor = 3 };
 

@@ -12,6 +12,7 @@ namespace or3 {
 // Device view of one uploaded scene.
 struct DevScene {
   const uint4 *nodes;          // WideNode[num_nodes] as 4 x uint4
+  const float4 *fnodes;        // WideNodeF[num_nodes] as 8 x float4 (optional FP32-box copy)
   const float4 *prims;         // 3 x float4 per record
   const PrimInfo *info;        // per record
   const TriShade *tri_shade;   // per record (triangles)
@@ -388,13 +389,49 @@ __device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint3
 // only internal children go through the stack (stack entries are node indices).
 // SORT: visit internal children nearest first (closest hit); an any-hit
 // query may take them in slot order.
-template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack>
+// FN: test the node's FP32 child boxes (S.fnodes); false: the quantised
+// boxes (S.nodes, optionally staged in shared memory as snodes[0..ns)).
+template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true>
 __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, STK &stk,
                                                  const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
   const uint32_t e = s.entry;
   if (e == kNoEntry) return true;
-  uint4 n0, n1, n2, n3;
   if (COUNT) cnt[0]++;
+  float key[4];
+  uint32_t kid[4];
+  uint32_t leafmask = 0, counts;
+  if (FN) {
+    // near / far planes picked by the ray's direction signs through the load offset
+    const float4 *np = S.fnodes + 8 * (size_t)e;
+    const uint32_t sx = s.signs & 1u, sy = (s.signs >> 1) & 1u, sz = (s.signs >> 2) & 1u;
+    const float4 bnx = __ldg(np + sx), bfx = __ldg(np + (sx ^ 1u));
+    const float4 bny = __ldg(np + 2 + sy), bfy = __ldg(np + 3 - sy);
+    const float4 bnz = __ldg(np + 4 + sz), bfz = __ldg(np + 5 - sz);
+    const uint4 ch = __ldg(reinterpret_cast<const uint4 *>(np + 6));
+    const uint4 mt = __ldg(reinterpret_cast<const uint4 *>(np + 7));
+    counts = mt.x;
+    const uint32_t imask = mt.y;
+    const float tlimit = s.tmax * 1.0000010f;
+    const float nxa[4] = {bnx.x, bnx.y, bnx.z, bnx.w}, fxa[4] = {bfx.x, bfx.y, bfx.z, bfx.w};
+    const float nya[4] = {bny.x, bny.y, bny.z, bny.w}, fya[4] = {bfy.x, bfy.y, bfy.z, bfy.w};
+    const float nza[4] = {bnz.x, bnz.y, bnz.z, bnz.w}, fza[4] = {bfz.x, bfz.y, bfz.z, bfz.w};
+    const uint32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const float tnx = fmaf(nxa[i], s.inv.x, s.oi.x), tfx = fmaf(fxa[i], s.inv.x, s.oi.x);
+      const float tny = fmaf(nya[i], s.inv.y, s.oi.y), tfy = fmaf(fya[i], s.inv.y, s.oi.y);
+      const float tnz = fmaf(nza[i], s.inv.z, s.oi.z), tfz = fmaf(fza[i], s.inv.z, s.oi.z);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+      const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
+      const bool internal = (imask >> i) & 1u;
+      const uint32_t c = (counts >> (8 * i)) & 0xFFu;
+      const bool hitbox = tn <= tf && tn <= tlimit;
+      key[i] = (hitbox && internal) ? tn : kInf * 2.f;
+      kid[i] = cha[i];
+      if (hitbox && !internal && c != 0u) leafmask |= 1u << i;
+    }
+  } else {
+  uint4 n0, n1, n2, n3;
   if (e < ns) {
     n0 = snodes[4 * e + 0];
     n1 = snodes[4 * e + 1];
@@ -418,11 +455,8 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
   const uint32_t wnx = (s.signs & 1u) ? n1.w : n1.x, wfx = (s.signs & 1u) ? n1.x : n1.w;
   const uint32_t wny = (s.signs & 2u) ? n2.x : n1.y, wfy = (s.signs & 2u) ? n1.y : n2.x;
   const uint32_t wnz = (s.signs & 4u) ? n2.y : n1.z, wfz = (s.signs & 4u) ? n1.z : n2.y;
-  const uint32_t counts = n3.z;
+  counts = n3.z;
   const float tlimit = s.tmax * 1.0000010f;
-  float key[4];
-  uint32_t kid[4];
-  uint32_t leafmask = 0;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const float tnx = fmaf(qbyte(wnx, i), ax, bx), tfx = fmaf(qbyte(wfx, i), ax, bx);
@@ -437,11 +471,11 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
     kid[i] = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
     if (hitbox && !internal && c != 0u) leafmask |= 1u << i;
   }
+  }
   while (leafmask) {
     const uint32_t i = __ffs(leafmask) - 1;
     leafmask &= leafmask - 1;
-    const uint32_t first = i == 0 ? n2.z : i == 1 ? n2.w : i == 2 ? n3.x : n3.y;
-    trav_leaf<COUNT>(S, s, first, (counts >> (8 * i)) & 0xFFu, cnt);
+    trav_leaf<COUNT>(S, s, kid[i], (counts >> (8 * i)) & 0xFFu, cnt);
   }
   if (ANY && s.rec != kMissRec) return true;
   const float inf2 = kInf * 2.f;

@@ -37,7 +37,8 @@ struct or3_context {
   std::map<int32_t, or3::SceneGPU *> scenes;
   int32_t next_scene = 1;
   int num_sms = 0;
-  int occ_extend = 1, occ_shade = 1;
+  // resident 256-thread blocks per SM: extend; shade without / with the light sample
+  int occ_extend = 1, occ_shade = 1, occ_shade_nee = 1;
 
   // queues
   size_t cap_rays = 0, cap_paths = 0;

@@ -90,8 +90,9 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // STEP 2: one node per step with its hit leaves tested in place, refill only
 //         once at least half of the warp is idle (amortises the atomic).
 // REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
-// nearest-first child order (off only for any-hit queries).
-template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true>
+// nearest-first child order (off only for any-hit queries).  FN: STEP 2 over
+// the FP32-box nodes (else the quantised ones).
+template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, bool FN = true>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
@@ -127,7 +128,8 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
     if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
       const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                  : trav_step_inline<ANY, COUNT, SORT>(S, st, stk, snodes, ns, cnt, err);
+                                  : trav_step_inline<ANY, COUNT, SORT, LocalStack, FN>(S, st, stk, snodes, ns,
+                                                                                       cnt, err);
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;
@@ -180,9 +182,10 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 
 // Closest hit for every queued ray.  COUNT adds the nodes, triangles and
 // spheres each ray touched to stats[3..5] (the algorithmic byte count).
-// VARIANT 0: gridstride_trace; 1, 2: persistent_trace<STEP = VARIANT>.
 // VARIANT 0: gridstride_trace; 1: persistent_trace STEP 1; 2, 4, 5: STEP 2
-// refilling at 16, 8 or 24 idle lanes.
+// refilling at 16, 8 or 24 idle lanes; 6: STEP 2 over the quantised nodes.
+// 0, 1 and 6 read the quantised nodes (and may stage the top ones in shared
+// memory), 2, 4 and 5 the FP32-box nodes.
 template <bool COUNT, int VARIANT>
 __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, int in, int smem_nodes,
                                             uint4 *snodes);
@@ -209,7 +212,7 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
   } else {
     constexpr int kStep = VARIANT == 1 ? 1 : 2;
     constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
-    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill>(
+    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, true, VARIANT != 6>(
         S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
         &q.counters[2]);
   }
@@ -669,11 +672,12 @@ struct ShadowSink {
 
 // Any-hit test of every queued shadow ray (persistent, lane-refilled).
 // SORT false: children in slot order (no distance sort).
-template <bool SORT>
+// FN: FP32-box nodes (else the quantised ones).
+template <bool SORT, bool FN>
 __global__ void __launch_bounds__(256) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT>(
+  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT, FN>(
       S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir}, ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u,
       nullptr, &q.counters[2]);
 }
@@ -963,13 +967,14 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
   const int sn = smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes;
   switch ((count ? 8 : 0) | (variant & 7)) {
     case 1: k_extend<false, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 4: k_extend<false, 4><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 5: k_extend<false, 5><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, 0); break;
+    case 4: k_extend<false, 4><<<grid, block, 0, st>>>(S, q, in, 0); break;
+    case 5: k_extend<false, 5><<<grid, block, 0, st>>>(S, q, in, 0); break;
+    case 6: k_extend<false, 6><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 8: k_extend<true, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 9: k_extend<true, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 10: case 12: case 13: case 14: case 15:  // counting runs use the default traversal
-      k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, sn); break;
+      k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, 0); break;
     default: k_extend<false, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
   }
 }
@@ -986,9 +991,10 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
   k_reset_count<<<1, 1, 0, st>>>(q.counters, which);
 }
 
-void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, cudaStream_t st) {
-  if (unsorted) k_shadow<false><<<grid, 256, 0, st>>>(S, q);
-  else k_shadow<true><<<grid, 256, 0, st>>>(S, q);
+void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st) {
+  if (quantised) k_shadow<true, false><<<grid, 256, 0, st>>>(S, q);
+  else if (unsorted) k_shadow<false, true><<<grid, 256, 0, st>>>(S, q);
+  else k_shadow<true, true><<<grid, 256, 0, st>>>(S, q);
 }
 
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st) {
@@ -1037,7 +1043,10 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
 }
 
 const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }
-const void *kernel_shade_ptr() { return (const void *)k_shade<false, false>; }
+const void *kernel_shade_ptr(bool batch, bool nee) {
+  if (batch) return nee ? (const void *)k_shade<true, true> : (const void *)k_shade<true, false>;
+  return nee ? (const void *)k_shade<false, true> : (const void *)k_shade<false, false>;
+}
 
 // ---------------------------------------------------------------- batched form
 

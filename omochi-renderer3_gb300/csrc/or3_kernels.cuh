@@ -122,7 +122,7 @@ void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int ou
 // Maps OR3_TUNE_EXTEND_MASK to a kernel variant (0 = default = 2, 3 = grid-stride).
 inline int extend_variant(uint32_t tuning) {
   const uint32_t v = tuning & 0x7u;
-  return v == 0 || v >= 6 ? 2 : v == 3 ? 0 : (int)v;  // 4, 5: refill thresholds
+  return v == 0 || v == 7 ? 2 : v == 3 ? 0 : (int)v;  // 4, 5: refill thresholds; 6: quantised nodes
 }
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    int variant, cudaStream_t st);
@@ -130,7 +130,7 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
                   int grid, int block, cudaStream_t st);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
-void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, cudaStream_t st);
+void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st);
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st);
@@ -161,6 +161,6 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
 
 // kernel handles for occupancy queries
 const void *kernel_extend_ptr();
-const void *kernel_shade_ptr();
+const void *kernel_shade_ptr(bool batch, bool nee);
 
 }  // namespace or3

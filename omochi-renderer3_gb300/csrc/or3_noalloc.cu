@@ -110,7 +110,7 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
   for (int bounce = 0; count > 0 && bounce < 1 << 20; bounce++) {
     launch_extend(S, q, in, grid_ext, 256, 0, false, extend_variant(0), st);
     launch_shade(S, rc, w, q, in, grid_sh, 256, st);
-    if (shadows) launch_shadow(S, q, grid_ext, false, st);
+    if (shadows) launch_shadow(S, q, grid_ext, false, false, st);
     launch_reset_count(q, in, st);
     in ^= 1;
     uint32_t hc[3] = {0, 0, 0};

@@ -483,7 +483,7 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
   for (int k = 0; k < S->unroll; k++) {
     const int in = k & 1;
     launch_extend_batch(b, q, in, ctx->num_sms * ctx->occ_extend, false, st);
-    launch_shade_batch(b, q, in, ctx->num_sms * ctx->occ_shade, shadows, st);
+    launch_shade_batch(b, q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows, st);
     if (shadows) launch_shadow_batch(b, q, ctx->num_sms * ctx->occ_extend, st);
     launch_reset_count(q, in, st);
   }

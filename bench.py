@@ -12,9 +12,8 @@ value      camera paths / device time of the passes (CUDA events on the
            library's stream, scene resident in HBM), Mpaths/s
 e2e        the same through the C ABI from host buffers: scene upload
            (flatten + BVH build + H2D), render, frame D2H, per step
-roofline   extend (closest-hit) kernel: algorithmic bytes (128 B per wide node
-           fetched -- FP32 child boxes; 64 B for the quantised variants 1, 3, 6
-           --, 48 B per triangle record, 16 B per sphere record, counted
+roofline   extend (closest-hit) kernel: algorithmic bytes (64 B per wide node
+           visited, 48 B per triangle record, 16 B per sphere record, counted
            by an instrumented run of the same render) / its event-timed
            duration, against the measured HBM copy bandwidth
 cpu_baseline  the C oracle (FP64 restatement of the reference path, its BVH)
@@ -44,6 +43,10 @@ METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency whe
 # profiles/k_traversal_terrain_480x270.md); roofline.traffic is this times
 # the rays of an average launch.
 EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.2, "terrain": 52.0}
+# The bounding roofline of a scene that stays in L2 is the SM issue rate: the
+# share of issue slots the extend kernel used on its active cycles
+# (smsp__issue_active), first and second launch of the same captures.
+EXTEND_ISSUE_ACTIVE = {"mesh": (0.767, 0.681), "terrain": (0.750, 0.769)}
 
 
 def workload(pkg, name):
@@ -436,8 +439,9 @@ def main():
 
     # algorithmic bytes per extension ray (instrumented run, untimed)
     c = ctx.render(sid, cam, seed=99, flags=A.OR3_FLAG_COUNT_TRAVERSAL, **kw)
-    node_bytes = 64.0 if (args.tuning & 7) in (1, 3, 6) else 128.0  # quantised or FP32 child boxes
-    alg_bytes_per_ray = (node_bytes * c["nodes_visited"] + 48.0 * c["tris_tested"] + 16.0 * c["spheres_tested"]) / \
+    # the per-unit figure of a node visit is 64 B whatever the node layout (the
+    # default FP32-box nodes load 128 B, from L1/L2 on these scenes)
+    alg_bytes_per_ray = (64.0 * c["nodes_visited"] + 48.0 * c["tris_tested"] + 16.0 * c["spheres_tested"]) / \
         max(c["extension_rays"], 1)
 
     for i in range(args.warmup):
@@ -523,7 +527,8 @@ def main():
                          "traffic_unit": "bytes per launch",
                          "alg_bytes_per_launch": alg_bytes_per_ray * ext_rays / max(ext_launches, 1),
                          "alg_bytes_per_ray": alg_bytes_per_ray, "avg_launch_ms": avg_ext_ms,
-                         "launches": ext_launches},
+                         "launches": ext_launches,
+                         "sm_issue_active_ncu": EXTEND_ISSUE_ACTIVE.get(args.workload)},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,

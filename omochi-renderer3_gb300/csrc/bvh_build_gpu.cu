@@ -567,57 +567,86 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
         }
       }
       __syncwarp();
-      if (lane == 0) {
-        const double parent = box_area(lo, hi);
-        double best = DBL_MAX;
-        double rarea[kBins];
-        uint32_t rcnt[kBins];
-        for (int a = 0; a < 3; a++) {
-          if (!(chi[a] - clo[a] > 0.f)) continue;
-          float alo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, ahi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-          uint32_t cnt = 0;
-          for (int b = kBins - 1; b > 0; b--) {
-            const uint32_t *w = sh.bins + (a * kBins + b) * 7;
-            if (w[6])
-              for (int k = 0; k < 3; k++) {
-                alo[k] = fminf(alo[k], o2f(w[k]));
-                ahi[k] = fmaxf(ahi[k], o2f(w[3 + k]));
-              }
-            cnt += w[6];
-            rarea[b] = box_area(alo, ahi);
-            rcnt[b] = cnt;
-          }
-          for (int k = 0; k < 3; k++) {
-            alo[k] = FLT_MAX;
-            ahi[k] = -FLT_MAX;
-          }
-          cnt = 0;
-          for (int b = 0; b < kBins - 1; b++) {
-            const uint32_t *w = sh.bins + (a * kBins + b) * 7;
-            if (w[6])
-              for (int k = 0; k < 3; k++) {
-                alo[k] = fminf(alo[k], o2f(w[k]));
-                ahi[k] = fmaxf(ahi[k], o2f(w[3 + k]));
-              }
-            cnt += w[6];
-            if (cnt == 0 || rcnt[b + 1] == 0) continue;
-            const double cost =
-                ct + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
-            if (cost < best) {
-              best = cost;
-              axis = a;
-              bin = b;
-              nleft = cnt;
+      // SAH over the 3 x 15 split candidates, one bin per lane: prefix and
+      // suffix unions by shuffle scans (min / max are exact, so the unions and
+      // the double costs are the sequential evaluation's, bit for bit); ties
+      // go to the lowest (axis, bin) like a sequential scan with a strict <
+      const double parent = box_area(lo, hi);
+      double bestc = DBL_MAX;
+      uint32_t bidx = 0xFFFFFFFFu, bcnt = 0;
+      for (int a = 0; a < 3; a++) {
+        if (!(chi[a] - clo[a] > 0.f)) continue;
+        float plo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, phi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t pc = 0;
+        if (lane < (uint32_t)kBins) {
+          const uint32_t *w = sh.bins + (a * kBins + lane) * 7;
+          pc = w[6];
+          if (pc)
+            for (int k = 0; k < 3; k++) {
+              plo[k] = o2f(w[k]);
+              phi[k] = o2f(w[3 + k]);
             }
+        }
+        float slo[3] = {plo[0], plo[1], plo[2]}, shi[3] = {phi[0], phi[1], phi[2]};
+        uint32_t sc2 = pc;
+#pragma unroll
+        for (int o = 1; o < kBins; o <<= 1) {
+          float ulo[3], uhi[3], dlo[3], dhi[3];
+          for (int k = 0; k < 3; k++) {
+            ulo[k] = __shfl_up_sync(0xFFFFFFFFu, plo[k], o);
+            uhi[k] = __shfl_up_sync(0xFFFFFFFFu, phi[k], o);
+            dlo[k] = __shfl_down_sync(0xFFFFFFFFu, slo[k], o);
+            dhi[k] = __shfl_down_sync(0xFFFFFFFFu, shi[k], o);
+          }
+          const uint32_t uc = __shfl_up_sync(0xFFFFFFFFu, pc, o), dc = __shfl_down_sync(0xFFFFFFFFu, sc2, o);
+          if (lane >= (uint32_t)o) {
+            for (int k = 0; k < 3; k++) {
+              plo[k] = fminf(plo[k], ulo[k]);
+              phi[k] = fmaxf(phi[k], uhi[k]);
+            }
+            pc += uc;
+          }
+          if (lane + o < 32u) {
+            for (int k = 0; k < 3; k++) {
+              slo[k] = fminf(slo[k], dlo[k]);
+              shi[k] = fmaxf(shi[k], dhi[k]);
+            }
+            sc2 += dc;
           }
         }
-        if (t.count <= (uint32_t)leaf_max && (axis < 0 || (double)t.count <= best)) mode = 2;
-        else if (axis < 0) mode = 1;
+        // the right side of the split after bin `lane` is the suffix from lane + 1
+        float rlo[3], rhi[3];
+        for (int k = 0; k < 3; k++) {
+          rlo[k] = __shfl_down_sync(0xFFFFFFFFu, slo[k], 1);
+          rhi[k] = __shfl_down_sync(0xFFFFFFFFu, shi[k], 1);
+        }
+        const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc2, 1);
+        if (lane < (uint32_t)kBins - 1 && pc != 0 && rc != 0) {
+          const double cost = ct + (box_area(plo, phi) * pc + box_area(rlo, rhi) * rc) / fmax(parent, 1e-30);
+          if (cost < bestc) {
+            bestc = cost;
+            bidx = (uint32_t)(a * kBins) + lane;
+            bcnt = pc;
+          }
+        }
       }
-      mode = __shfl_sync(0xFFFFFFFFu, mode, 0);
-      axis = __shfl_sync(0xFFFFFFFFu, axis, 0);
-      bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
-      nleft = __shfl_sync(0xFFFFFFFFu, nleft, 0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double c2 = __shfl_xor_sync(0xFFFFFFFFu, bestc, o);
+        const uint32_t i2 = __shfl_xor_sync(0xFFFFFFFFu, bidx, o), n2 = __shfl_xor_sync(0xFFFFFFFFu, bcnt, o);
+        if (c2 < bestc || (c2 == bestc && i2 < bidx)) {
+          bestc = c2;
+          bidx = i2;
+          bcnt = n2;
+        }
+      }
+      if (bidx != 0xFFFFFFFFu) {
+        axis = (int)(bidx / kBins);
+        bin = (int)(bidx % kBins);
+        nleft = bcnt;
+      }
+      if (t.count <= (uint32_t)leaf_max && (axis < 0 || (double)t.count <= bestc)) mode = 2;
+      else if (axis < 0) mode = 1;
       if (axis >= 0) scale = sc[axis];
     }
     if (mode == 2) continue;

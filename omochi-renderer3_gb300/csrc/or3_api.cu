@@ -366,7 +366,6 @@ int or3_context_create(int device, or3_context **out) {
   cudaMemset(ctx->dstats, 0, 8 * sizeof(unsigned long long));
   cudaEventCreate(&ctx->ev0);
   cudaEventCreate(&ctx->ev1);
-  for (int k = 0; k < 4; k++) cudaEventCreate(&ctx->kev[k]);
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(OR3_ERR_CUDA);
   *out = ctx;
   return OR3_OK;
@@ -398,8 +397,7 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFreeHost(ctx->frame_pinned);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  for (int k = 0; k < 4; k++)
-    if (ctx->kev[k]) cudaEventDestroy(ctx->kev[k]);
+  for (cudaEvent_t e : ctx->kpool) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return OR3_OK;
@@ -681,8 +679,11 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     const uint32_t W = d->env_width, H = d->env_height;
     const size_t texels = (size_t)W * H;
     float *env_d = nullptr, *marg_d = nullptr, *cond_d = nullptr;
+    uint32_t *gmarg_d = nullptr, *gcond_d = nullptr;
     if ((rc = dev_alloc(ctx, sg, &env_d, 3 * texels)) || (rc = dev_alloc(ctx, sg, &marg_d, H)) ||
-        (rc = dev_alloc(ctx, sg, &cond_d, texels)) || (rc = tmp.alloc(ctx, &env_total, (size_t)H + 1))) {
+        (rc = dev_alloc(ctx, sg, &cond_d, texels)) || (rc = dev_alloc(ctx, sg, &gmarg_d, (size_t)H + 1)) ||
+        (rc = dev_alloc(ctx, sg, &gcond_d, (size_t)H * (W + 1))) ||
+        (rc = tmp.alloc(ctx, &env_total, (size_t)H + 1))) {
       free_scene(sg);
       return rc;
     }
@@ -700,10 +701,12 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "environment upload: %s", cudaGetErrorString(ce));
     }
-    launch_env_cdf(env_d, W, H, marg_d, cond_d, env_total, ctx->stream);
+    launch_env_cdf(env_d, W, H, marg_d, cond_d, env_total, gmarg_d, gcond_d, ctx->stream);
     S.env = env_d;
     S.env_marg = marg_d;
     S.env_cond = cond_d;
+    S.env_gmarg = gmarg_d;
+    S.env_gcond = gcond_d;
     S.env_w = W;
     S.env_h = H;
   }
@@ -867,17 +870,24 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const bool countk = (prm->flags & OR3_FLAG_COUNT_TRAVERSAL) != 0;
   const bool shadows = prm->next_event_estimation && (sg->view.num_lights > 0 || sg->view.env_light != 0);
   // sized for the shade instance launch_shade picks
-  const int grid_sh = ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade);
+  const bool nee4 = (prm->tuning & OR3_TUNE_SHADE_NEE_OCC4) != 0;
+  const int grid_sh = ctx->num_sms * (shadows && !nee4 ? ctx->occ_shade_nee : ctx->occ_shade);
+
+  // a depth bound of at most 32 enqueues every bounce of a wave at once
+  const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;
+  const int chunk = whole ? prm->max_depth : 8;
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
   ctx->last_kept_paths = (prm->flags & OR3_FLAG_KEEP_PATHS) != 0;
+  std::memset(ctx->host_counters, 0, 16 * sizeof(uint32_t));  // no stale error bits from an earlier render
   auto wall0 = std::chrono::steady_clock::now();
   int32_t prev = 0;
   int passes = 0;
   bool stopped = false;
   for (int32_t next = prm->min_samples; next <= prm->max_samples; next += prm->step_samples) {
     if (ctx->stop.load()) { stopped = true; break; }
+    size_t kused = 0;  // timing events used in this pass
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
     // waves over [prev, next) samples
     for (uint32_t s = (uint32_t)prev; s < (uint32_t)next && !stopped;) {
@@ -892,39 +902,43 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         w.npix = (uint32_t)np;
         w.ns = ns;
         launch_raygen(rcst, w, q, 0, 0, block, st);
+        // Bounces are enqueued in chunks without a host round trip: every
+        // kernel reads its queue length on the device, so a bounce after the
+        // last ray is a few empty launches.  With a depth bound the chunk is
+        // the whole path (no read-back at all); without one, the live count
+        // is read after each chunk of 8 (or the bound is above 32).
         int in = 0;
-        uint32_t count = w.num_paths;
-        for (int bounce = 0; count > 0; bounce++) {
-          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[0], st));
-          launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
-          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[1], st));
-          launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st);
-          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[2], st));
-          if (shadows)
-            launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, st);
-          if (timek) OR3_CUDA(ctx, cudaEventRecord(ctx->kev[3], st));
-          launch_reset_count(q, in, st);
-          in ^= 1;
+        for (int chunks = 0;; chunks++) {
+          for (int b = 0; b < chunk; b++) {
+            cudaEvent_t e4[4] = {};
+            if (timek) {
+              while (ctx->kpool.size() < kused + 4) {
+                cudaEvent_t e;
+                OR3_CUDA(ctx, cudaEventCreate(&e));
+                ctx->kpool.push_back(e);
+              }
+              for (int k = 0; k < 4; k++) e4[k] = ctx->kpool[kused + k];
+              kused += 4;
+            }
+            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[0], st));
+            launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
+            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[1], st));
+            launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st, nee4);
+            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
+            if (shadows)
+              launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, st);
+            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
+            launch_reset_count(q, in, st);
+            in ^= 1;
+            stats.extend_launches++;
+            stats.shade_launches++;
+            if (shadows) stats.shadow_launches++;
+          }
+          if (whole) break;
           OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t),
                                         cudaMemcpyDeviceToHost, st));
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
-          count = ctx->host_counters[in];
-          if (timek) {
-            float e = 0.f, s2 = 0.f, s3 = 0.f;
-            cudaEventElapsedTime(&e, ctx->kev[0], ctx->kev[1]);
-            cudaEventElapsedTime(&s2, ctx->kev[1], ctx->kev[2]);
-            cudaEventElapsedTime(&s3, ctx->kev[2], ctx->kev[3]);
-            stats.extend_ms += e;
-            stats.shade_ms += s2;
-            stats.extend_launches++;
-            stats.shade_launches++;
-            if (shadows) {
-              stats.shadow_ms += s3;
-              stats.shadow_launches++;
-            }
-          }
-          if (ctx->host_counters[2]) break;
-          if (bounce > 100000) break;
+          if (ctx->host_counters[in] == 0 || ctx->host_counters[2] || chunks > 100000) break;
         }
         launch_accumulate(q, w, ss2, ctx->pix_sum, ctx->pix_sumsq,
                           (int)std::min<uint64_t>((np + 7) / 8, 152 * 64), block, st);
@@ -937,8 +951,20 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       if (ctx->host_counters[2]) break;
       if (ctx->stop.load() && s < (uint32_t)next) stopped = true;
     }
+    // error bits of the pass (queue capacity, traversal stack)
+    OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                  st));
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
     OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    for (size_t k = 0; k + 3 < kused; k += 4) {
+      float e = 0.f, s2 = 0.f, s3 = 0.f;
+      cudaEventElapsedTime(&e, ctx->kpool[k], ctx->kpool[k + 1]);
+      cudaEventElapsedTime(&s2, ctx->kpool[k + 1], ctx->kpool[k + 2]);
+      cudaEventElapsedTime(&s3, ctx->kpool[k + 2], ctx->kpool[k + 3]);
+      stats.extend_ms += e;
+      stats.shade_ms += s2;
+      if (shadows) stats.shadow_ms += s3;
+    }
     if (ctx->host_counters[2]) {
       const uint32_t bits = ctx->host_counters[2];
       cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);

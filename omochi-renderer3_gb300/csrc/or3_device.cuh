@@ -28,6 +28,8 @@ struct DevScene {
   const float *light_pdf;      // [num_lights] selection probability among local lights
   const float *env_marg;       // [env_h] inclusive marginal CDF over rows
   const float *env_cond;       // [env_h * env_w] inclusive conditional CDF per row
+  const uint32_t *env_gmarg;   // [env_h + 1] guide table of env_marg
+  const uint32_t *env_gcond;   // [env_h * (env_w + 1)] guide table of each env_cond row
   uint32_t num_nodes, num_prims, num_planes, num_lights;
   uint32_t env_w, env_h, num_textures;
   int32_t env_light;           // 0 none, 1 equirect map (CDF), 2 constant background
@@ -424,11 +426,10 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
       const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
       const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
       const bool internal = (imask >> i) & 1u;
-      const uint32_t c = (counts >> (8 * i)) & 0xFFu;
-      const bool hitbox = tn <= tf && tn <= tlimit;
+      const bool hitbox = tn <= tf && tn <= tlimit;  // never for an empty slot (+inf / -inf planes)
       key[i] = (hitbox && internal) ? tn : kInf * 2.f;
       kid[i] = cha[i];
-      if (hitbox && !internal && c != 0u) leafmask |= 1u << i;
+      if (hitbox && !internal) leafmask |= 1u << i;
     }
   } else {
   uint4 n0, n1, n2, n3;

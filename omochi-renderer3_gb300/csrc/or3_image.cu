@@ -180,6 +180,23 @@ __global__ void __launch_bounds__(1024) k_env_marg(uint32_t H, double *rows, flo
   if (threadIdx.x == 0) rows[H] = total;
 }
 
+// Guide tables of the CDFs above: thread k of row r stores the first index
+// whose CDF value exceeds k / n (n - 1 if none), k = 0..n; one block per row.
+__global__ void __launch_bounds__(256) k_env_guide(const float *cdf, uint32_t n, uint32_t *guide) {
+  const float *c = cdf + (size_t)blockIdx.x * n;
+  uint32_t *g = guide + (size_t)blockIdx.x * (n + 1);
+  for (uint32_t k = threadIdx.x; k <= n; k += blockDim.x) {
+    const float t = (float)k / (float)n;
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (c[mid] > t) hi = mid;
+      else lo = mid + 1;
+    }
+    g[k] = lo;
+  }
+}
+
 }  // namespace
 
 int ensure_gamma_table(int device) {
@@ -206,9 +223,11 @@ void launch_decode_rgbe(const uint8_t *in, size_t npix, float *out, cudaStream_t
 }
 
 void launch_env_cdf(const float *env, uint32_t W, uint32_t H, float *marg, float *cond, double *rows,
-                    cudaStream_t st) {
+                    uint32_t *gmarg, uint32_t *gcond, cudaStream_t st) {
   k_env_rows<<<H, 256, 0, st>>>(env, W, H, cond, rows);
   k_env_marg<<<1, 1024, 0, st>>>(H, rows, marg);
+  k_env_guide<<<H, 256, 0, st>>>(cond, W, gcond);
+  k_env_guide<<<1, 256, 0, st>>>(marg, H, gmarg);
 }
 
 }  // namespace or3

@@ -66,7 +66,9 @@ struct or3_context {
   uint64_t last_wave_paths = 0;
   bool last_kept_paths = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t kev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // per-kernel timing events of one pass (4 per bounce: before extend, shade,
+  // shadow and after), created on first use and kept for later renders
+  std::vector<cudaEvent_t> kpool;
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

@@ -191,7 +191,7 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
                                             uint4 *snodes);
 
 template <bool COUNT, int VARIANT>
-__global__ void __launch_bounds__(256) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
+__global__ void __launch_bounds__(256, 4) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
   __shared__ uint4 snodes[kSmemNodes * 4];
   extend_body<COUNT, VARIANT>(S, q, in, smem_nodes, snodes);
 }
@@ -266,6 +266,23 @@ __device__ __forceinline__ uint32_t cdf_find(const float *cdf, uint32_t n, float
   return lo;
 }
 
+// cdf_find through a guide table (the cutpoint method of Chen and Asau,
+// 1974): guide[k] is the first index whose CDF value exceeds k / n (n - 1
+// if none), k = 0..n.  u in cell k = floor(u n) has its answer between
+// guide[k - 1] and guide[k + 2]: the one-cell margins cover the rounding of
+// u n and of k / n, so the result is cdf_find's, in a few steps instead of
+// log2(n).
+__device__ __forceinline__ uint32_t cdf_find_guided(const float *cdf, const uint32_t *guide, uint32_t n, float u) {
+  const uint32_t k = min((uint32_t)(u * (float)n), n - 1u);
+  uint32_t lo = __ldg(guide + (k ? k - 1u : 0u)), hi = __ldg(guide + min(k + 2u, n));
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(cdf + mid) > u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
 // BRDF times colour of the vertex: Lambert rho/pi, or the Phong lobe
 // rho (n+2)/(2 pi) cos^n about the mirror direction.
 struct Brdf {
@@ -298,10 +315,10 @@ __device__ __forceinline__ bool sample_light(const DevScene &S, uint4 rl, V3 x, 
     float pdf;
     if (S.env_light == 1) {
       const uint32_t W = S.env_w, H = S.env_h;
-      const uint32_t i = cdf_find(S.env_marg, H, u1);
+      const uint32_t i = cdf_find_guided(S.env_marg, S.env_gmarg, H, u1);
       const float prev = i ? __ldg(S.env_marg + i - 1) : 0.f, pr = __ldg(S.env_marg + i) - prev;
       const float *row = S.env_cond + (size_t)i * W;
-      const uint32_t j = cdf_find(row, W, u2);
+      const uint32_t j = cdf_find_guided(row, S.env_gcond + (size_t)i * (W + 1), W, u2);
       const float prevc = j ? __ldg(row + j - 1) : 0.f, pc = __ldg(row + j) - prevc;
       const float u = ((float)j + (u2 - prevc) / pc) / (float)W;
       const float v = ((float)i + (u1 - prev) / pr) / (float)H;
@@ -573,8 +590,8 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
 
 // BATCH: the ray's segment (beta.w) selects the job's scene, constants and
 // RNG numbering; continuation rays inherit it.
-template <bool BATCH, bool NEE>
-__global__ void __launch_bounds__(256, NEE ? 3 : 4) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in,
+template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4>
+__global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in,
                                                             Batch b) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   const int out = in ^ 1;
@@ -674,7 +691,7 @@ struct ShadowSink {
 // SORT false: children in slot order (no distance sort).
 // FN: FP32-box nodes (else the quantised ones).
 template <bool SORT, bool FN>
-__global__ void __launch_bounds__(256) k_shadow(DevScene S, Queues q) {
+__global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
   persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT, FN>(
@@ -980,8 +997,10 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
 }
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
-                  int grid, int block, cudaStream_t st) {
-  if (rc.nee && (S.num_lights > 0 || S.env_light != 0))
+                  int grid, int block, cudaStream_t st, bool nee4) {
+  if (rc.nee && (S.num_lights > 0 || S.env_light != 0) && nee4)
+    k_shade<false, true, 4><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+  else if (rc.nee && (S.num_lights > 0 || S.env_light != 0))
     k_shade<false, true><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
   else
     k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});

@@ -126,8 +126,9 @@ inline int extend_variant(uint32_t tuning) {
 }
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    int variant, cudaStream_t st);
+// nee4: the light-sampling instance limited to 64 registers (4 blocks per SM)
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
-                  int grid, int block, cudaStream_t st);
+                  int grid, int block, cudaStream_t st, bool nee4 = false);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);
@@ -150,9 +151,10 @@ int ensure_gamma_table(int device);  // per device, before launch_encode_rgb8 wi
 void launch_encode_rgb8(const double *in, size_t nvals, int gamma, uint8_t *out, cudaStream_t st);
 void launch_encode_rgbe(const double *in, size_t npix, uint8_t *out, cudaStream_t st);
 void launch_decode_rgbe(const uint8_t *in, size_t npix, float *out, cudaStream_t st);
-// rows: H + 1 doubles of scratch; rows[H] receives the map's total weight
+// rows: H + 1 doubles of scratch; rows[H] receives the map's total weight.
+// gmarg [H + 1] and gcond [H * (W + 1)]: guide tables of marg and of each cond row.
 void launch_env_cdf(const float *env, uint32_t W, uint32_t H, float *marg, float *cond, double *rows,
-                    cudaStream_t st);
+                    uint32_t *gmarg, uint32_t *gcond, cudaStream_t st);
 
 // or3_noalloc.cu: the bounce loop on the static scratch array
 int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &rc, uint64_t first,

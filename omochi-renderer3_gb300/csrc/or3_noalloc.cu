@@ -107,12 +107,18 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
   int in = 0;
   uint32_t count = num_paths, errbits = 0;
   const bool shadows = rc.nee && (S.num_lights > 0 || S.env_light != 0);
-  for (int bounce = 0; count > 0 && bounce < 1 << 20; bounce++) {
-    launch_extend(S, q, in, grid_ext, 256, 0, false, extend_variant(0), st);
-    launch_shade(S, rc, w, q, in, grid_sh, 256, st);
-    if (shadows) launch_shadow(S, q, grid_ext, false, false, st);
-    launch_reset_count(q, in, st);
-    in ^= 1;
+  // bounces in chunks without a host round trip (kernels read their queue
+  // length on the device): the whole path under a depth bound of at most 32
+  const bool whole = rc.max_depth > 0 && rc.max_depth <= 32;
+  const int chunk = whole ? rc.max_depth : 8;
+  for (int chunks = 0; count > 0 && chunks < 1 << 20; chunks++) {
+    for (int b = 0; b < chunk; b++) {
+      launch_extend(S, q, in, grid_ext, 256, 0, false, extend_variant(0), st);
+      launch_shade(S, rc, w, q, in, grid_sh, 256, st);
+      if (shadows) launch_shadow(S, q, grid_ext, false, false, st);
+      launch_reset_count(q, in, st);
+      in ^= 1;
+    }
     uint32_t hc[3] = {0, 0, 0};
     e = cudaMemcpyAsync(hc, sc->counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -120,7 +126,7 @@ int render_paths_noalloc(const DevScene &S, bool has_split, const RenderConst &r
       *err = std::string("no-alloc bounce: ") + cudaGetErrorString(e);
       return OR3_ERR_CUDA;
     }
-    count = hc[in];
+    count = whole ? 0u : hc[in];
     errbits = hc[2];
     if (errbits) break;
   }

@@ -1,4 +1,4 @@
-"""Every traversal variant behind or3_render_params.tuning renders the same paths.
+"""Every kernel variant behind or3_render_params.tuning renders the same paths.
 
 The closest hit of a ray does not depend on the tree's box format (FP32
 child boxes by default, 8-bit quantised ones for variants 1, 3 and 6), on
@@ -21,6 +21,7 @@ VARIANTS = {
     "step2_quantised_smem": 6 | 0x10,
     "shadow_unsorted": 0x20,
     "l2_window": 0x40,
+    "shade_nee_4_blocks": 0x80,
 }
 
 

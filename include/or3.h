@@ -224,10 +224,11 @@ typedef struct or3_scene_info {
   uint64_t num_primitives;
   uint64_t num_nodes;      /* wide nodes */
   uint64_t device_bytes;
-  double build_ms;         /* host BVH build */
-  double upload_ms;        /* H2D copies */
+  double build_ms;         /* flattening + BVH build (host or device) */
+  double upload_ms;        /* records, materials, environment, lights to the device */
   int32_t tree_depth;
   int32_t num_lights;      /* next-event lights: in-BVH objects with an emissive layer */
+  double flatten_ms;       /* the part of build_ms spent flattening the primitives (host threads) */
 } or3_scene_info;
 
 typedef struct or3_context or3_context;

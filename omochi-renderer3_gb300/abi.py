@@ -93,7 +93,7 @@ class RenderStatsC(ctypes.Structure):
 class SceneInfoC(ctypes.Structure):
     _fields_ = [("num_primitives", ctypes.c_uint64), ("num_nodes", ctypes.c_uint64),
                 ("device_bytes", ctypes.c_uint64), ("build_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
-                ("tree_depth", ctypes.c_int32), ("num_lights", ctypes.c_int32)]
+                ("tree_depth", ctypes.c_int32), ("num_lights", ctypes.c_int32), ("flatten_ms", ctypes.c_double)]
 
 
 FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, f64p, ctypes.c_size_t, ctypes.c_size_t,

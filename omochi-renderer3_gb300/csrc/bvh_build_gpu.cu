@@ -869,13 +869,32 @@ __global__ void k_leaf_kinds(uint32_t nw, WideNode *wn, uint32_t *order, const B
   }
 }
 
+// Temporaries: stream-ordered from `pool` when given (no device-wide sync
+// on free), else cudaMalloc / cudaFree.
+struct TempAlloc {
+  cudaMemPool_t pool;
+  cudaStream_t st;
+  template <class T>
+  cudaError_t get(T **p, size_t n) const {
+    *p = nullptr;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    if (pool) return cudaMallocFromPoolAsync(reinterpret_cast<void **>(p), bytes, pool, st);
+    return cudaMalloc(p, bytes);
+  }
+  void put(void *p) const {
+    if (!p) return;
+    if (pool) cudaFreeAsync(p, st);
+    else cudaFree(p);
+  }
+};
+
 template <class T>
-cudaError_t grow(T **p, size_t &cap, size_t n) {
+cudaError_t grow(const TempAlloc &ta, T **p, size_t &cap, size_t n) {
   if (n <= cap) return cudaSuccess;
-  cudaFree(*p);
+  ta.put(*p);
   *p = nullptr;
   cap = 0;
-  const cudaError_t e = cudaMalloc(p, std::max<size_t>(n, 1) * sizeof(T));
+  const cudaError_t e = ta.get(p, n);
   if (e == cudaSuccess) cap = n;
   return e;
 }
@@ -883,8 +902,9 @@ cudaError_t grow(T **p, size_t &cap, size_t n) {
 }  // namespace
 
 bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cudaStream_t st, DeviceBVH &out,
-                           std::string *err, double trav_cost) {
+                           std::string *err, double trav_cost, cudaMemPool_t pool) {
   out = DeviceBVH();
+  const TempAlloc ta{pool, st};
   auto fail = [&](const char *what, cudaError_t e) {
     if (err) *err = std::string("device BVH build: ") + what + ": " + cudaGetErrorString(e);
     return false;
@@ -910,17 +930,17 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
   do {
     size_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0, c7 = 0, c8 = 0, c9 = 0, c10 = 0, c11 = 0,
            c12 = 0, c13 = 0, c14 = 0, c15 = 0, c16 = 0;
-    if ((e = grow(&idx, c0, n)) || (e = grow(&idx2, c1, n)) || (e = grow(&pt, c2, n)) || (e = grow(&pt2, c3, n)) ||
-        (e = grow(&flags, c4, n)) || (e = grow(&scan, c5, n)) || (e = grow(&sums, c6, nsb)) ||
-        (e = grow(&tbox, c7, 12 * (size_t)ntmax)) || (e = grow(&bins, c8, (size_t)kBinWords * ntmax)) ||
-        (e = grow(&tasks, c9, ntmax)) || (e = grow(&next, c10, ntmax)) || (e = grow(&small, c11, n)) ||
-        (e = grow(&dec, c12, ntmax)) || (e = grow(&nodes, c13, 2 * (size_t)n)) || (e = grow(&wa, c14, n)) ||
-        (e = grow(&wb, c15, n)) || (e = grow(&ctr, c16, 1))) {
+    if ((e = grow(ta, &idx, c0, n)) || (e = grow(ta, &idx2, c1, n)) || (e = grow(ta, &pt, c2, n)) ||
+        (e = grow(ta, &pt2, c3, n)) || (e = grow(ta, &flags, c4, n)) || (e = grow(ta, &scan, c5, n)) ||
+        (e = grow(ta, &sums, c6, nsb)) || (e = grow(ta, &tbox, c7, 12 * (size_t)ntmax)) ||
+        (e = grow(ta, &bins, c8, (size_t)kBinWords * ntmax)) || (e = grow(ta, &tasks, c9, ntmax)) ||
+        (e = grow(ta, &next, c10, ntmax)) || (e = grow(ta, &small, c11, n)) || (e = grow(ta, &dec, c12, ntmax)) ||
+        (e = grow(ta, &nodes, c13, 2 * (size_t)n)) || (e = grow(ta, &wa, c14, n)) || (e = grow(ta, &wb, c15, n)) ||
+        (e = grow(ta, &ctr, c16, 1))) {
       fail("allocation", e);
       break;
     }
-    if ((e = cudaMalloc(&wide, (size_t)n * sizeof(WideNode))) ||
-        (e = cudaMalloc(&wbox, (size_t)n * 24 * sizeof(float)))) {
+    if ((e = ta.get(&wide, (size_t)n)) || (e = ta.get(&wbox, (size_t)n * 24))) {
       fail("allocation", e);
       break;
     }
@@ -1022,29 +1042,14 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
     ok = true;
   } while (false);
   cudaStreamSynchronize(st);
-  cudaFree(idx);
-  cudaFree(idx2);
-  cudaFree(pt);
-  cudaFree(pt2);
-  cudaFree(flags);
-  cudaFree(scan);
-  cudaFree(sums);
-  cudaFree(tbox);
-  cudaFree(bins);
-  cudaFree(tasks);
-  cudaFree(next);
-  cudaFree(small);
-  cudaFree(dec);
-  cudaFree(nodes);
-  cudaFree(wa);
-  cudaFree(wb);
-  cudaFree(wide);
-  cudaFree(wbox);
-  cudaFree(ctr);
+  for (void *p : {(void *)idx, (void *)idx2, (void *)pt, (void *)pt2, (void *)flags, (void *)scan, (void *)sums,
+                  (void *)tbox, (void *)bins, (void *)tasks, (void *)next, (void *)small, (void *)dec,
+                  (void *)nodes, (void *)wa, (void *)wb, (void *)wide, (void *)wbox, (void *)ctr})
+    ta.put(p);
   if (!ok) {
     cudaFree(out.nodes);
     cudaFree(out.fnodes);
-    cudaFree(out.order);
+    ta.put(out.order);
     out = DeviceBVH();
   }
   return ok;

@@ -24,9 +24,11 @@ struct DeviceBVH {
 };
 
 // prims: device array of n primitive bounds (input order).  Blocks on `st`.
-// Returns false (with *err) on invalid input or a CUDA error.
+// Returns false (with *err) on invalid input or a CUDA error.  pool: where
+// the temporaries (and out.order) come from, stream-ordered on `st`; null =
+// cudaMalloc (then out.order is freed with cudaFree).
 bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cudaStream_t st, DeviceBVH &out,
-                           std::string *err, double trav_cost = 1.0);
+                           std::string *err, double trav_cost = 1.0, cudaMemPool_t pool = nullptr);
 
 // Records, PrimInfo and TriShade from input order into leaf order.
 void gather_leaf_order(uint32_t n, const uint32_t *order, const float4 *prims_in, const PrimInfo *info_in,

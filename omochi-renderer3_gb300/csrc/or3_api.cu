@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -49,19 +50,23 @@ int dev_alloc(or3_context *ctx, SceneGPU *sg, T **out, size_t n) {
 }
 
 // Device buffers that live only during one upload.
+// Temporaries of one upload, stream-ordered from the context's pool (freed
+// on the stream when the upload returns).
 struct DeviceTemps {
+  or3_context *ctx = nullptr;
   std::vector<void *> p;
+  explicit DeviceTemps(or3_context *c) : ctx(c) {}
   template <class T>
-  int alloc(or3_context *ctx, T **out, size_t n) {
+  int alloc(or3_context *c, T **out, size_t n) {
     *out = nullptr;
     void *q = nullptr;
-    OR3_CUDA(ctx, cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    OR3_CUDA(c, cudaMallocFromPoolAsync(&q, std::max<size_t>(n, 1) * sizeof(T), c->tmp_pool, c->stream));
     p.push_back(q);
     *out = static_cast<T *>(q);
     return OR3_OK;
   }
   ~DeviceTemps() {
-    for (void *q : p) cudaFree(q);
+    for (void *q : p) cudaFreeAsync(q, ctx->stream);
   }
 };
 
@@ -126,7 +131,7 @@ struct LightTables {
   float env_prob = 0.f;
 };
 
-void build_light_tables(const or3_scene_desc *d, const std::vector<float> &geom, LightTables &T) {
+void build_light_tables(const or3_scene_desc *d, const float *geom, LightTables &T) {
   const uint32_t nt = d->num_triangles, nsph = d->num_spheres;
   std::vector<double> power;
   double total = 0;
@@ -235,12 +240,9 @@ int ensure_pixels(or3_context *ctx, size_t pixels, size_t frame_doubles) {
   }
   if (frame_doubles > ctx->cap_frame) {
     cudaFree(ctx->frame_dev);
-    cudaFreeHost(ctx->frame_pinned);
     ctx->frame_dev = nullptr;
-    ctx->frame_pinned = nullptr;
     ctx->cap_frame = 0;
     OR3_CUDA(ctx, cudaMalloc(&ctx->frame_dev, frame_doubles * sizeof(double)));
-    OR3_CUDA(ctx, cudaMallocHost(&ctx->frame_pinned, frame_doubles * sizeof(double)));
     ctx->cap_frame = frame_doubles;
   }
   return OR3_OK;
@@ -359,6 +361,15 @@ int or3_context_create(int device, or3_context **out) {
     (nee ? ctx->occ_shade_nee : ctx->occ_shade) = std::max(o, 1);
   }
   set_query_grid(ctx->num_sms * ctx->occ_extend);
+  {
+    cudaMemPoolProps pp{};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = device;
+    if (cudaMemPoolCreate(&ctx->tmp_pool, &pp) != cudaSuccess) return bail(OR3_ERR_CUDA);
+    uint64_t keep = uint64_t(1) << 30;
+    cudaMemPoolSetAttribute(ctx->tmp_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMallocHost(&ctx->host_counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
@@ -395,13 +406,109 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFree(ctx->pix_sumsq);
   cudaFree(ctx->frame_dev);
   cudaFreeHost(ctx->frame_pinned);
+  cudaFreeHost(ctx->frame_front);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->kpool) cudaEventDestroy(e);
+  if (ctx->stage) cudaFreeHost(ctx->stage);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->tmp_pool) cudaMemPoolDestroy(ctx->tmp_pool);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return OR3_OK;
 }
+
+namespace {
+
+// Flattened in-BVH primitives in input order (triangles, then spheres):
+// the kernels' FP32 geometry (12 floats), build bounds, PrimInfo, TriShade.
+struct FlatPrims {
+  float *geom = nullptr;
+  BuildPrim *bp = nullptr;
+  PrimInfo *info = nullptr;
+  TriShade *shade = nullptr;
+  std::vector<float> vgeom;  // storage unless the context's pinned staging holds them
+  std::vector<BuildPrim> vbp;
+  std::vector<PrimInfo> vinfo;
+  std::vector<TriShade> vshade;
+};
+
+constexpr size_t kFlatBytes = 12 * sizeof(float) + sizeof(BuildPrim) + sizeof(PrimInfo) + sizeof(TriShade);
+constexpr size_t kStageMax = size_t(4) << 30;  // larger scenes flatten into pageable memory
+
+// Primitives [i0, i1) of the flattening.  Returns the first index whose
+// layers (or sphere radius) are invalid, or i1; *bad_bounds is set when a
+// finished primitive has an invalid or non-finite box.
+uint32_t flatten_range(const or3_scene_desc *d, uint32_t i0, uint32_t i1, FlatPrims &f, bool *bad_bounds) {
+  const uint32_t nt = d->num_triangles;
+  for (uint32_t i = i0; i < i1; i++) {
+    const bool tri = i < nt;
+    const uint32_t j = tri ? i : i - nt;
+    const uint32_t *lay = tri ? d->tri_layers + 2 * (size_t)i : d->sphere_layers + 2 * (size_t)j;
+    if (lay[1] == 0 || (uint64_t)lay[0] + lay[1] > d->num_layers) return i;
+    if (!tri && !(d->spheres[4 * (size_t)j + 3] > 0)) return i;
+    float *g = f.geom + 12 * (size_t)i;
+    BuildPrim &b = f.bp[i];
+    TriShade &ts = f.shade[i];
+    std::memset(g, 0, 12 * sizeof(float));
+    std::memset(&ts, 0, sizeof(ts));
+    if (tri) {
+      const double *v = d->tri_vertices + 9 * (size_t)i;
+      for (int a = 0; a < 3; a++) {
+        g[a] = (float)v[a];                   // v0
+        g[3 + a] = (float)(v[3 + a] - v[a]);  // e1 = p1 - p0
+        g[6 + a] = (float)(v[6 + a] - v[a]);  // e2 = p2 - p0
+      }
+      for (int a = 0; a < 3; a++) {
+        const double p0 = g[a], p1 = (double)g[a] + g[3 + a], p2 = (double)g[a] + g[6 + a];
+        b.lo[a] = down(std::min(p0, std::min(p1, p2)));
+        b.hi[a] = up(std::max(p0, std::max(p1, p2)));
+      }
+      b.kind = kPrimTriangle;
+      f.info[i] = PrimInfo{d->tri_ids ? d->tri_ids[i] : i, lay[0], lay[1], kPrimTriangle | (layer_flags(d, lay) << 8)};
+      double n0[3], n1[3], n2[3];
+      if (d->tri_normals) {
+        const double *n = d->tri_normals + 9 * (size_t)i;
+        for (int a = 0; a < 3; a++) { n0[a] = n[a]; n1[a] = n[3 + a]; n2[a] = n[6 + a]; }
+      } else {
+        const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+        const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+        double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        for (int a = 0; a < 3; a++) n0[a] = n1[a] = n2[a] = l > 0 ? c[a] / l : 0.0;
+      }
+      for (int a = 0; a < 3; a++) {
+        ts.n0[a] = (float)n0[a];
+        ts.dn1[a] = (float)(n1[a] - n0[a]);
+        ts.dn2[a] = (float)(n2[a] - n0[a]);
+      }
+      if (d->tri_uvs) {
+        const double *u = d->tri_uvs + 6 * (size_t)i;
+        for (int a = 0; a < 2; a++) {
+          ts.uv0[a] = (float)u[a];
+          ts.duv1[a] = (float)(u[2 + a] - u[a]);
+          ts.duv2[a] = (float)(u[4 + a] - u[a]);
+        }
+      }
+    } else {
+      const double *sp = d->spheres + 4 * (size_t)j;
+      g[0] = (float)sp[0]; g[1] = (float)sp[1]; g[2] = (float)sp[2]; g[3] = (float)sp[3];
+      for (int a = 0; a < 3; a++) {
+        b.lo[a] = down((double)g[a] - (double)g[3]);
+        b.hi[a] = up((double)g[a] + (double)g[3]);
+      }
+      b.kind = kPrimSphere;
+      uint32_t fl = layer_flags(d, lay);
+      if (d->sphere_flags && (d->sphere_flags[j] & OR3_SPHERE_LIGHT)) fl |= kFlagSphereLight;
+      f.info[i] = PrimInfo{d->sphere_ids ? d->sphere_ids[j] : nt + j, lay[0], lay[1], kPrimSphere | (fl << 8)};
+    }
+    for (int a = 0; a < 3; a++)
+      if (!(b.lo[a] <= b.hi[a]) || !std::isfinite(b.lo[a]) || !std::isfinite(b.hi[a])) *bad_bounds = true;
+  }
+  return i1;
+}
+
+}  // namespace
 
 int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_out) {
   if (!ctx || !d || !scene_out) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
@@ -438,74 +545,76 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   SceneGPU *sg = new SceneGPU();
   const uint32_t nt = d->num_triangles, nsph = d->num_spheres, np = nt + nsph;
 
-  // ---- primitives and their bounds (in the FP32 geometry the kernels test)
-  std::vector<float> geom(12 * (size_t)np, 0.f);
-  std::vector<BuildPrim> bp(np);
-  std::vector<PrimInfo> pinfo(np);
-  std::vector<TriShade> tshade(np);
-  for (uint32_t i = 0; i < nt; i++) {
-    int rc = check_layers(ctx, d, d->tri_layers + 2 * i, "triangle", i);
-    if (rc) { free_scene(sg); return rc; }
-    const double *v = d->tri_vertices + 9 * (size_t)i;
-    float *g = &geom[12 * (size_t)i];
-    for (int a = 0; a < 3; a++) {
-      g[a] = (float)v[a];                 // v0
-      g[3 + a] = (float)(v[3 + a] - v[a]);  // e1 = p1 - p0
-      g[6 + a] = (float)(v[6 + a] - v[a]);  // e2 = p2 - p0
-    }
-    for (int a = 0; a < 3; a++) {
-      const double p0 = g[a], p1 = (double)g[a] + g[3 + a], p2 = (double)g[a] + g[6 + a];
-      bp[i].lo[a] = down(std::min(p0, std::min(p1, p2)));
-      bp[i].hi[a] = up(std::max(p0, std::max(p1, p2)));
-    }
-    bp[i].kind = kPrimTriangle;
-    const uint32_t *lay = d->tri_layers + 2 * i;
-    pinfo[i] = PrimInfo{d->tri_ids ? d->tri_ids[i] : i, lay[0], lay[1], kPrimTriangle | (layer_flags(d, lay) << 8)};
-    TriShade &ts = tshade[i];
-    std::memset(&ts, 0, sizeof(ts));
-    double n0[3], n1[3], n2[3];
-    if (d->tri_normals) {
-      const double *n = d->tri_normals + 9 * (size_t)i;
-      for (int a = 0; a < 3; a++) { n0[a] = n[a]; n1[a] = n[3 + a]; n2[a] = n[6 + a]; }
-    } else {
-      const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
-      const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
-      double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-      const double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-      for (int a = 0; a < 3; a++) n0[a] = n1[a] = n2[a] = l > 0 ? c[a] / l : 0.0;
-    }
-    for (int a = 0; a < 3; a++) {
-      ts.n0[a] = (float)n0[a];
-      ts.dn1[a] = (float)(n1[a] - n0[a]);
-      ts.dn2[a] = (float)(n2[a] - n0[a]);
-    }
-    if (d->tri_uvs) {
-      const double *u = d->tri_uvs + 6 * (size_t)i;
-      for (int a = 0; a < 2; a++) {
-        ts.uv0[a] = (float)u[a];
-        ts.duv1[a] = (float)(u[2 + a] - u[a]);
-        ts.duv2[a] = (float)(u[4 + a] - u[a]);
-      }
+  // ---- primitives and their bounds (in the FP32 geometry the kernels test),
+  // on all host threads; a device build reads them from pinned staging
+  const bool dev_build = np > 0 && np <= (1u << 26) &&
+                         (d->build == OR3_BUILD_DEVICE ||
+                          (d->build == OR3_BUILD_AUTO && np >= OR3_BUILD_DEVICE_MIN_PRIMS));
+  FlatPrims fp;
+  const size_t stage_need = kFlatBytes * (size_t)np + 4 * 64;
+  if (dev_build && stage_need <= kStageMax) {
+    if (ctx->stage_bytes < stage_need) {
+      cudaStreamSynchronize(ctx->stream);
+      if (ctx->stage) cudaFreeHost(ctx->stage);
+      ctx->stage = nullptr;
+      ctx->stage_bytes = 0;
+      if (cudaMallocHost(&ctx->stage, stage_need) == cudaSuccess) ctx->stage_bytes = stage_need;
+      else ctx->stage = nullptr;
     }
   }
-  for (uint32_t j = 0; j < nsph; j++) {
-    const uint32_t i = nt + j;
-    int rc = check_layers(ctx, d, d->sphere_layers + 2 * j, "sphere", j);
-    if (rc) { free_scene(sg); return rc; }
-    const double *s = d->spheres + 4 * (size_t)j;
-    if (!(s[3] > 0)) { free_scene(sg); return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sphere %u: radius <= 0", j); }
-    float *g = &geom[12 * (size_t)i];
-    g[0] = (float)s[0]; g[1] = (float)s[1]; g[2] = (float)s[2]; g[3] = (float)s[3];
-    for (int a = 0; a < 3; a++) {
-      bp[i].lo[a] = down((double)g[a] - (double)g[3]);
-      bp[i].hi[a] = up((double)g[a] + (double)g[3]);
-    }
-    bp[i].kind = kPrimSphere;
-    const uint32_t *lay = d->sphere_layers + 2 * j;
-    uint32_t fl = layer_flags(d, lay);
-    if (d->sphere_flags && (d->sphere_flags[j] & OR3_SPHERE_LIGHT)) fl |= kFlagSphereLight;
-    pinfo[i] = PrimInfo{d->sphere_ids ? d->sphere_ids[j] : nt + j, lay[0], lay[1], kPrimSphere | (fl << 8)};
+  if (dev_build && ctx->stage && ctx->stage_bytes >= stage_need) {
+    cudaStreamSynchronize(ctx->stream);  // no copy out of the staging still in flight
+    char *c = static_cast<char *>(ctx->stage);
+    auto carve = [&](size_t bytes) {
+      char *r = c;
+      c += (bytes + 63) & ~size_t(63);
+      return r;
+    };
+    fp.geom = reinterpret_cast<float *>(carve(12 * sizeof(float) * (size_t)np));
+    fp.bp = reinterpret_cast<BuildPrim *>(carve(sizeof(BuildPrim) * (size_t)np));
+    fp.info = reinterpret_cast<PrimInfo *>(carve(sizeof(PrimInfo) * (size_t)np));
+    fp.shade = reinterpret_cast<TriShade *>(carve(sizeof(TriShade) * (size_t)np));
+  } else {
+    fp.vgeom.resize(12 * (size_t)np);
+    fp.vbp.resize(np);
+    fp.vinfo.resize(np);
+    fp.vshade.resize(np);
+    fp.geom = fp.vgeom.data();
+    fp.bp = fp.vbp.data();
+    fp.info = fp.vinfo.data();
+    fp.shade = fp.vshade.data();
   }
+  {
+    const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t nth = std::max(1u, std::min<uint32_t>(hw, np / 8192u));
+    std::vector<uint32_t> first_bad(nth, np);
+    std::vector<char> bad_bounds(nth, 0);
+    auto work = [&](uint32_t t) {
+      const uint32_t a = (uint32_t)((uint64_t)np * t / nth), b = (uint32_t)((uint64_t)np * (t + 1) / nth);
+      bool bb = false;
+      const uint32_t r = flatten_range(d, a, b, fp, &bb);
+      first_bad[t] = r < b ? r : np;
+      bad_bounds[t] = bb;
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t t = 1; t < nth; t++) pool.emplace_back(work, t);
+    work(0);
+    for (std::thread &th : pool) th.join();
+    const uint32_t bad = *std::min_element(first_bad.begin(), first_bad.end());
+    if (bad < np) {
+      // the message of the first invalid primitive, as a sequential check gives it
+      int rc = bad < nt ? check_layers(ctx, d, d->tri_layers + 2 * (size_t)bad, "triangle", bad)
+                        : check_layers(ctx, d, d->sphere_layers + 2 * (size_t)(bad - nt), "sphere", bad - nt);
+      if (!rc) rc = fail(ctx, OR3_ERR_INVALID_ARGUMENT, "sphere %u: radius <= 0", bad - nt);
+      free_scene(sg);
+      return rc;
+    }
+    if (dev_build && std::find(bad_bounds.begin(), bad_bounds.end(), 1) != bad_bounds.end()) {
+      free_scene(sg);
+      return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "build_wide_bvh: primitive with invalid or non-finite bounds");
+    }
+  }
+  auto tf = std::chrono::steady_clock::now();
 
   // ---- BVH: host threads, or the device for large scenes (same tree rules)
   if (d->build > OR3_BUILD_DEVICE) {
@@ -518,34 +627,26 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     free_scene(sg);
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "leaf_max %d: at most 8", leaf_max);
   }
-  const bool on_device = np > 0 && np <= (1u << 26) &&
-                         (d->build == OR3_BUILD_DEVICE ||
-                          (d->build == OR3_BUILD_AUTO && np >= OR3_BUILD_DEVICE_MIN_PRIMS));
+  const bool on_device = dev_build;
   WideBVH bvh;
   DeviceBVH dbvh;
-  DeviceTemps tmp;  // freed when the upload returns (after its stream sync)
+  DeviceTemps tmp(ctx);  // freed on the stream when the upload returns
   std::string berr;
   if (!on_device) {
-    if (!build_wide_bvh(bp, 16, leaf_max, bvh, &berr, trav_cost)) {
+    if (!build_wide_bvh(fp.vbp, 16, leaf_max, bvh, &berr, trav_cost)) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "%s", berr.c_str());
     }
   } else {
-    for (const BuildPrim &b : bp)
-      for (int a = 0; a < 3; a++)
-        if (!(b.lo[a] <= b.hi[a]) || !std::isfinite(b.lo[a]) || !std::isfinite(b.hi[a])) {
-          free_scene(sg);
-          return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "build_wide_bvh: primitive with invalid or non-finite bounds");
-        }
     BuildPrim *bp_dev = nullptr;
     if (int rc = tmp.alloc(ctx, &bp_dev, np)) { free_scene(sg); return rc; }
-    const cudaError_t ce = cudaMemcpyAsync(bp_dev, bp.data(), np * sizeof(BuildPrim), cudaMemcpyHostToDevice,
+    const cudaError_t ce = cudaMemcpyAsync(bp_dev, fp.bp, np * sizeof(BuildPrim), cudaMemcpyHostToDevice,
                                            ctx->stream);
     if (ce != cudaSuccess) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(ce));
     }
-    if (!build_wide_bvh_device(bp_dev, np, leaf_max, ctx->stream, dbvh, &berr, trav_cost)) {
+    if (!build_wide_bvh_device(bp_dev, np, leaf_max, ctx->stream, dbvh, &berr, trav_cost, ctx->tmp_pool)) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "%s", berr.c_str());
     }
@@ -562,7 +663,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   std::vector<TriShade> shade(nrec);
   for (uint32_t r = 0; r < nrec; r++) {
     const uint32_t src = bvh.order[r];
-    const float *g = &geom[12 * (size_t)src];
+    const float *g = fp.geom + 12 * (size_t)src;
     if (src < nt) {
       prims[3 * r + 0] = make_float4(g[0], g[1], g[2], g[3]);
       prims[3 * r + 1] = make_float4(g[4], g[5], g[6], g[7]);
@@ -572,8 +673,8 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       prims[3 * r + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
       prims[3 * r + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    info[r] = pinfo[src];
-    shade[r] = tshade[src];
+    info[r] = fp.info[src];
+    shade[r] = fp.shade[src];
   }
   std::vector<PlaneRec> planes(d->num_planes);
   for (uint32_t i = 0; i < d->num_planes; i++) {
@@ -648,12 +749,12 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       free_scene(sg);
       return rc;
     }
-    cudaError_t ce = cudaMemcpyAsync(geom_in, geom.data(), 12 * sizeof(float) * (size_t)np, cudaMemcpyHostToDevice,
+    cudaError_t ce = cudaMemcpyAsync(geom_in, fp.geom, 12 * sizeof(float) * (size_t)np, cudaMemcpyHostToDevice,
                                      ctx->stream);
     if (ce == cudaSuccess)
-      ce = cudaMemcpyAsync(info_in, pinfo.data(), np * sizeof(PrimInfo), cudaMemcpyHostToDevice, ctx->stream);
+      ce = cudaMemcpyAsync(info_in, fp.info, np * sizeof(PrimInfo), cudaMemcpyHostToDevice, ctx->stream);
     if (ce == cudaSuccess)
-      ce = cudaMemcpyAsync(shade_in, tshade.data(), np * sizeof(TriShade), cudaMemcpyHostToDevice, ctx->stream);
+      ce = cudaMemcpyAsync(shade_in, fp.shade, np * sizeof(TriShade), cudaMemcpyHostToDevice, ctx->stream);
     if (ce != cudaSuccess) {
       free_scene(sg);
       return fail(ctx, OR3_ERR_CUDA, "scene upload: %s", cudaGetErrorString(ce));
@@ -711,7 +812,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     S.env_h = H;
   }
   LightTables T;
-  build_light_tables(d, geom, T);
+  build_light_tables(d, fp.geom, T);
   if ((rc = dev_upload(ctx, sg, T.lights, &S.lights))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, T.cdf, &S.light_cdf))) { free_scene(sg); return rc; }
   if ((rc = dev_upload(ctx, sg, T.pdf, &S.light_pdf))) { free_scene(sg); return rc; }
@@ -746,6 +847,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
   sg->info.num_primitives = np + d->num_planes;
   sg->info.num_nodes = S.num_nodes;
   sg->info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  sg->info.flatten_ms = std::chrono::duration<double, std::milli>(tf - t0).count();
   sg->info.upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
   sg->info.tree_depth = on_device ? dbvh.wide_depth : bvh.wide_depth;
   const int32_t id = ctx->next_scene++;
@@ -980,20 +1082,30 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     // frame = running mean over `next` samples (PathTracer.cpp:169-170)
     const double scale = 1.0 / ((double)next * ss2);
     launch_frame(ctx->pix_sum, W, H, prm->output_layout, scale, ctx->frame_dev, st);
+    if (frame_doubles > ctx->cap_back) {  // the back buffer is never read by another thread
+      cudaStreamSynchronize(st);
+      cudaFreeHost(ctx->frame_pinned);
+      ctx->frame_pinned = nullptr;
+      ctx->cap_back = 0;
+      OR3_CUDA(ctx, cudaMallocHost(&ctx->frame_pinned, frame_doubles * sizeof(double)));
+      ctx->cap_back = frame_doubles;
+    }
     OR3_CUDA(ctx, cudaMemcpyAsync(ctx->frame_pinned, ctx->frame_dev, frame_doubles * sizeof(double),
                                   cudaMemcpyDeviceToHost, st));
     OR3_CUDA(ctx, cudaStreamSynchronize(st));
     {
       std::lock_guard<std::mutex> lk(ctx->frame_mu);
-      ctx->frame_host.assign(ctx->frame_pinned, ctx->frame_pinned + frame_doubles);
+      std::swap(ctx->frame_pinned, ctx->frame_front);
+      std::swap(ctx->cap_back, ctx->cap_front);
+      ctx->front_doubles = frame_doubles;
       ctx->frame_samples = next;
     }
     ctx->last_count = (uint64_t)next * ss2;
     prev = next;
-    if (cb) {
+    if (cb) {  // the front frame changes only in this thread, after the callback returns
       const double minutes =
           std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count() / 60.0;
-      cb(user, next, ctx->frame_pinned, (prm->output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * (size_t)W,
+      cb(user, next, ctx->frame_front, (prm->output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * (size_t)W,
          (size_t)H, minutes);
     }
   }
@@ -1019,10 +1131,10 @@ int or3_get_frame(or3_context *ctx, double *rgb, size_t capacity, int32_t *sampl
   if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(ctx->frame_mu);
   if (samples_out) *samples_out = ctx->frame_samples;
-  if (ctx->frame_host.empty()) return fail(ctx, OR3_ERR_NOT_FOUND, "no frame rendered yet");
-  if (!rgb || capacity < ctx->frame_host.size())
-    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "frame needs %zu doubles", ctx->frame_host.size());
-  std::memcpy(rgb, ctx->frame_host.data(), ctx->frame_host.size() * sizeof(double));
+  if (ctx->front_doubles == 0) return fail(ctx, OR3_ERR_NOT_FOUND, "no frame rendered yet");
+  if (!rgb || capacity < ctx->front_doubles)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "frame needs %zu doubles", ctx->front_doubles);
+  std::memcpy(rgb, ctx->frame_front, ctx->front_doubles * sizeof(double));
   return OR3_OK;
 }
 

@@ -264,7 +264,7 @@ int frame_bytes(or3_context *ctx, uint8_t *out, size_t capacity, int32_t *sample
   {
     std::lock_guard<std::mutex> lk(ctx->frame_mu);
     if (samples) *samples = ctx->frame_samples;
-    nd = ctx->frame_host.size();
+    nd = ctx->front_doubles;
   }
   if (nd == 0) return fail(ctx, OR3_ERR_NOT_FOUND, "no frame rendered yet");
   const size_t npix = nd / 3;

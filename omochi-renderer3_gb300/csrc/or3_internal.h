@@ -53,8 +53,12 @@ struct or3_context {
   size_t cap_pixels = 0;
   double *pix_sum = nullptr, *pix_sumsq = nullptr;
   size_t cap_frame = 0;
-  double *frame_dev = nullptr, *frame_pinned = nullptr;
-  std::vector<double> frame_host;  // last completed frame (Renderer::GetResult)
+  double *frame_dev = nullptr;
+  // pinned host frames: the pass's copy lands in the back buffer, which then
+  // becomes the front (last completed frame, Renderer::GetResult) by a
+  // pointer swap under frame_mu
+  double *frame_pinned = nullptr, *frame_front = nullptr;
+  size_t cap_back = 0, cap_front = 0, front_doubles = 0;
   std::mutex frame_mu;
   int32_t frame_samples = 0;
 
@@ -69,6 +73,12 @@ struct or3_context {
   // per-kernel timing events of one pass (4 per bounce: before extend, shade,
   // shadow and after), created on first use and kept for later renders
   std::vector<cudaEvent_t> kpool;
+  // pinned staging of flattened primitives for device BVH builds (grown on demand)
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  // stream-ordered pool for the temporaries of a scene upload (keeps up to
+  // 1 GiB cached between uploads)
+  cudaMemPool_t tmp_pool = nullptr;
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

@@ -112,3 +112,36 @@ def test_auto_build_location(pkg, ctx):
     bad = _with_build(small, 7)
     with pytest.raises(pkg.Or3Error):
         ctx.upload(bad)
+
+
+def test_upload_names_the_first_invalid_primitive(pkg, ctx):
+    """The primitives are flattened on all host threads; the error is still the
+    one a sequential check meets first (lowest triangle index, then spheres)."""
+    def scene(bad_tris=(), inf_tri=None, bad_sphere=False):
+        sd = pkg.SceneDesc()
+        m = sd.material(pkg.abi.OR3_LAMBERT, (0.5, 0.5, 0.5))
+        rng = np.random.default_rng(5)
+        v = rng.uniform(0, 100, (40000, 1, 3)) + rng.uniform(-2, 2, (40000, 3, 3))
+        if inf_tri is not None:
+            v[inf_tri, 1, 0] = np.inf
+        lay = np.tile(np.asarray(sd.layers(m), np.uint32), (40000, 1))
+        for i in bad_tris:
+            lay[i] = (0, 0)
+        sd.add_triangles(v, lay)
+        sd.add_sphere((50, 50, 50), -1.0 if bad_sphere else 3.0, sd.layers(m))
+        return sd
+
+    for kw, text in ((dict(bad_tris=(31000, 20001, 39999)), "triangle 20001"),
+                     (dict(bad_sphere=True), "sphere 0"),
+                     (dict(bad_tris=(7,), bad_sphere=True), "triangle 7")):
+        with pytest.raises(pkg.Or3Error) as e:
+            ctx.upload(scene(**kw))
+        assert e.value.code == pkg.abi.OR3_ERR_INVALID_ARGUMENT
+        assert text in str(e.value), str(e.value)
+    with pytest.raises(pkg.Or3Error) as e:
+        ctx.upload(scene(inf_tri=12345))
+    assert "non-finite" in str(e.value)
+    # the context stays usable
+    sid = ctx.upload(scene())
+    assert ctx.scene_info(sid)["flatten_ms"] > 0
+    ctx.release(sid)

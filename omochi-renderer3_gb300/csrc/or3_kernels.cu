@@ -101,31 +101,29 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
   LocalStack stk{stk_e, stk_t};
   TravState st;
   uint32_t r = kNoEntry;
-  bool exhausted = false;
+  bool drained = false;  // warp-uniform: the shared fetch counter has passed n
   const uint32_t lane = threadIdx.x & 31u;
   for (;;) {
-    const bool need = (r == kNoEntry) && !exhausted;
-    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    if (STEP == 2 && __popc(m) < REFILL && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
-    if (m) {
-      const int leader = __ffs(m) - 1;
+    // one vote per step: the idle lanes
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, r == kNoEntry);
+    if (!drained && idle != 0u && (STEP == 1 || __popc(idle) >= REFILL || idle == 0xFFFFFFFFu)) {
+      const int leader = __ffs(idle) - 1;
+      const uint32_t want = (uint32_t)__popc(idle);
       uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+      if ((int)lane == leader) base = atomicAdd(fetch, want);
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
-      const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-      if (need) {
-        if (idx < n) {
-          V3 o, d;
-          float tmax;
-          src.load(idx, o, d, tmax);
-          trav_init(st, o, d, tmax, S.num_nodes);
-          r = idx;
-        } else {
-          exhausted = true;
-        }
+      const uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+      if (r == kNoEntry && idx < n) {
+        V3 o, d;
+        float tmax;
+        src.load(idx, o, d, tmax);
+        trav_init(st, o, d, tmax, S.num_nodes);
+        r = idx;
       }
+      drained = base + want >= n;
+    } else if (drained && idle == 0xFFFFFFFFu) {
+      break;
     }
-    if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
       const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
                                   : trav_step_inline<ANY, COUNT, SORT, LocalStack, FN>(S, st, stk, snodes, ns,
@@ -853,33 +851,30 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
   TravState st;
   const DevScene *sp = nullptr;
   uint32_t r = kNoEntry;
-  bool exhausted = false;
+  bool drained = false;  // warp-uniform: the shared fetch counter has passed n
   const uint32_t lane = threadIdx.x & 31u;
   for (;;) {
-    const bool need = (r == kNoEntry) && !exhausted;
-    unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    if (__popc(m) < 16 && m != __ballot_sync(0xFFFFFFFFu, !exhausted)) m = 0;
-    if (m) {
-      const int leader = __ffs(m) - 1;
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, r == kNoEntry);
+    if (!drained && (__popc(idle) >= 16 || idle == 0xFFFFFFFFu)) {
+      const int leader = __ffs(idle) - 1;
+      const uint32_t want = (uint32_t)__popc(idle);
       uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+      if ((int)lane == leader) base = atomicAdd(fetch, want);
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
-      if (need) {
-        const uint32_t idx = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-        if (idx < n) {
-          V3 o, d;
-          float tmax;
-          uint32_t tag;
-          src.load(idx, o, d, tmax, tag);
-          sp = &b.scenes[b.jobs[b.segs[tag].job].scene];
-          trav_init(st, o, d, tmax, sp->num_nodes);
-          r = idx;
-        } else {
-          exhausted = true;
-        }
+      const uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+      if (r == kNoEntry && idx < n) {
+        V3 o, d;
+        float tmax;
+        uint32_t tag;
+        src.load(idx, o, d, tmax, tag);
+        sp = &b.scenes[b.jobs[b.segs[tag].job].scene];
+        trav_init(st, o, d, tmax, sp->num_nodes);
+        r = idx;
       }
+      drained = base + want >= n;
+    } else if (drained && idle == 0xFFFFFFFFu) {
+      break;
     }
-    if (__all_sync(0xFFFFFFFFu, r == kNoEntry)) break;
     if (r != kNoEntry) {
       if (trav_step_inline<ANY, COUNT>(*sp, st, stk, nullptr, 0u, cnt, err)) {
         sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);

@@ -452,19 +452,16 @@ def main():
     time.sleep(0.3)
     barrier(dist)
     torch.cuda.synchronize()
-    render_ms = ext_ms = shade_ms = shadow_ms = 0.0
+    render_ms = 0.0
     shadow_rays = 0
-    ext_launches = paths = ext_rays = bounces = waves = passes = 0
+    launches_all = paths = ext_rays = bounces = waves = passes = 0
     w0 = time.perf_counter()
     for i in range(args.steps):
         flush.zero_()  # L2 (129 MB) flushed between steps
-        s = ctx.render(sid, cam, seed=i, flags=A.OR3_FLAG_TIME_KERNELS, **kw)
+        s = ctx.render(sid, cam, seed=i, **kw)
         render_ms += s["render_ms"]
-        ext_ms += s["extend_ms"]
-        shade_ms += s["shade_ms"]
-        shadow_ms += s["shadow_ms"]
         shadow_rays += s["shadow_rays"]
-        ext_launches += s["extend_launches"]
+        launches_all += s["extend_launches"]
         paths += s["camera_paths"]
         ext_rays += s["extension_rays"]
         bounces += s["bounces"]
@@ -474,6 +471,12 @@ def main():
     barrier(dist)
     wall_s = time.perf_counter() - w0
     clk = clocks.stop()
+    # the kernel split: one more render of the same step with per-kernel CUDA
+    # events (that flag keeps every wave on one stream), untimed
+    flush.zero_()
+    t = ctx.render(sid, cam, seed=args.steps, flags=A.OR3_FLAG_TIME_KERNELS, **kw)
+    ext_ms, shade_ms, shadow_ms = t["extend_ms"], t["shade_ms"], t["shadow_ms"]
+    ext_launches, t_ext_rays = t["extend_launches"], t["extension_rays"]
     dev_s = max_over_ranks(dist, render_ms / 1000.0)
     total_paths = sum_over_ranks(dist, float(paths))
     value = total_paths / dev_s / 1e6
@@ -492,10 +495,10 @@ def main():
     e2e_s = max_over_ranks(dist, time.perf_counter() - e0)
     e2e_paths = sum_over_ranks(dist, float(paths / args.steps * e2e_steps))
 
-    # per wave raygen + accumulate; per bounce extend, shade, reset (+ shadow with NEE); per pass frame
-    launches = 2 * waves + (4 if shadow_rays else 3) * ext_launches + passes
+    # per wave raygen + accumulate; per bounce extend, shade, reset (+ shadow); per pass frame (+ merge)
+    launches = 2 * waves + (4 if shadow_rays else 3) * launches_all + 2 * passes
     avg_ext_ms = ext_ms / max(ext_launches, 1)
-    achieved = alg_bytes_per_ray * ext_rays / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else None
+    achieved = alg_bytes_per_ray * t_ext_rays / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else None
     peak, peak_kind = load_peaks()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -512,8 +515,9 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "wall_s_timed": wall_s, "shadow_rays_per_step": shadow_rays // args.steps,
                        "mrays_per_s": (ext_rays + shadow_rays) / (render_ms / 1000.0) / 1e6,
-                       "extend_ms_per_step": ext_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps,
-                       "shadow_ms_per_step": shadow_ms / args.steps,
+                       "kernel_split": "extend / shade / shadow device time of one more step with per-kernel "
+                                       "CUDA events, all waves on one stream",
+                       "extend_ms_per_step": ext_ms, "shade_ms_per_step": shade_ms, "shadow_ms_per_step": shadow_ms,
                        "per_extension_ray": {k: c[k] / max(c["extension_rays"], 1)
                                              for k in ("nodes_visited", "tris_tested", "spheres_tested")}},
             "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
@@ -522,10 +526,10 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,
-                         "traffic": (EXTEND_DRAM_BYTES_PER_RAY[args.workload] * ext_rays / max(ext_launches, 1)
+                         "traffic": (EXTEND_DRAM_BYTES_PER_RAY[args.workload] * t_ext_rays / max(ext_launches, 1)
                                      if args.workload in EXTEND_DRAM_BYTES_PER_RAY else None),
                          "traffic_unit": "bytes per launch",
-                         "alg_bytes_per_launch": alg_bytes_per_ray * ext_rays / max(ext_launches, 1),
+                         "alg_bytes_per_launch": alg_bytes_per_ray * t_ext_rays / max(ext_launches, 1),
                          "alg_bytes_per_ray": alg_bytes_per_ray, "avg_launch_ms": avg_ext_ms,
                          "launches": ext_launches,
                          "sm_issue_active_ncu": EXTEND_ISSUE_ACTIVE.get(args.workload)},

@@ -147,6 +147,7 @@ OR3_TUNE_SMEM_NODES = 0x10
 OR3_TUNE_SHADOW_UNSORTED = 0x20
 OR3_TUNE_L2_PERSIST = 0x40
 OR3_TUNE_SHADE_NEE_OCC4 = 0x80
+OR3_TUNE_ONE_LANE = 0x100
 
 # name -> (restype, argtypes); every function declared in include/or3.h
 PROTOTYPES = {

@@ -266,6 +266,73 @@ Queues make_queues(or3_context *ctx) {
   return q;
 }
 
+// The second wave lane: stream, events and counters once; queues and pixel
+// sums grown like the first lane's.
+int ensure_lane1(or3_context *ctx, size_t paths, size_t rays, size_t pixels) {
+  or3_context::Lane &L = ctx->lane1;
+  if (!L.stream) {
+    OR3_CUDA(ctx, cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+    OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    OR3_CUDA(ctx, cudaMalloc(&L.counters, 16 * sizeof(uint32_t)));
+    OR3_CUDA(ctx, cudaMalloc(&L.dstats, 8 * sizeof(unsigned long long)));
+  }
+  if (paths > L.cap_paths || rays > L.cap_rays) {
+    for (int k = 0; k < 2; k++) {
+      cudaFree(L.qorig[k]);
+      cudaFree(L.qdir[k]);
+      cudaFree(L.qbeta[k]);
+      L.qorig[k] = L.qdir[k] = L.qbeta[k] = nullptr;
+    }
+    for (float4 **p : {&L.hits, &L.pathL, &L.sorig, &L.sdir, &L.scontrib}) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+    L.cap_paths = L.cap_rays = 0;
+    for (int k = 0; k < 2; k++) {
+      OR3_CUDA(ctx, cudaMalloc(&L.qorig[k], rays * sizeof(float4)));
+      OR3_CUDA(ctx, cudaMalloc(&L.qdir[k], rays * sizeof(float4)));
+      OR3_CUDA(ctx, cudaMalloc(&L.qbeta[k], rays * sizeof(float4)));
+    }
+    OR3_CUDA(ctx, cudaMalloc(&L.hits, rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&L.pathL, paths * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&L.sorig, rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&L.sdir, rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&L.scontrib, rays * sizeof(float4)));
+    L.cap_paths = paths;
+    L.cap_rays = rays;
+  }
+  if (pixels > L.cap_pixels) {
+    cudaFree(L.pix_sum);
+    cudaFree(L.pix_sumsq);
+    L.pix_sum = L.pix_sumsq = nullptr;
+    L.cap_pixels = 0;
+    OR3_CUDA(ctx, cudaMalloc(&L.pix_sum, pixels * 3 * sizeof(double)));
+    OR3_CUDA(ctx, cudaMalloc(&L.pix_sumsq, pixels * 3 * sizeof(double)));
+    L.cap_pixels = pixels;
+  }
+  return OR3_OK;
+}
+
+Queues lane1_queues(or3_context *ctx) {
+  const or3_context::Lane &L = ctx->lane1;
+  Queues q{};
+  for (int k = 0; k < 2; k++) {
+    q.orig[k] = L.qorig[k];
+    q.dir[k] = L.qdir[k];
+    q.beta[k] = L.qbeta[k];
+  }
+  q.hits = L.hits;
+  q.pathL = L.pathL;
+  q.sorig = L.sorig;
+  q.sdir = L.sdir;
+  q.scontrib = L.scontrib;
+  q.counters = L.counters;
+  q.stats = L.dstats;
+  q.capacity = (uint32_t)L.cap_rays;
+  return q;
+}
+
 // Camera::Camera (src/renderer/Camera.h:12-43) in double.
 int validate_render(or3_context *ctx, const or3_camera *cam, const or3_render_params *prm) {
   if (cam->width == 0 || cam->height == 0) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "empty image");
@@ -411,6 +478,21 @@ int or3_context_destroy(or3_context *ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->kpool) cudaEventDestroy(e);
   if (ctx->stage) cudaFreeHost(ctx->stage);
+  {
+    or3_context::Lane &L = ctx->lane1;
+    if (L.stream) cudaStreamSynchronize(L.stream);
+    for (int k = 0; k < 2; k++) {
+      cudaFree(L.qorig[k]);
+      cudaFree(L.qdir[k]);
+      cudaFree(L.qbeta[k]);
+    }
+    for (void *p : {(void *)L.hits, (void *)L.pathL, (void *)L.sorig, (void *)L.sdir, (void *)L.scontrib,
+                    (void *)L.counters, (void *)L.dstats, (void *)L.pix_sum, (void *)L.pix_sumsq})
+      cudaFree(p);
+    if (L.stream) cudaStreamDestroy(L.stream);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  }
   cudaStreamSynchronize(ctx->stream);
   if (ctx->tmp_pool) cudaMemPoolDestroy(ctx->tmp_pool);
   cudaStreamDestroy(ctx->stream);
@@ -978,6 +1060,19 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // a depth bound of at most 32 enqueues every bounce of a wave at once
   const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;
   const int chunk = whole ? prm->max_depth : 8;
+  // two lanes: odd waves on a second stream (only where nothing per wave or
+  // per kernel is read back)
+  const bool two = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
+                   !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
+  Queues q1{};
+  if (two) {
+    if ((rc = ensure_lane1(ctx, max_wave_paths, rays, npix))) return rc;
+    q1 = lane1_queues(ctx);
+    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.pix_sum, 0, npix * 3 * sizeof(double), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.pix_sumsq, 0, npix * 3 * sizeof(double), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.counters, 0, 16 * sizeof(uint32_t), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.dstats, 0, 8 * sizeof(unsigned long long), st));
+  }
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
@@ -990,7 +1085,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   for (int32_t next = prm->min_samples; next <= prm->max_samples; next += prm->step_samples) {
     if (ctx->stop.load()) { stopped = true; break; }
     size_t kused = 0;  // timing events used in this pass
+    uint32_t wave_index = 0;
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+    if (two) {
+      OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+      OR3_CUDA(ctx, cudaStreamWaitEvent(ctx->lane1.stream, ctx->ev_fork, 0));
+    }
     // waves over [prev, next) samples
     for (uint32_t s = (uint32_t)prev; s < (uint32_t)next && !stopped;) {
       const uint32_t ns = (uint32_t)std::min<uint64_t>(ns_per_wave, (uint64_t)next - s);
@@ -1003,7 +1103,10 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         w.pix0 = (uint32_t)p0;
         w.npix = (uint32_t)np;
         w.ns = ns;
-        launch_raygen(rcst, w, q, 0, 0, block, st);
+        const bool odd = two && (wave_index++ & 1u);
+        const Queues &ql = odd ? q1 : q;
+        cudaStream_t sl = odd ? ctx->lane1.stream : st;
+        launch_raygen(rcst, w, ql, 0, 0, block, sl);
         // Bounces are enqueued in chunks without a host round trip: every
         // kernel reads its queue length on the device, so a bounce after the
         // last ray is a few empty launches.  With a depth bound the chunk is
@@ -1023,14 +1126,14 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
               kused += 4;
             }
             if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[0], st));
-            launch_extend(sg->view, q, in, grid_ext, block, smem_nodes, countk, variant, st);
+            launch_extend(sg->view, ql, in, grid_ext, block, smem_nodes, countk, variant, sl);
             if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[1], st));
-            launch_shade(sg->view, rcst, w, q, in, grid_sh, block, st, nee4);
+            launch_shade(sg->view, rcst, w, ql, in, grid_sh, block, sl, nee4);
             if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
             if (shadows)
-              launch_shadow(sg->view, q, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, st);
+              launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl);
             if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
-            launch_reset_count(q, in, st);
+            launch_reset_count(ql, in, sl);
             in ^= 1;
             stats.extend_launches++;
             stats.shade_launches++;
@@ -1042,8 +1145,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
           if (ctx->host_counters[in] == 0 || ctx->host_counters[2] || chunks > 100000) break;
         }
-        launch_accumulate(q, w, ss2, ctx->pix_sum, ctx->pix_sumsq,
-                          (int)std::min<uint64_t>((np + 7) / 8, 152 * 64), block, st);
+        launch_accumulate(ql, w, ss2, odd ? ctx->lane1.pix_sum : ctx->pix_sum,
+                          odd ? ctx->lane1.pix_sumsq : ctx->pix_sumsq, (int)std::min<uint64_t>((np + 7) / 8, 152 * 64),
+                          block, sl);
         stats.waves++;
         stats.camera_paths += w.num_paths;
         ctx->last_wave_paths = w.num_paths;
@@ -1052,6 +1156,13 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       s += ns;
       if (ctx->host_counters[2]) break;
       if (ctx->stop.load() && s < (uint32_t)next) stopped = true;
+    }
+    if (two) {  // join the second lane and fold its pixel sums into the first lane's
+      OR3_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->lane1.stream));
+      OR3_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+      launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, ctx->lane1.pix_sum, ctx->lane1.pix_sumsq, st);
+      OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8, ctx->lane1.counters, 4 * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, st));
     }
     // error bits of the pass (queue capacity, traversal stack)
     OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -1067,9 +1178,10 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       stats.shade_ms += s2;
       if (shadows) stats.shadow_ms += s3;
     }
-    if (ctx->host_counters[2]) {
-      const uint32_t bits = ctx->host_counters[2];
+    if (ctx->host_counters[2] || (two && ctx->host_counters[10])) {
+      const uint32_t bits = ctx->host_counters[2] | (two ? ctx->host_counters[10] : 0u);
       cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
+      if (two) cudaMemsetAsync(ctx->lane1.counters, 0, 16 * sizeof(uint32_t), st);
       cudaStreamSynchronize(st);
       return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x (%s)", bits,
                   (bits & kErrQueue) ? "ray queue capacity" : "traversal stack");
@@ -1111,6 +1223,11 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   }
   unsigned long long hs[8];
   OR3_CUDA(ctx, cudaMemcpy(hs, ctx->dstats, sizeof(hs), cudaMemcpyDeviceToHost));
+  if (two) {
+    unsigned long long h1[8];
+    OR3_CUDA(ctx, cudaMemcpy(h1, ctx->lane1.dstats, sizeof(h1), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 8; k++) hs[k] += h1[k];
+  }
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];
   stats.bounces = hs[2];

@@ -657,6 +657,17 @@ __global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc
   }
 }
 
+// a[i] += b[i], b[i] = 0 over n doubles of two pixel-sum pairs (the second
+// wave lane's sums folded into the first lane's at the end of a pass)
+__global__ void k_merge_sums(size_t n, double *a, double *aq, double *b, double *bq) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    a[i] += b[i];
+    aq[i] += bq[i];
+    b[i] = 0.0;
+    bq[i] = 0.0;
+  }
+}
+
 // Clears a consumed queue's length and its extend fetch counter, and the
 // shadow queue's length and fetch counter.
 __global__ void k_reset_count(uint32_t *counters, int which) {
@@ -999,6 +1010,11 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
     k_shade<false, true><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
   else
     k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+}
+
+void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, cudaStream_t st) {
+  const size_t g = (n + 255) / 256;
+  if (n) k_merge_sums<<<(unsigned)(g < 152 * 16 ? g : 152 * 16), 256, 0, st>>>(n, a, aq, b, bq);
 }
 
 void launch_reset_count(const Queues &q, int which, cudaStream_t st) {

@@ -168,6 +168,34 @@ def test_waves_do_not_change_the_image(pkg, ctx):
     np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("nee", [False, True])
+def test_two_wave_lanes_match_one(pkg, ctx, nee):
+    """Odd waves run on a second stream with their own queues and pixel sums,
+    merged at the end of each pass: the image, the moments and the ray counts
+    equal the one-stream render's (up to the order of float additions: FP64
+    pixel sums, and FP32 atomics of light samples into a path's radiance)."""
+    sd, cam = pkg.workloads.sky_floor(48, 32) if nee else pkg.workloads.icosphere_in_box(48, 32, level=3)[:2]
+    sid = ctx.upload(sd)
+    kw = dict(supersamples=4, min_samples=2, max_samples=6, step_samples=2, seed=5, max_depth=8,
+              wave_paths=3000, next_event_estimation=nee)
+    try:
+        s2 = ctx.render(sid, cam, **kw)
+        f2, n2 = ctx.frame(cam.width, cam.height)
+        m2 = ctx.moments(cam.width, cam.height)
+        s1 = ctx.render(sid, cam, tuning=pkg.abi.OR3_TUNE_ONE_LANE, **kw)
+        f1, n1 = ctx.frame(cam.width, cam.height)
+        m1 = ctx.moments(cam.width, cam.height)
+    finally:
+        ctx.release(sid)
+    assert s2["waves"] > 10 and n1 == n2 == 6
+    for k in ("extension_rays", "shadow_rays", "camera_paths"):
+        assert s1[k] == s2[k], k
+    np.testing.assert_allclose(f2, f1, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(m2[0], m1[0], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(m2[1], m1[1], rtol=1e-5, atol=1e-7)
+    assert f1.sum() > 0
+
+
 def test_invalid_arguments_are_reported(pkg, ctx):
     sd, cam, _ = pkg.workloads.cornell_box(8, 8)
     sid = ctx.upload(sd)

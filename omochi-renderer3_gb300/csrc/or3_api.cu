@@ -266,14 +266,14 @@ Queues make_queues(or3_context *ctx) {
   return q;
 }
 
-// The second wave lane: stream, events and counters once; queues and pixel
-// sums grown like the first lane's.
-int ensure_lane1(or3_context *ctx, size_t paths, size_t rays, size_t pixels) {
-  or3_context::Lane &L = ctx->lane1;
+// An extra wave lane: stream, events and counters once; queues and pixel
+// sums grown like lane 0's.
+int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixels) {
+  or3_context::Lane &L = ctx->xl[k];
+  if (!ctx->ev_fork) OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
   if (!L.stream) {
     OR3_CUDA(ctx, cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
-    OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-    OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join[k], cudaEventDisableTiming));
     OR3_CUDA(ctx, cudaMalloc(&L.counters, 16 * sizeof(uint32_t)));
     OR3_CUDA(ctx, cudaMalloc(&L.dstats, 8 * sizeof(unsigned long long)));
   }
@@ -314,8 +314,7 @@ int ensure_lane1(or3_context *ctx, size_t paths, size_t rays, size_t pixels) {
   return OR3_OK;
 }
 
-Queues lane1_queues(or3_context *ctx) {
-  const or3_context::Lane &L = ctx->lane1;
+Queues lane_queues(const or3_context::Lane &L) {
   Queues q{};
   for (int k = 0; k < 2; k++) {
     q.orig[k] = L.qorig[k];
@@ -478,21 +477,21 @@ int or3_context_destroy(or3_context *ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->kpool) cudaEventDestroy(e);
   if (ctx->stage) cudaFreeHost(ctx->stage);
-  {
-    or3_context::Lane &L = ctx->lane1;
+  for (int k = 0; k < 2; k++) {
+    or3_context::Lane &L = ctx->xl[k];
     if (L.stream) cudaStreamSynchronize(L.stream);
-    for (int k = 0; k < 2; k++) {
-      cudaFree(L.qorig[k]);
-      cudaFree(L.qdir[k]);
-      cudaFree(L.qbeta[k]);
+    for (int j = 0; j < 2; j++) {
+      cudaFree(L.qorig[j]);
+      cudaFree(L.qdir[j]);
+      cudaFree(L.qbeta[j]);
     }
     for (void *p : {(void *)L.hits, (void *)L.pathL, (void *)L.sorig, (void *)L.sdir, (void *)L.scontrib,
                     (void *)L.counters, (void *)L.dstats, (void *)L.pix_sum, (void *)L.pix_sumsq})
       cudaFree(p);
     if (L.stream) cudaStreamDestroy(L.stream);
-    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->ev_join[k]) cudaEventDestroy(ctx->ev_join[k]);
   }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->tmp_pool) cudaMemPoolDestroy(ctx->tmp_pool);
   cudaStreamDestroy(ctx->stream);
@@ -1060,18 +1059,21 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // a depth bound of at most 32 enqueues every bounce of a wave at once
   const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;
   const int chunk = whole ? prm->max_depth : 8;
-  // two lanes: odd waves on a second stream (only where nothing per wave or
-  // per kernel is read back)
-  const bool two = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
-                   !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
-  Queues q1{};
-  if (two) {
-    if ((rc = ensure_lane1(ctx, max_wave_paths, rays, npix))) return rc;
-    q1 = lane1_queues(ctx);
-    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.pix_sum, 0, npix * 3 * sizeof(double), st));
-    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.pix_sumsq, 0, npix * 3 * sizeof(double), st));
-    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.counters, 0, 16 * sizeof(uint32_t), st));
-    OR3_CUDA(ctx, cudaMemsetAsync(ctx->lane1.dstats, 0, 8 * sizeof(unsigned long long), st));
+  // extra wave lanes: waves round robin over 1 + nx streams (only where
+  // nothing per wave or per kernel is read back)
+  const bool multi = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
+                     !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
+  const int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : 2;
+  const bool two = nx > 0;
+  Queues qx[2] = {};
+  for (int k = 0; k < nx; k++) {
+    or3_context::Lane &L = ctx->xl[k];
+    if ((rc = ensure_lane(ctx, k, max_wave_paths, rays, npix))) return rc;
+    qx[k] = lane_queues(L);
+    OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sum, 0, npix * 3 * sizeof(double), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sumsq, 0, npix * 3 * sizeof(double), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(L.counters, 0, 16 * sizeof(uint32_t), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(L.dstats, 0, 8 * sizeof(unsigned long long), st));
   }
 
   or3_render_stats stats{};
@@ -1089,7 +1091,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
     if (two) {
       OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
-      OR3_CUDA(ctx, cudaStreamWaitEvent(ctx->lane1.stream, ctx->ev_fork, 0));
+      for (int k = 0; k < nx; k++) OR3_CUDA(ctx, cudaStreamWaitEvent(ctx->xl[k].stream, ctx->ev_fork, 0));
     }
     // waves over [prev, next) samples
     for (uint32_t s = (uint32_t)prev; s < (uint32_t)next && !stopped;) {
@@ -1103,9 +1105,11 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         w.pix0 = (uint32_t)p0;
         w.npix = (uint32_t)np;
         w.ns = ns;
-        const bool odd = two && (wave_index++ & 1u);
-        const Queues &ql = odd ? q1 : q;
-        cudaStream_t sl = odd ? ctx->lane1.stream : st;
+        const int lane = two ? (int)(wave_index++ % (uint32_t)(1 + nx)) : 0;
+        const Queues &ql = lane ? qx[lane - 1] : q;
+        cudaStream_t sl = lane ? ctx->xl[lane - 1].stream : st;
+        double *lsum = lane ? ctx->xl[lane - 1].pix_sum : ctx->pix_sum;
+        double *lsq = lane ? ctx->xl[lane - 1].pix_sumsq : ctx->pix_sumsq;
         launch_raygen(rcst, w, ql, 0, 0, block, sl);
         // Bounces are enqueued in chunks without a host round trip: every
         // kernel reads its queue length on the device, so a bounce after the
@@ -1145,9 +1149,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
           if (ctx->host_counters[in] == 0 || ctx->host_counters[2] || chunks > 100000) break;
         }
-        launch_accumulate(ql, w, ss2, odd ? ctx->lane1.pix_sum : ctx->pix_sum,
-                          odd ? ctx->lane1.pix_sumsq : ctx->pix_sumsq, (int)std::min<uint64_t>((np + 7) / 8, 152 * 64),
-                          block, sl);
+        launch_accumulate(ql, w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, 152 * 64), block, sl);
         stats.waves++;
         stats.camera_paths += w.num_paths;
         ctx->last_wave_paths = w.num_paths;
@@ -1157,11 +1159,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       if (ctx->host_counters[2]) break;
       if (ctx->stop.load() && s < (uint32_t)next) stopped = true;
     }
-    if (two) {  // join the second lane and fold its pixel sums into the first lane's
-      OR3_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->lane1.stream));
-      OR3_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
-      launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, ctx->lane1.pix_sum, ctx->lane1.pix_sumsq, st);
-      OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8, ctx->lane1.counters, 4 * sizeof(uint32_t),
+    for (int k = 0; k < nx; k++) {  // join the extra lanes and fold their pixel sums into lane 0's
+      or3_context::Lane &L = ctx->xl[k];
+      OR3_CUDA(ctx, cudaEventRecord(ctx->ev_join[k], L.stream));
+      OR3_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join[k], 0));
+      launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, L.pix_sum, L.pix_sumsq, st);
+      OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8 + 4 * k, L.counters, 4 * sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, st));
     }
     // error bits of the pass (queue capacity, traversal stack)
@@ -1178,10 +1181,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       stats.shade_ms += s2;
       if (shadows) stats.shadow_ms += s3;
     }
-    if (ctx->host_counters[2] || (two && ctx->host_counters[10])) {
-      const uint32_t bits = ctx->host_counters[2] | (two ? ctx->host_counters[10] : 0u);
+    uint32_t errbits = ctx->host_counters[2];
+    for (int k = 0; k < nx; k++) errbits |= ctx->host_counters[8 + 4 * k + 2];
+    if (errbits) {
+      const uint32_t bits = errbits;
       cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
-      if (two) cudaMemsetAsync(ctx->lane1.counters, 0, 16 * sizeof(uint32_t), st);
+      for (int k = 0; k < nx; k++) cudaMemsetAsync(ctx->xl[k].counters, 0, 16 * sizeof(uint32_t), st);
       cudaStreamSynchronize(st);
       return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x (%s)", bits,
                   (bits & kErrQueue) ? "ray queue capacity" : "traversal stack");
@@ -1223,10 +1228,10 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   }
   unsigned long long hs[8];
   OR3_CUDA(ctx, cudaMemcpy(hs, ctx->dstats, sizeof(hs), cudaMemcpyDeviceToHost));
-  if (two) {
+  for (int k = 0; k < nx; k++) {
     unsigned long long h1[8];
-    OR3_CUDA(ctx, cudaMemcpy(h1, ctx->lane1.dstats, sizeof(h1), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < 8; k++) hs[k] += h1[k];
+    OR3_CUDA(ctx, cudaMemcpy(h1, ctx->xl[k].dstats, sizeof(h1), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < 8; j++) hs[j] += h1[j];
   }
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];

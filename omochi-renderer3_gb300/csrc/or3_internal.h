@@ -80,10 +80,10 @@ struct or3_context {
   // 1 GiB cached between uploads)
   cudaMemPool_t tmp_pool = nullptr;
 
-  // or3_render's second wave lane: odd waves run on their own stream with
-  // their own queues, counters and pixel sums (merged into the first lane's
-  // at the end of each pass), so one wave's latency-bound shading overlaps
-  // the other's traversal
+  // or3_render's extra wave lanes (two by default): waves are dealt round robin to lane 0
+  // (the buffers above) and these, each on its own stream with its own
+  // queues, counters and pixel sums (merged into lane 0's at the end of each
+  // pass), so one wave's latency-bound shading overlaps another's traversal
   struct Lane {
     cudaStream_t stream = nullptr;
     float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
@@ -92,8 +92,8 @@ struct or3_context {
     unsigned long long *dstats = nullptr;
     double *pix_sum = nullptr, *pix_sumsq = nullptr;
     size_t cap_paths = 0, cap_rays = 0, cap_pixels = 0;
-  } lane1;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  } xl[2];
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

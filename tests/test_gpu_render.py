@@ -168,10 +168,10 @@ def test_waves_do_not_change_the_image(pkg, ctx):
     np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("nee", [False, True])
-def test_two_wave_lanes_match_one(pkg, ctx, nee):
-    """Odd waves run on a second stream with their own queues and pixel sums,
-    merged at the end of each pass: the image, the moments and the ray counts
+@pytest.mark.parametrize("nee,tuning", [(False, 0), (True, 0), (True, 0x200)])
+def test_wave_lanes_match_one(pkg, ctx, nee, tuning):
+    """Waves run round robin on three (or two, 0x200) streams with their own
+    queues and pixel sums, merged at the end of each pass: the image, the moments and the ray counts
     equal the one-stream render's (up to the order of float additions: FP64
     pixel sums, and FP32 atomics of light samples into a path's radiance)."""
     sd, cam = pkg.workloads.sky_floor(48, 32) if nee else pkg.workloads.icosphere_in_box(48, 32, level=3)[:2]
@@ -179,7 +179,7 @@ def test_two_wave_lanes_match_one(pkg, ctx, nee):
     kw = dict(supersamples=4, min_samples=2, max_samples=6, step_samples=2, seed=5, max_depth=8,
               wave_paths=3000, next_event_estimation=nee)
     try:
-        s2 = ctx.render(sid, cam, **kw)
+        s2 = ctx.render(sid, cam, tuning=tuning, **kw)
         f2, n2 = ctx.frame(cam.width, cam.height)
         m2 = ctx.moments(cam.width, cam.height)
         s1 = ctx.render(sid, cam, tuning=pkg.abi.OR3_TUNE_ONE_LANE, **kw)

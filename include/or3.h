@@ -157,6 +157,7 @@ typedef struct or3_camera {
 #define OR3_FLAG_NO_GRAPH 4u     /* batched/served forms: launch the bounce loop without a CUDA graph */
 #define OR3_FLAG_TIME_KERNELS 16u      /* CUDA events around every extend/shade launch */
 #define OR3_FLAG_COUNT_TRAVERSAL 32u   /* count nodes and primitives visited (slower) */
+#define OR3_FLAG_ONE_LANE 64u          /* batched form: every wave on one stream (default: three that overlap) */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */
@@ -299,7 +300,7 @@ typedef struct or3_batch_job {
 
 typedef struct or3_batch_params {
   uint64_t wave_paths;     /* camera paths per wave, 0 = automatic */
-  uint32_t flags;          /* OR3_FLAG_NO_GRAPH, OR3_FLAG_COUNT_TRAVERSAL */
+  uint32_t flags;          /* OR3_FLAG_NO_GRAPH, OR3_FLAG_COUNT_TRAVERSAL, OR3_FLAG_ONE_LANE */
   uint32_t graph_bounces;  /* bounce iterations per graph launch, 0 = 8 */
   uint32_t blocks_per_sm;  /* persistent kernel blocks per SM, 0 = occupancy limit */
   uint32_t reserved;
@@ -333,10 +334,11 @@ typedef struct or3_server_params {
   uint32_t max_active_jobs;     /* 0 = 64 */
   uint32_t frame_every_samples; /* progressive frame cadence, 0 = 16 */
   uint32_t graph_bounces;       /* 0 = 8 */
-  uint32_t flags;               /* OR3_SERVER_KEEP_MOMENTS */
+  uint32_t flags;               /* OR3_SERVER_KEEP_MOMENTS, OR3_SERVER_ONE_LANE */
 } or3_server_params;
 
 #define OR3_SERVER_KEEP_MOMENTS 1u /* keep finished jobs' pixel sums on the host for or3_server_get_moments */
+#define OR3_SERVER_ONE_LANE 2u     /* each wave on one stream (default: split over three streams that overlap) */
 
 /* frame of job `job_id`: samples so far, frame in the job's output layout,
    final = 1 for the last one.  Called on the server thread. */

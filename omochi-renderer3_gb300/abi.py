@@ -29,6 +29,7 @@ OR3_FLAG_KEEP_PATHS = 1
 OR3_FLAG_NO_GRAPH = 4
 OR3_FLAG_TIME_KERNELS = 16
 OR3_FLAG_COUNT_TRAVERSAL = 32
+OR3_FLAG_ONE_LANE = 64
 
 API_VERSION = 1
 
@@ -143,6 +144,7 @@ JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c
 
 OR3_JOB_QUEUED, OR3_JOB_RUNNING, OR3_JOB_DONE, OR3_JOB_CANCELLED, OR3_JOB_FAILED = 0, 1, 2, 3, 4
 OR3_SERVER_KEEP_MOMENTS = 1
+OR3_SERVER_ONE_LANE = 2
 OR3_TUNE_SMEM_NODES = 0x10
 OR3_TUNE_SHADOW_UNSORTED = 0x20
 OR3_TUNE_L2_PERSIST = 0x40

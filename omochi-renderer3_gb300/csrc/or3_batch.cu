@@ -32,12 +32,18 @@ struct BatchBuffers {
   size_t cap_scenes = 0;
   JobDev *jobs = nullptr;
   size_t cap_jobs = 0;
-  Segment *segs = nullptr;
-  size_t cap_segs = 0;
-  WaveInfo *info = nullptr;
-  Segment *segs_host = nullptr;  // pinned staging
-  size_t cap_segs_host = 0;
-  WaveInfo *info_host = nullptr;  // pinned
+  // per wave lane (lane 0: the context's stream and queues; 1, 2: its extra
+  // lanes): the wave's segment table, pinned staging, read-back counters
+  struct Lane {
+    Segment *segs = nullptr;
+    size_t cap_segs = 0;
+    WaveInfo *info = nullptr;
+    Segment *segs_host = nullptr;  // pinned staging
+    size_t cap_segs_host = 0;
+    WaveInfo *info_host = nullptr;  // pinned
+    uint32_t *hc = nullptr;         // pinned
+    cudaEvent_t ev = nullptr;
+  } lanes[3];
   double *frame_dev = nullptr, *frame_pinned = nullptr;
   size_t cap_frame = 0;
   struct JobOut {
@@ -56,10 +62,14 @@ void destroy_batch_state(or3_context *ctx) {
   cudaFree(b->sumsq);
   cudaFree(b->scenes);
   cudaFree(b->jobs);
-  cudaFree(b->segs);
-  cudaFree(b->info);
-  cudaFreeHost(b->segs_host);
-  cudaFreeHost(b->info_host);
+  for (BatchBuffers::Lane &L : b->lanes) {
+    cudaFree(L.segs);
+    cudaFree(L.info);
+    cudaFreeHost(L.segs_host);
+    cudaFreeHost(L.info_host);
+    cudaFreeHost(L.hc);
+    if (L.ev) cudaEventDestroy(L.ev);
+  }
   cudaFree(b->frame_dev);
   cudaFreeHost(b->frame_pinned);
   delete b;
@@ -207,10 +217,28 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   if ((rc = grow_dev(ctx, B.sumsq, B.cap_sumsq, 3 * pixels))) return rc;
   if ((rc = grow_dev(ctx, B.scenes, B.cap_scenes, scenes.size()))) return rc;
   if ((rc = grow_dev(ctx, B.jobs, B.cap_jobs, n))) return rc;
-  if ((rc = grow_dev(ctx, B.segs, B.cap_segs, max_segs))) return rc;
-  if ((rc = grow_pinned(ctx, B.segs_host, B.cap_segs_host, max_segs))) return rc;
-  if (!B.info) OR3_CUDA(ctx, cudaMalloc(&B.info, sizeof(WaveInfo)));
-  if (!B.info_host) OR3_CUDA(ctx, cudaMallocHost(&B.info_host, sizeof(WaveInfo)));
+  // wave lanes (three unless OR3_FLAG_ONE_LANE): each runs its own waves on
+  // its own stream and queues; the lanes' pixel sums are the jobs' (atomic adds)
+  const int nl = (bp->flags & OR3_FLAG_ONE_LANE) || waves.size() < 2 ? 1 : (int)std::min<size_t>(3, waves.size());
+  Queues ql[3];
+  cudaStream_t sl[3];
+  for (int l = 0; l < nl; l++) {
+    BatchBuffers::Lane &L = B.lanes[l];
+    if (l == 0) {
+      ql[0] = make_queues(ctx);
+      sl[0] = ctx->stream;
+    } else {
+      if ((rc = ensure_lane(ctx, l - 1, cap, cap * (split ? 8 : 1), 1))) return rc;
+      ql[l] = lane_queues(ctx->xl[l - 1]);
+      sl[l] = ctx->xl[l - 1].stream;
+    }
+    if ((rc = grow_dev(ctx, L.segs, L.cap_segs, max_segs))) return rc;
+    if ((rc = grow_pinned(ctx, L.segs_host, L.cap_segs_host, max_segs))) return rc;
+    if (!L.info) OR3_CUDA(ctx, cudaMalloc(&L.info, sizeof(WaveInfo)));
+    if (!L.info_host) OR3_CUDA(ctx, cudaMallocHost(&L.info_host, sizeof(WaveInfo)));
+    if (!L.hc) OR3_CUDA(ctx, cudaMallocHost(&L.hc, 4 * sizeof(uint32_t)));
+    if (!L.ev) OR3_CUDA(ctx, cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
+  }
   cudaStream_t st = ctx->stream;
   for (size_t j = 0; j < n; j++) {
     jd[j].sum = B.sum + 3 * outs[j].pix_base;
@@ -220,11 +248,11 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   OR3_CUDA(ctx, cudaMemcpyAsync(B.jobs, jd.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, st));
   OR3_CUDA(ctx, cudaMemsetAsync(B.sum, 0, 3 * pixels * sizeof(double), st));
   OR3_CUDA(ctx, cudaMemsetAsync(B.sumsq, 0, 3 * pixels * sizeof(double), st));
-  OR3_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st));
-  OR3_CUDA(ctx, cudaMemsetAsync(ctx->dstats, 0, 8 * sizeof(unsigned long long), st));
+  for (int l = 0; l < nl; l++) {
+    OR3_CUDA(ctx, cudaMemsetAsync(ql[l].counters, 0, 16 * sizeof(uint32_t), st));
+    OR3_CUDA(ctx, cudaMemsetAsync(ql[l].stats, 0, 8 * sizeof(unsigned long long), st));
+  }
 
-  Batch b{B.scenes, B.jobs, B.segs, B.info};
-  const Queues q = make_queues(ctx);
   const int bps_ext = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, ctx->occ_extend) : ctx->occ_extend;
   const int occ_sh = shadows ? ctx->occ_shade_nee : ctx->occ_shade;  // the instance launch_shade_batch picks
   const int bps_sh = bp->blocks_per_sm ? std::min<int>((int)bp->blocks_per_sm, occ_sh) : occ_sh;
@@ -235,61 +263,106 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   unroll = std::max(2, std::min(unroll, 64));
   unroll += unroll & 1;  // even: the live queue is queue 0 after every replay
 
-  // the bounce loop, captured once per call
-  cudaGraphExec_t gexec = nullptr;
-  const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
-  auto launch_bounces = [&]() {
+  // the bounce loop, captured once per call and lane
+  auto lane_batch = [&](int l) { return Batch{B.scenes, B.jobs, B.lanes[l].segs, B.lanes[l].info}; };
+  auto launch_bounces = [&](int l) {
+    const Batch b = lane_batch(l);
     for (int k = 0; k < unroll; k++) {
       const int in = k & 1;
-      launch_extend_batch(b, q, in, grid_ext, count, st);
-      launch_shade_batch(b, q, in, grid_sh, shadows, st);
-      if (shadows) launch_shadow_batch(b, q, grid_ext, st);
-      launch_reset_count(q, in, st);
+      launch_extend_batch(b, ql[l], in, grid_ext, count, sl[l]);
+      launch_shade_batch(b, ql[l], in, grid_sh, shadows, sl[l]);
+      if (shadows) launch_shadow_batch(b, ql[l], grid_ext, sl[l]);
+      launch_reset_count(ql[l], in, sl[l]);
     }
   };
-  if (use_graph) {
-    cudaGraph_t graph = nullptr;
-    OR3_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    launch_bounces();
-    OR3_CUDA(ctx, cudaStreamEndCapture(st, &graph));
-    cudaError_t e = cudaGraphInstantiate(&gexec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-  }
   struct GraphGuard {
-    cudaGraphExec_t g;
+    cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
     ~GraphGuard() {
-      if (g) cudaGraphExecDestroy(g);
+      for (cudaGraphExec_t x : g)
+        if (x) cudaGraphExecDestroy(x);
     }
-  } guard{gexec};
+  } guard;
+  const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
+  if (use_graph) {
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int l = 0; l < nl; l++) {
+      cudaGraph_t graph = nullptr;
+      OR3_CUDA(ctx, cudaStreamBeginCapture(sl[l], cudaStreamCaptureModeThreadLocal));
+      launch_bounces(l);
+      OR3_CUDA(ctx, cudaStreamEndCapture(sl[l], &graph));
+      cudaError_t e = cudaGraphInstantiate(&guard.g[l], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+  }
 
   or3_render_stats stats{};
   OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-  for (const PlannedWave &w : waves) {
-    std::memcpy(B.segs_host, w.segs.data(), w.segs.size() * sizeof(Segment));
-    B.info_host->nseg = (uint32_t)w.segs.size();
-    B.info_host->ngroups = w.ngroups;
-    B.info_host->num_paths = w.num_paths;
-    OR3_CUDA(ctx, cudaMemcpyAsync(B.segs, B.segs_host, w.segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
-    OR3_CUDA(ctx, cudaMemcpyAsync(B.info, B.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, st));
-    launch_raygen_batch(b, w.num_paths, q, 0, st);
-    for (int rep = 0;; rep++) {
-      if (use_graph) OR3_CUDA(ctx, cudaGraphLaunch(gexec, st));
-      else launch_bounces();
-      OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-      OR3_CUDA(ctx, cudaStreamSynchronize(st));
-      if (ctx->host_counters[2]) {
-        const uint32_t bits = ctx->host_counters[2];
-        cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
+  if (nl > 1) {  // the extra lanes start after the tables and sums above
+    OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+    for (int l = 1; l < nl; l++) OR3_CUDA(ctx, cudaStreamWaitEvent(sl[l], ctx->ev_fork, 0));
+  }
+  auto replay = [&](int l) -> int {
+    BatchBuffers::Lane &L = B.lanes[l];
+    if (use_graph) OR3_CUDA(ctx, cudaGraphLaunch(guard.g[l], sl[l]));
+    else launch_bounces(l);
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.hc, ql[l].counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, sl[l]));
+    OR3_CUDA(ctx, cudaEventRecord(L.ev, sl[l]));
+    return OR3_OK;
+  };
+  // waves in plan order, each to the next free lane; the lanes are visited in turn
+  size_t next_wave = 0;
+  int wave_of[3] = {-1, -1, -1}, reps[3] = {0, 0, 0};
+  auto start = [&](int l) -> int {
+    if (next_wave >= waves.size()) return OR3_OK;
+    const PlannedWave &w = waves[next_wave];
+    BatchBuffers::Lane &L = B.lanes[l];
+    std::memcpy(L.segs_host, w.segs.data(), w.segs.size() * sizeof(Segment));
+    L.info_host->nseg = (uint32_t)w.segs.size();
+    L.info_host->ngroups = w.ngroups;
+    L.info_host->num_paths = w.num_paths;
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.segs, L.segs_host, w.segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, sl[l]));
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.info, L.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, sl[l]));
+    launch_raygen_batch(lane_batch(l), w.num_paths, ql[l], 0, sl[l]);
+    wave_of[l] = (int)next_wave++;
+    reps[l] = 0;
+    return replay(l);
+  };
+  int live = 0;
+  for (int l = 0; l < nl; l++) {
+    if ((rc = start(l))) return rc;
+    if (wave_of[l] >= 0) live++;
+  }
+  while (live > 0) {
+    for (int l = 0; l < nl; l++) {
+      if (wave_of[l] < 0) continue;
+      BatchBuffers::Lane &L = B.lanes[l];
+      OR3_CUDA(ctx, cudaEventSynchronize(L.ev));
+      if (L.hc[2]) {
+        const uint32_t bits = L.hc[2];
+        for (int k = 0; k < nl; k++) cudaStreamSynchronize(sl[k]);
+        for (int k = 0; k < nl; k++) cudaMemsetAsync(ql[k].counters, 0, 16 * sizeof(uint32_t), st);
         cudaStreamSynchronize(st);
         return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x in a batch", bits);
       }
-      if (ctx->host_counters[0] == 0) break;
-      if (rep > (1 << 16)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+      if (L.hc[0] != 0) {
+        if (++reps[l] > (1 << 16)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+        if ((rc = replay(l))) return rc;
+        continue;
+      }
+      const PlannedWave &w = waves[(size_t)wave_of[l]];
+      launch_accumulate_batch(lane_batch(l), w.ngroups, ql[l], sl[l]);
+      stats.waves++;
+      stats.camera_paths += w.num_paths;
+      wave_of[l] = -1;
+      live--;
+      if ((rc = start(l))) return rc;
+      if (wave_of[l] >= 0) live++;
     }
-    launch_accumulate_batch(b, w.ngroups, q, st);
-    stats.waves++;
-    stats.camera_paths += w.num_paths;
+  }
+  for (int l = 1; l < nl; l++) {  // join the extra lanes
+    OR3_CUDA(ctx, cudaEventRecord(B.lanes[l].ev, sl[l]));
+    OR3_CUDA(ctx, cudaStreamWaitEvent(st, B.lanes[l].ev, 0));
   }
   OR3_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
@@ -322,8 +395,12 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
       std::memcpy(job.frame_host, B.frame_pinned, doubles * sizeof(double));
     }
   }
-  unsigned long long hs[8];
-  OR3_CUDA(ctx, cudaMemcpy(hs, ctx->dstats, sizeof(hs), cudaMemcpyDeviceToHost));
+  unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int l = 0; l < nl; l++) {
+    unsigned long long h1[8];
+    OR3_CUDA(ctx, cudaMemcpy(h1, ql[l].stats, sizeof(h1), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 8; k++) hs[k] += h1[k];
+  }
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];
   stats.bounces = hs[2];

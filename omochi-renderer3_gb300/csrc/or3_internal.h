@@ -123,6 +123,9 @@ inline int fail(or3_context *ctx, int code, const char *fmt, ...) {
 // or3_api.cu
 int ensure_queues(or3_context *ctx, size_t paths, size_t rays);
 Queues make_queues(or3_context *ctx);
+// extra wave lane k (0 or 1): stream, queues, counters, pixel sums
+int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixels);
+Queues lane_queues(const or3_context::Lane &L);
 void camera_basis(const or3_camera *c, Camera32 &out);
 int validate_render(or3_context *ctx, const or3_camera *cam, const or3_render_params *prm);
 void fill_render_const(const or3_camera *cam, const or3_render_params *prm, RenderConst &rc);

@@ -75,18 +75,33 @@ struct Server {
   double device_ms = 0, busy_s = 0;
   int error = OR3_OK;
   std::string error_msg;
-  // device tables (fixed capacity: the captured graph holds their addresses)
+  // device tables (fixed capacity: the captured graphs hold their addresses)
   std::map<int32_t, uint32_t> scene_index;
   DevScene *scenes_dev = nullptr;
   JobDev *jobs_dev = nullptr;
   JobDev *jobs_host = nullptr;
-  Segment *segs_dev = nullptr, *segs_host = nullptr;
-  WaveInfo *info_dev = nullptr, *info_host = nullptr;
   uint32_t cap_segs = 0;
+  // Wave lanes: a wave's segments are dealt to the lanes, each with its own
+  // stream, ray queues, segment table and captured bounce loop; the lanes run
+  // at once and join before the frames.  Lane 0 is the context's stream and
+  // queues, lanes 1.. the context's extra lanes.
+  struct Lane {
+    cudaStream_t st = nullptr;
+    Queues q{};
+    Segment *segs_dev = nullptr, *segs_host = nullptr;
+    WaveInfo *info_dev = nullptr, *info_host = nullptr;
+    uint32_t *hc = nullptr;  // pinned: the lane's queue counters, read back per replay
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::vector<Segment> segs;
+    uint64_t used = 0, groups = 0;
+    bool live = false;
+  };
+  std::vector<Lane> lanes;
+  cudaEvent_t ev_jobs = nullptr;
   double *frame_dev = nullptr, *frame_pinned = nullptr;
   size_t cap_frame = 0;
   uint8_t *frame8_dev = nullptr, *frame8_pinned = nullptr;  // 8-bit frames (3 bytes per pixel)
-  cudaGraphExec_t graph = nullptr;
   int unroll = 8;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 
@@ -193,64 +208,104 @@ int run_wave(or3_context *ctx, Server &S, std::vector<SJob *> &act) {
     d.sum = j.sum;
     d.sumsq = j.sumsq;
   }
-  // fair shares, then leftover room
-  std::vector<Segment> segs;
+  // Segments, lane by lane: each lane takes up to cap / lanes paths, fair
+  // shares of the active jobs first, then leftover room.
+  const size_t nl = S.lanes.size();
+  const uint64_t cap_l = std::max<uint64_t>(S.cap / nl, 1);
   std::vector<uint64_t> taken(na, 0);
-  uint64_t used = 0, groups = 0;
-  auto give = [&](size_t k, uint64_t want) {
-    SJob &j = *act[k];
-    while (want >= j.ss2 && j.cursor < j.total && used + j.ss2 <= S.cap && segs.size() < S.cap_segs) {
-      uint32_t pf = 0;
-      const uint64_t pend = pass_end(j, j.cursor, &pf);
-      uint64_t take = std::min<uint64_t>({want, pend - j.cursor, S.cap - used});
-      take = take / j.ss2 * j.ss2;
-      if (take == 0) break;
-      Segment s{};
-      s.g_first = j.cursor;
-      s.job = (uint32_t)k;
-      s.wave_first = (uint32_t)used;
-      s.count = (uint32_t)take;
-      s.pass_first = pf;
-      s.group_first = (uint32_t)groups;
-      segs.push_back(s);
-      used += take;
-      groups += take / j.ss2;
-      j.cursor += take;
-      taken[k] += take;
-      want -= take;
-    }
-  };
-  const uint64_t share = std::max<uint64_t>(S.cap / std::max<size_t>(na, 1), 1);
-  for (size_t k = 0; k < na; k++) give(k, share);
-  for (size_t k = 0; k < na && used < S.cap; k++) give(k, S.cap - used);
-  if (segs.empty()) return OR3_OK;
-
-  std::memcpy(S.segs_host, segs.data(), segs.size() * sizeof(Segment));
-  S.info_host->nseg = (uint32_t)segs.size();
-  S.info_host->ngroups = (uint32_t)groups;
-  S.info_host->num_paths = (uint32_t)used;
-  OR3_CUDA(ctx, cudaMemcpyAsync(S.jobs_dev, S.jobs_host, na * sizeof(JobDev), cudaMemcpyHostToDevice, st));
-  OR3_CUDA(ctx, cudaMemcpyAsync(S.segs_dev, S.segs_host, segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
-  OR3_CUDA(ctx, cudaMemcpyAsync(S.info_dev, S.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, st));
-  const Batch b{S.scenes_dev, S.jobs_dev, S.segs_dev, S.info_dev};
-  const Queues q = make_queues(ctx);
-  OR3_CUDA(ctx, cudaEventRecord(S.e0, st));
-  launch_raygen_batch(b, (uint32_t)used, q, 0, st);
-  for (int rep = 0;; rep++) {
-    OR3_CUDA(ctx, cudaGraphLaunch(S.graph, st));
-    OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    OR3_CUDA(ctx, cudaStreamSynchronize(st));
-    if (ctx->host_counters[2]) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel error bits 0x%x", ctx->host_counters[2]);
-    if (ctx->host_counters[0] == 0) break;
-    if (rep > (1 << 16)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+  uint64_t used_all = 0;
+  for (size_t l = 0; l < nl; l++) {
+    Server::Lane &L = S.lanes[l];
+    std::vector<Segment> &segs = L.segs;
+    segs.clear();
+    uint64_t used = 0, groups = 0;
+    auto give = [&](size_t k, uint64_t want) {
+      SJob &j = *act[k];
+      while (want >= j.ss2 && j.cursor < j.total && used + j.ss2 <= cap_l && segs.size() < S.cap_segs) {
+        uint32_t pf = 0;
+        const uint64_t pend = pass_end(j, j.cursor, &pf);
+        uint64_t take = std::min<uint64_t>({want, pend - j.cursor, cap_l - used});
+        take = take / j.ss2 * j.ss2;
+        if (take == 0) break;
+        Segment s{};
+        s.g_first = j.cursor;
+        s.job = (uint32_t)k;
+        s.wave_first = (uint32_t)used;
+        s.count = (uint32_t)take;
+        s.pass_first = pf;
+        s.group_first = (uint32_t)groups;
+        segs.push_back(s);
+        used += take;
+        groups += take / j.ss2;
+        j.cursor += take;
+        taken[k] += take;
+        want -= take;
+      }
+    };
+    const uint64_t share = std::max<uint64_t>(cap_l / std::max<size_t>(na, 1), 1);
+    for (size_t k = 0; k < na; k++) give(k, share);
+    for (size_t k = 0; k < na && used < cap_l; k++) give(k, cap_l - used);
+    L.used = used;
+    L.groups = groups;
+    used_all += used;
   }
-  launch_accumulate_batch(b, (uint32_t)groups, q, st);
+  if (used_all == 0) return OR3_OK;
+
+  OR3_CUDA(ctx, cudaEventRecord(S.e0, st));
+  OR3_CUDA(ctx, cudaMemcpyAsync(S.jobs_dev, S.jobs_host, na * sizeof(JobDev), cudaMemcpyHostToDevice, st));
+  OR3_CUDA(ctx, cudaEventRecord(S.ev_jobs, st));
+  int live = 0;
+  for (size_t l = 0; l < nl; l++) {
+    Server::Lane &L = S.lanes[l];
+    L.live = false;
+    if (L.segs.empty()) continue;
+    if (l) OR3_CUDA(ctx, cudaStreamWaitEvent(L.st, S.ev_jobs, 0));
+    std::memcpy(L.segs_host, L.segs.data(), L.segs.size() * sizeof(Segment));
+    L.info_host->nseg = (uint32_t)L.segs.size();
+    L.info_host->ngroups = (uint32_t)L.groups;
+    L.info_host->num_paths = (uint32_t)L.used;
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.segs_dev, L.segs_host, L.segs.size() * sizeof(Segment), cudaMemcpyHostToDevice,
+                                  L.st));
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.info_dev, L.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, L.st));
+    const Batch b{S.scenes_dev, S.jobs_dev, L.segs_dev, L.info_dev};
+    launch_raygen_batch(b, (uint32_t)L.used, L.q, 0, L.st);
+    OR3_CUDA(ctx, cudaGraphLaunch(L.graph, L.st));
+    OR3_CUDA(ctx, cudaMemcpyAsync(L.hc, L.q.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, L.st));
+    OR3_CUDA(ctx, cudaEventRecord(L.ev, L.st));
+    L.live = true;
+    live++;
+  }
+  // replay each lane's bounce loop until its queue is empty, visiting the
+  // lanes in turn (the others keep running meanwhile)
+  for (int rep = 0; live > 0; rep++) {
+    if (rep > (1 << 18)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+    for (size_t l = 0; l < nl; l++) {
+      Server::Lane &L = S.lanes[l];
+      if (!L.live) continue;
+      OR3_CUDA(ctx, cudaEventSynchronize(L.ev));
+      if (L.hc[2]) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel error bits 0x%x", L.hc[2]);
+      if (L.hc[0] == 0) {
+        const Batch b{S.scenes_dev, S.jobs_dev, L.segs_dev, L.info_dev};
+        launch_accumulate_batch(b, (uint32_t)L.groups, L.q, L.st);
+        if (l) {
+          OR3_CUDA(ctx, cudaEventRecord(L.ev, L.st));
+          OR3_CUDA(ctx, cudaStreamWaitEvent(st, L.ev, 0));
+        }
+        L.live = false;
+        live--;
+        continue;
+      }
+      OR3_CUDA(ctx, cudaGraphLaunch(L.graph, L.st));
+      OR3_CUDA(ctx, cudaMemcpyAsync(L.hc, L.q.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, L.st));
+      OR3_CUDA(ctx, cudaEventRecord(L.ev, L.st));
+    }
+  }
   OR3_CUDA(ctx, cudaEventRecord(S.e1, st));
   OR3_CUDA(ctx, cudaEventSynchronize(S.e1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, S.e0, S.e1);
   S.device_ms += ms;
-  S.paths += used;
+  S.paths += used_all;
   S.waves++;
   // progressive and final frames
   const uint64_t every = S.p.frame_every_samples ? S.p.frame_every_samples : 16;
@@ -392,14 +447,20 @@ void destroy_server_state(or3_context *ctx) {
     free_job_device(kv.second);
     delete kv.second;
   }
-  if (S->graph) cudaGraphExecDestroy(S->graph);
+  for (Server::Lane &L : S->lanes) {
+    if (L.st) cudaStreamSynchronize(L.st);
+    if (L.graph) cudaGraphExecDestroy(L.graph);
+    cudaFree(L.segs_dev);
+    cudaFreeHost(L.segs_host);
+    cudaFree(L.info_dev);
+    cudaFreeHost(L.info_host);
+    cudaFreeHost(L.hc);
+    if (L.ev) cudaEventDestroy(L.ev);
+  }
+  if (S->ev_jobs) cudaEventDestroy(S->ev_jobs);
   cudaFree(S->scenes_dev);
   cudaFree(S->jobs_dev);
   cudaFreeHost(S->jobs_host);
-  cudaFree(S->segs_dev);
-  cudaFreeHost(S->segs_host);
-  cudaFree(S->info_dev);
-  cudaFreeHost(S->info_host);
   cudaFree(S->frame_dev);
   cudaFreeHost(S->frame_pinned);
   cudaFree(S->frame8_dev);
@@ -458,40 +519,59 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
   S->budget = S->p.hbm_budget_bytes ? S->p.hbm_budget_bytes : free_b / 2;
   if (cudaMalloc(&S->scenes_dev, scenes.size() * sizeof(DevScene)) != cudaSuccess ||
       cudaMalloc(&S->jobs_dev, maxa * sizeof(JobDev)) != cudaSuccess ||
-      cudaMallocHost(&S->jobs_host, maxa * sizeof(JobDev)) != cudaSuccess ||
-      cudaMalloc(&S->segs_dev, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
-      cudaMallocHost(&S->segs_host, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
-      cudaMalloc(&S->info_dev, sizeof(WaveInfo)) != cudaSuccess ||
-      cudaMallocHost(&S->info_host, sizeof(WaveInfo)) != cudaSuccess)
+      cudaMallocHost(&S->jobs_host, maxa * sizeof(JobDev)) != cudaSuccess)
     return bail(fail(ctx, OR3_ERR_OUT_OF_MEMORY, "server tables"));
   cudaEventCreate(&S->e0);
   cudaEventCreate(&S->e1);
+  cudaEventCreateWithFlags(&S->ev_jobs, cudaEventDisableTiming);
+  const int nl = (S->p.flags & OR3_SERVER_ONE_LANE) ? 1 : 3;
+  S->lanes.resize(nl);
+  for (int l = 0; l < nl; l++) {
+    Server::Lane &L = S->lanes[l];
+    if (l == 0) {
+      L.st = ctx->stream;
+      L.q = make_queues(ctx);
+    } else {
+      if ((rc = ensure_lane(ctx, l - 1, S->cap, S->cap * (S->split ? 8 : 1), 1))) return bail(rc);
+      L.st = ctx->xl[l - 1].stream;
+      L.q = lane_queues(ctx->xl[l - 1]);
+    }
+    if (cudaMalloc(&L.segs_dev, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
+        cudaMallocHost(&L.segs_host, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
+        cudaMalloc(&L.info_dev, sizeof(WaveInfo)) != cudaSuccess ||
+        cudaMallocHost(&L.info_host, sizeof(WaveInfo)) != cudaSuccess ||
+        cudaMallocHost(&L.hc, 4 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(ctx, OR3_ERR_OUT_OF_MEMORY, "server lane tables"));
+    cudaMemsetAsync(L.q.counters, 0, 16 * sizeof(uint32_t), L.st);
+    cudaMemsetAsync(L.q.stats, 0, 8 * sizeof(unsigned long long), L.st);
+  }
   cudaStream_t st = ctx->stream;
   if (cudaMemcpy(S->scenes_dev, scenes.data(), scenes.size() * sizeof(DevScene), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(ctx, OR3_ERR_CUDA, "scene table upload"));
-  cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st);
-  cudaMemsetAsync(ctx->dstats, 0, 8 * sizeof(unsigned long long), st);
-  // captured bounce loop
-  const Batch b{S->scenes_dev, S->jobs_dev, S->segs_dev, S->info_dev};
-  const Queues q = make_queues(ctx);
+  // one captured bounce loop per lane (its queues and segment table)
   S->unroll = S->p.graph_bounces ? (int)S->p.graph_bounces : 8;
   S->unroll = std::max(2, std::min(S->unroll, 64));
   S->unroll += S->unroll & 1;
-  cudaGraph_t graph = nullptr;
-  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-    return bail(fail(ctx, OR3_ERR_CUDA, "graph capture"));
-  for (int k = 0; k < S->unroll; k++) {
-    const int in = k & 1;
-    launch_extend_batch(b, q, in, ctx->num_sms * ctx->occ_extend, false, st);
-    launch_shade_batch(b, q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows, st);
-    if (shadows) launch_shadow_batch(b, q, ctx->num_sms * ctx->occ_extend, st);
-    launch_reset_count(q, in, st);
+  for (Server::Lane &L : S->lanes) {
+    const Batch b{S->scenes_dev, S->jobs_dev, L.segs_dev, L.info_dev};
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamSynchronize(L.st) != cudaSuccess ||
+        cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return bail(fail(ctx, OR3_ERR_CUDA, "graph capture"));
+    for (int k = 0; k < S->unroll; k++) {
+      const int in = k & 1;
+      launch_extend_batch(b, L.q, in, ctx->num_sms * ctx->occ_extend, false, L.st);
+      launch_shade_batch(b, L.q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows, L.st);
+      if (shadows) launch_shadow_batch(b, L.q, ctx->num_sms * ctx->occ_extend, L.st);
+      launch_reset_count(L.q, in, L.st);
+    }
+    if (cudaStreamEndCapture(L.st, &graph) != cudaSuccess || cudaGraphInstantiate(&L.graph, graph, 0) != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return bail(fail(ctx, OR3_ERR_CUDA, "graph instantiate"));
+    }
+    cudaGraphDestroy(graph);
   }
-  if (cudaStreamEndCapture(st, &graph) != cudaSuccess || cudaGraphInstantiate(&S->graph, graph, 0) != cudaSuccess) {
-    if (graph) cudaGraphDestroy(graph);
-    return bail(fail(ctx, OR3_ERR_CUDA, "graph instantiate"));
-  }
-  cudaGraphDestroy(graph);
   if (cudaStreamSynchronize(st) != cudaSuccess) return bail(fail(ctx, OR3_ERR_CUDA, "server start"));
   S->th = std::thread(worker, ctx);
   return OR3_OK;

@@ -207,8 +207,8 @@ __device__ __forceinline__ void trav_init(TravState &s, V3 o, V3 d, float tmax, 
   s.sp = 0;
 }
 
-// Traversal stack for trav_step_inline: put(i, entry, key), ent(i), key(i)
-// over the thread's arrays (local memory).
+// Traversal stack for trav_step_inline: put(i, entry, key), pair(i) =
+// (entry, key bits), over the thread's arrays (local memory).
 struct LocalStack {
   uint32_t *e;
   float *t;
@@ -216,16 +216,24 @@ struct LocalStack {
     e[i] = ee;
     t[i] = tt;
   }
-  __device__ __forceinline__ uint32_t ent(int i) const { return e[i]; }
-  __device__ __forceinline__ float key(int i) const { return t[i]; }
+  __device__ __forceinline__ uint2 pair(int i) const { return make_uint2(e[i], __float_as_uint(t[i])); }
+};
+
+// The same with (entry, key) side by side: one 8-byte store per push and one
+// 8-byte load per pop.
+struct PairStack {
+  uint2 *s;
+  __device__ __forceinline__ void put(int i, uint32_t ee, float tt) { s[i] = make_uint2(ee, __float_as_uint(tt)); }
+  __device__ __forceinline__ uint2 pair(int i) const { return s[i]; }
 };
 
 template <class STK>
 __device__ __forceinline__ bool trav_pop_stk(TravState &s, const STK &stk) {
   while (s.sp > 0) {
     s.sp--;
-    if (stk.key(s.sp) <= s.tmax * 1.0000010f) {
-      s.entry = stk.ent(s.sp);
+    const uint2 p = stk.pair(s.sp);
+    if (__uint_as_float(p.y) <= s.tmax * 1.0000010f) {
+      s.entry = p.x;
       return true;
     }
   }

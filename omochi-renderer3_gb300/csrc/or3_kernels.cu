@@ -98,7 +98,8 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
                                                  uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
-  LocalStack stk{stk_e, stk_t};
+  uint2 stk_p[kStackSize];
+  PairStack stk{stk_p};
   TravState st;
   uint32_t r = kNoEntry;
   bool drained = false;  // warp-uniform: the shared fetch counter has passed n
@@ -126,8 +127,8 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
     }
     if (r != kNoEntry) {
       const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                  : trav_step_inline<ANY, COUNT, SORT, LocalStack, FN>(S, st, stk, snodes, ns,
-                                                                                       cnt, err);
+                                  : trav_step_inline<ANY, COUNT, SORT, PairStack, FN>(S, st, stk, snodes, ns,
+                                                                                      cnt, err);
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;
@@ -856,9 +857,8 @@ __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
 template <bool ANY, bool COUNT, class Src, class Sink>
 __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t *fetch, const Src &src,
                                             const Sink &sink, uint32_t *cnt, uint32_t *err) {
-  uint32_t stk_e[kStackSize];
-  float stk_t[kStackSize];
-  LocalStack stk{stk_e, stk_t};
+  uint2 stk_p[kStackSize];
+  PairStack stk{stk_p};
   TravState st;
   const DevScene *sp = nullptr;
   uint32_t r = kNoEntry;
@@ -887,7 +887,7 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
       break;
     }
     if (r != kNoEntry) {
-      if (trav_step_inline<ANY, COUNT>(*sp, st, stk, nullptr, 0u, cnt, err)) {
+      if (trav_step_inline<ANY, COUNT, true, PairStack>(*sp, st, stk, nullptr, 0u, cnt, err)) {
         sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);
         r = kNoEntry;
       }
@@ -914,7 +914,7 @@ struct BatchShadowSrc {
 };
 
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in) {
+__global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int in) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&q.stats[0], (unsigned long long)n);
@@ -939,7 +939,7 @@ __global__ void __launch_bounds__(256) k_extend_batch(Batch b, Queues q, int in)
   }
 }
 
-__global__ void __launch_bounds__(256) k_shadow_batch(Batch b, Queues q) {
+__global__ void __launch_bounds__(256, 4) k_shadow_batch(Batch b, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
   batch_trace<true, false>(b, n, &q.counters[6], BatchShadowSrc{q.sorig, q.sdir, q.scontrib},

@@ -228,11 +228,12 @@ class Context:
 
     # ---- served form
     def server_start(self, *, wave_paths=0, hbm_budget_bytes=0, max_active_jobs=0, frame_every_samples=0,
-                     graph_bounces=0, keep_moments=False, on_frame=None, rgb8=False):
+                     graph_bounces=0, keep_moments=False, on_frame=None, rgb8=False, one_lane=False):
         """rgb8: frames encoded to 8-bit on the device (or3_server_start8); on_frame then
-        receives uint8 images."""
+        receives uint8 images.  one_lane: every wave on one stream."""
         p = abi.ServerParamsC(wave_paths, hbm_budget_bytes, max_active_jobs, frame_every_samples, graph_bounces,
-                              abi.OR3_SERVER_KEEP_MOMENTS if keep_moments else 0)
+                              (abi.OR3_SERVER_KEEP_MOMENTS if keep_moments else 0) |
+                              (abi.OR3_SERVER_ONE_LANE if one_lane else 0))
         if rgb8:
             def _cb8(user, job_id, samples, rgb, w, h, final):
                 if on_frame is not None:

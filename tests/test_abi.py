@@ -30,6 +30,17 @@ def test_library_builds_and_exports_every_declared_symbol(pkg):
     assert set(declared_functions()) <= set(pkg.abi.PROTOTYPES), set(declared_functions()) - set(pkg.abi.PROTOTYPES)
 
 
+def test_python_constants_match_the_header(pkg):
+    """Every OR3_* integer constant of include/or3.h has the same value in abi.py."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    defines = dict(re.findall(r"#define\s+(OR3_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?\b", src))
+    assert len(defines) > 30
+    missing = [k for k in defines if not hasattr(pkg.abi, k)]
+    assert not missing, missing
+    wrong = {k: (v, getattr(pkg.abi, k)) for k, v in defines.items() if int(v, 0) != getattr(pkg.abi, k)}
+    assert not wrong, wrong
+
+
 def test_library_loads_without_a_gpu(pkg):
     lib = ctypes.CDLL(pkg.build.build_library())
     lib.or3_api_version.restype = ctypes.c_int
@@ -49,7 +60,7 @@ int main(void) {
   S(or3_camera) O(or3_camera, position) O(or3_camera, aperture_radius)
   S(or3_render_params) O(or3_render_params, seed) O(or3_render_params, flags)
   S(or3_render_stats) O(or3_render_stats, render_ms) O(or3_render_stats, passes)
-  S(or3_scene_info) O(or3_scene_info, build_ms) O(or3_scene_info, tree_depth)
+  S(or3_scene_info) O(or3_scene_info, build_ms) O(or3_scene_info, tree_depth) O(or3_scene_info, flatten_ms)
   return 0;
 }
 """

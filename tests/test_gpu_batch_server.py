@@ -40,12 +40,14 @@ def _plain(ctx, sid, cam, st):
     return s, q, n, img
 
 
-@pytest.mark.parametrize("wave_paths", [0, 3000])
-def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths):
+@pytest.mark.parametrize("wave_paths,flags", [(0, 0), (3000, 0), (3000, 64)])
+def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags):
+    """flags 64 = OR3_FLAG_ONE_LANE (every wave on one stream; the default
+    deals waves to three lanes)."""
     sids, jobs = _jobs(pkg, ctx)
     try:
         alone = [_plain(ctx, *j) for j in jobs]
-        stats, frames = ctx.render_batch(jobs, frames=True, wave_paths=wave_paths)
+        stats, frames = ctx.render_batch(jobs, frames=True, wave_paths=wave_paths, flags=flags)
         if wave_paths:
             assert stats["waves"] > 3  # jobs really were cut and mixed across waves
         for k, (sid, cam, st) in enumerate(jobs):
@@ -91,7 +93,8 @@ def test_batch_rejects_bad_jobs(pkg, ctx):
     ctx.release(sid)
 
 
-def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx):
+@pytest.mark.parametrize("one_lane", [False, True])
+def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx, one_lane):
     sids, jobs = _jobs(pkg, ctx)
     alone = [_plain(ctx, *j) for j in jobs]
     frames = defaultdict(list)
@@ -101,7 +104,8 @@ def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx):
         with lock:
             frames[jid].append((samples, final, img))
 
-    ctx.server_start(keep_moments=True, frame_every_samples=1, wave_paths=1 << 16, on_frame=on_frame)
+    ctx.server_start(keep_moments=True, frame_every_samples=1, wave_paths=1 << 16, on_frame=on_frame,
+                     one_lane=one_lane)
     try:
         ids = [ctx.server_submit(*jobs[0][:2], **jobs[0][2])]
         time.sleep(0.05)  # later arrivals join while the first job runs

@@ -118,9 +118,15 @@ class Context:
         self._check(self.lib.or3_get_stats(self.h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in abi.RenderStatsC._fields_}
 
-    def frame(self, width, height, layout=abi.OR3_LAYOUT_REFERENCE):
+    def frame(self, width, height, layout=abi.OR3_LAYOUT_REFERENCE, out=None):
+        """The last frame (2W x H x 3 doubles in the reference layout).  out: a
+        C-contiguous float64 array of that shape to fill instead of a new one
+        (repeated reads then skip the page faults of a fresh buffer)."""
         w = width * (2 if layout == abi.OR3_LAYOUT_REFERENCE else 1)
-        out = np.zeros((height, w, 3), np.float64)
+        if out is None:
+            out = np.zeros((height, w, 3), np.float64)
+        elif out.shape != (height, w, 3) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape %s" % ((height, w, 3),))
         s = ctypes.c_int32()
         self._check(self.lib.or3_get_frame(self.h, out.ctypes.data_as(abi.f64p), out.size, ctypes.byref(s)))
         return out, s.value

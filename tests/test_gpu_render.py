@@ -127,6 +127,20 @@ def test_frame_layout_and_progressive_callbacks(pkg, ctx):
     assert n == 7 * 4
 
 
+def test_frame_into_the_callers_buffer(pkg, ctx):
+    sd, cam, _ = pkg.workloads.cornell_box(16, 12)
+    sid = ctx.upload(sd)
+    ctx.render(sid, cam, supersamples=2, seed=3)
+    ctx.release(sid)
+    ref, n = ctx.frame(cam.width, cam.height)
+    buf = np.full((cam.height, 2 * cam.width, 3), -1.0)
+    out, n2 = ctx.frame(cam.width, cam.height, out=buf)
+    assert out is buf and n2 == n
+    np.testing.assert_array_equal(buf, ref)
+    with pytest.raises(ValueError):
+        ctx.frame(cam.width, cam.height, out=np.zeros((cam.height, cam.width, 3)))
+
+
 def test_compact_layout(pkg, ctx):
     sd, cam, _ = pkg.workloads.cornell_box(20, 10)
     sid = ctx.upload(sd)

@@ -92,6 +92,15 @@ __device__ __forceinline__ double box_area(const float lo[3], const float hi[3])
   return dx * dy + dy * dz + dz * dx;
 }
 
+// The same surface measure in FP32: the device build compares SAH costs
+// scaled by the parent's area (no division) in FP32, since GB300's FP64 pipe
+// is a small fraction of its FP32 rate.
+__device__ __forceinline__ float box_area_f(const float lo[3], const float hi[3]) {
+  if (!(lo[0] <= hi[0])) return 0.f;
+  const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
 __device__ __forceinline__ int ceil_log2(uint64_t v) {
   int r = 0;
   while ((uint64_t(1) << r) < v) r++;
@@ -254,9 +263,10 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
   d.scale = 0.f;
   const int need = ceil_log2((t.count + leaf_max - 1) / leaf_max);
   if (t.depth + need < kMaxBinaryDepth) {
-    const double parent = box_area(lo, hi);
-    double best = DBL_MAX;
-    double rarea[kBins];
+    // cost x parent area: ct * A + A_left * n_left + A_right * n_right
+    const float parent = fmaxf(box_area_f(lo, hi), 1e-30f), ctp = (float)ct * parent;
+    float best = FLT_MAX;
+    float rarea[kBins];
     uint32_t rcnt[kBins];
     const uint32_t *B = bins + (size_t)kBinWords * ti;
     for (int a = 0; a < 3; a++) {
@@ -273,7 +283,7 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
           }
         }
         cnt += w[6];
-        rarea[b] = box_area(alo, ahi);
+        rarea[b] = box_area_f(alo, ahi);
         rcnt[b] = cnt;
       }
       for (int k = 0; k < 3; k++) {
@@ -291,7 +301,7 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
         }
         cnt += w[6];
         if (cnt == 0 || rcnt[b + 1] == 0) continue;
-        const double cost = ct + (box_area(alo, ahi) * cnt + rarea[b + 1] * rcnt[b + 1]) / fmax(parent, 1e-30);
+        const float cost = ctp + box_area_f(alo, ahi) * (float)cnt + rarea[b + 1] * (float)rcnt[b + 1];
         if (cost < best) {
           best = cost;
           d.axis = a;
@@ -568,11 +578,11 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
       }
       __syncwarp();
       // SAH over the 3 x 15 split candidates, one bin per lane: prefix and
-      // suffix unions by shuffle scans (min / max are exact, so the unions and
-      // the double costs are the sequential evaluation's, bit for bit); ties
-      // go to the lowest (axis, bin) like a sequential scan with a strict <
-      const double parent = box_area(lo, hi);
-      double bestc = DBL_MAX;
+      // suffix unions by shuffle scans (min / max are exact); costs scaled by
+      // the parent's area in FP32; ties go to the lowest (axis, bin) like a
+      // sequential scan with a strict <
+      const float parent = fmaxf(box_area_f(lo, hi), 1e-30f), ctp = (float)ct * parent;
+      float bestc = FLT_MAX;
       uint32_t bidx = 0xFFFFFFFFu, bcnt = 0;
       for (int a = 0; a < 3; a++) {
         if (!(chi[a] - clo[a] > 0.f)) continue;
@@ -622,7 +632,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
         }
         const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc2, 1);
         if (lane < (uint32_t)kBins - 1 && pc != 0 && rc != 0) {
-          const double cost = ct + (box_area(plo, phi) * pc + box_area(rlo, rhi) * rc) / fmax(parent, 1e-30);
+          const float cost = ctp + box_area_f(plo, phi) * (float)pc + box_area_f(rlo, rhi) * (float)rc;
           if (cost < bestc) {
             bestc = cost;
             bidx = (uint32_t)(a * kBins) + lane;
@@ -632,7 +642,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double c2 = __shfl_xor_sync(0xFFFFFFFFu, bestc, o);
+        const float c2 = __shfl_xor_sync(0xFFFFFFFFu, bestc, o);
         const uint32_t i2 = __shfl_xor_sync(0xFFFFFFFFu, bidx, o), n2 = __shfl_xor_sync(0xFFFFFFFFu, bcnt, o);
         if (c2 < bestc || (c2 == bestc && i2 < bidx)) {
           bestc = c2;
@@ -645,7 +655,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(uint32_t nsmall, con
         bin = (int)(bidx % kBins);
         nleft = bcnt;
       }
-      if (t.count <= (uint32_t)leaf_max && (axis < 0 || (double)t.count <= bestc)) mode = 2;
+      if (t.count <= (uint32_t)leaf_max && (axis < 0 || (float)t.count * parent <= bestc)) mode = 2;
       else if (axis < 0) mode = 1;
       if (axis >= 0) scale = sc[axis];
     }

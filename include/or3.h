@@ -192,6 +192,7 @@ typedef struct or3_render_params {
 #define OR3_TUNE_SHADE_NEE_OCC4 0x80u  /* or3_render: light-sampling shade kernel at 64 registers, 4 blocks/SM */
 #define OR3_TUNE_ONE_LANE 0x100u       /* or3_render: all waves on one stream (no overlap of waves) */
 #define OR3_TUNE_TWO_LANES 0x200u      /* or3_render: waves round robin over two streams instead of three */
+#define OR3_TUNE_FOUR_LANES 0x400u     /* or3_render: waves round robin over four streams instead of three */
 
 /* Called after each pass, like PathTracer's RenderingFinishCallbackFunction
    (src/renderer/PathTracer.h:21): samples so far, the frame in the requested

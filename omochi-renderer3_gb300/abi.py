@@ -153,6 +153,7 @@ OR3_TUNE_L2_PERSIST = 0x40
 OR3_TUNE_SHADE_NEE_OCC4 = 0x80
 OR3_TUNE_ONE_LANE = 0x100
 OR3_TUNE_TWO_LANES = 0x200
+OR3_TUNE_FOUR_LANES = 0x400
 
 # name -> (restype, argtypes); every function declared in include/or3.h
 PROTOTYPES = {

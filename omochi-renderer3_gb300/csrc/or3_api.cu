@@ -438,7 +438,8 @@ int or3_context_create(int device, or3_context **out) {
   }
   if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
-  if (cudaMallocHost(&ctx->host_counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
+  // pinned read-back counters: lane 0 at [0, 4), extra lane k at [8 + 4k, 12 + 4k)
+  if (cudaMallocHost(&ctx->host_counters, 32 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   cudaMemset(ctx->counters, 0, 16 * sizeof(uint32_t));
   cudaMemset(ctx->dstats, 0, 8 * sizeof(unsigned long long));
   cudaEventCreate(&ctx->ev0);
@@ -477,7 +478,7 @@ int or3_context_destroy(or3_context *ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : ctx->kpool) cudaEventDestroy(e);
   if (ctx->stage) cudaFreeHost(ctx->stage);
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < kExtraLanes; k++) {
     or3_context::Lane &L = ctx->xl[k];
     if (L.stream) cudaStreamSynchronize(L.stream);
     for (int j = 0; j < 2; j++) {
@@ -1063,9 +1064,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // nothing per wave or per kernel is read back)
   const bool multi = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
                      !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
-  const int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : 2;
+  const int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : (prm->tuning & OR3_TUNE_FOUR_LANES) ? 3 : 2;
   const bool two = nx > 0;
-  Queues qx[2] = {};
+  Queues qx[kExtraLanes] = {};
   for (int k = 0; k < nx; k++) {
     or3_context::Lane &L = ctx->xl[k];
     if ((rc = ensure_lane(ctx, k, max_wave_paths, rays, npix))) return rc;
@@ -1079,7 +1080,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   or3_render_stats stats{};
   ctx->moments_valid = false;
   ctx->last_kept_paths = (prm->flags & OR3_FLAG_KEEP_PATHS) != 0;
-  std::memset(ctx->host_counters, 0, 16 * sizeof(uint32_t));  // no stale error bits from an earlier render
+  std::memset(ctx->host_counters, 0, 32 * sizeof(uint32_t));  // no stale error bits from an earlier render
   auto wall0 = std::chrono::steady_clock::now();
   int32_t prev = 0;
   int passes = 0;

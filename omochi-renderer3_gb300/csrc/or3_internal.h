@@ -30,6 +30,9 @@ struct Server;        // or3_batch.cu
 
 }  // namespace or3
 
+// extra wave lanes a context can hold (or3_render uses two by default)
+constexpr int kExtraLanes = 3;
+
 struct or3_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -92,8 +95,8 @@ struct or3_context {
     unsigned long long *dstats = nullptr;
     double *pix_sum = nullptr, *pix_sumsq = nullptr;
     size_t cap_paths = 0, cap_rays = 0, cap_pixels = 0;
-  } xl[2];
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  } xl[kExtraLanes];
+  cudaEvent_t ev_fork = nullptr, ev_join[kExtraLanes] = {};
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

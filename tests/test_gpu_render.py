@@ -182,9 +182,9 @@ def test_waves_do_not_change_the_image(pkg, ctx):
     np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("nee,tuning", [(False, 0), (True, 0), (True, 0x200)])
+@pytest.mark.parametrize("nee,tuning", [(False, 0), (True, 0), (True, 0x200), (True, 0x400)])
 def test_wave_lanes_match_one(pkg, ctx, nee, tuning):
-    """Waves run round robin on three (or two, 0x200) streams with their own
+    """Waves run round robin on three (two: 0x200, four: 0x400) streams with their own
     queues and pixel sums, merged at the end of each pass: the image, the moments and the ray counts
     equal the one-stream render's (up to the order of float additions: FP64
     pixel sums, and FP32 atomics of light samples into a path's radiance)."""

@@ -1150,7 +1150,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           OR3_CUDA(ctx, cudaStreamSynchronize(st));
           if (ctx->host_counters[in] == 0 || ctx->host_counters[2] || chunks > 100000) break;
         }
-        launch_accumulate(ql, w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, 152 * 64), block, sl);
+        launch_accumulate(ql, w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, (uint64_t)ctx->num_sms * 64),
+                          block, sl);
         stats.waves++;
         stats.camera_paths += w.num_paths;
         ctx->last_wave_paths = w.num_paths;
@@ -1164,7 +1165,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       or3_context::Lane &L = ctx->xl[k];
       OR3_CUDA(ctx, cudaEventRecord(ctx->ev_join[k], L.stream));
       OR3_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join[k], 0));
-      launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, L.pix_sum, L.pix_sumsq, st);
+      launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, L.pix_sum, L.pix_sumsq, ctx->num_sms * 16, st);
       OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8 + 4 * k, L.counters, 4 * sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, st));
     }

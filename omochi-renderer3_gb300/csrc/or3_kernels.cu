@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(256) k_trace_occluded(DevScene S, uint32_t n, 
                                    nullptr, &counters[2]);
 }
 
-int g_query_grid = 152 * 4;
+int g_query_grid = 1;  // set from the device's SM count and occupancy when a context is created
 
 // ---------------------------------------------------------------- batched form kernels
 
@@ -1012,9 +1012,9 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
     k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
 }
 
-void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, cudaStream_t st) {
+void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st) {
   const size_t g = (n + 255) / 256;
-  if (n) k_merge_sums<<<(unsigned)(g < 152 * 16 ? g : 152 * 16), 256, 0, st>>>(n, a, aq, b, bq);
+  if (n) k_merge_sums<<<(unsigned)(g < (size_t)max_grid ? g : (size_t)max_grid), 256, 0, st>>>(n, a, aq, b, bq);
 }
 
 void launch_reset_count(const Queues &q, int which, cudaStream_t st) {

@@ -131,7 +131,7 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
                   int grid, int block, cudaStream_t st, bool nee4 = false);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 // a += b, b = 0 over n doubles (sums and sums of squares)
-void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, cudaStream_t st);
+void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st);

@@ -222,6 +222,8 @@ typedef struct or3_render_stats {
   /* OR3_FLAG_TIME_KERNELS: the shadow-ray (any-hit) kernel, next-event estimation only */
   double shadow_ms;
   uint64_t shadow_launches;
+  uint32_t lanes;          /* wave lanes (streams) the render used */
+  uint32_t reserved;
 } or3_render_stats;
 
 typedef struct or3_scene_info {

@@ -314,6 +314,23 @@ int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixel
   return OR3_OK;
 }
 
+void free_lane_buffers(or3_context::Lane &L) {
+  for (int k = 0; k < 2; k++) {
+    cudaFree(L.qorig[k]);
+    cudaFree(L.qdir[k]);
+    cudaFree(L.qbeta[k]);
+    L.qorig[k] = L.qdir[k] = L.qbeta[k] = nullptr;
+  }
+  for (float4 **p : {&L.hits, &L.pathL, &L.sorig, &L.sdir, &L.scontrib}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(L.pix_sum);
+  cudaFree(L.pix_sumsq);
+  L.pix_sum = L.pix_sumsq = nullptr;
+  L.cap_paths = L.cap_rays = L.cap_pixels = 0;
+}
+
 Queues lane_queues(const or3_context::Lane &L) {
   Queues q{};
   for (int k = 0; k < 2; k++) {
@@ -1064,18 +1081,27 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // nothing per wave or per kernel is read back)
   const bool multi = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
                      !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
-  const int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : (prm->tuning & OR3_TUNE_FOUR_LANES) ? 3 : 2;
-  const bool two = nx > 0;
+  int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : (prm->tuning & OR3_TUNE_FOUR_LANES) ? 3 : 2;
   Queues qx[kExtraLanes] = {};
   for (int k = 0; k < nx; k++) {
     or3_context::Lane &L = ctx->xl[k];
-    if ((rc = ensure_lane(ctx, k, max_wave_paths, rays, npix))) return rc;
+    if ((rc = ensure_lane(ctx, k, max_wave_paths, rays, npix))) {
+      if (rc != OR3_ERR_OUT_OF_MEMORY) return rc;
+      // no room for another lane's queues: render on the lanes that fit
+      cudaGetLastError();
+      free_lane_buffers(L);
+      ctx->err.clear();
+      nx = k;
+      break;
+    }
     qx[k] = lane_queues(L);
     OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sum, 0, npix * 3 * sizeof(double), st));
     OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sumsq, 0, npix * 3 * sizeof(double), st));
     OR3_CUDA(ctx, cudaMemsetAsync(L.counters, 0, 16 * sizeof(uint32_t), st));
     OR3_CUDA(ctx, cudaMemsetAsync(L.dstats, 0, 8 * sizeof(unsigned long long), st));
   }
+
+  const bool two = nx > 0;
 
   or3_render_stats stats{};
   ctx->moments_valid = false;
@@ -1235,6 +1261,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     OR3_CUDA(ctx, cudaMemcpy(h1, ctx->xl[k].dstats, sizeof(h1), cudaMemcpyDeviceToHost));
     for (int j = 0; j < 8; j++) hs[j] += h1[j];
   }
+  stats.lanes = (uint32_t)(1 + nx);
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];
   stats.bounces = hs[2];

@@ -401,6 +401,7 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     OR3_CUDA(ctx, cudaMemcpy(h1, ql[l].stats, sizeof(h1), cudaMemcpyDeviceToHost));
     for (int k = 0; k < 8; k++) hs[k] += h1[k];
   }
+  stats.lanes = (uint32_t)nl;
   stats.extension_rays = hs[0];
   stats.shadow_rays = hs[1];
   stats.bounces = hs[2];

@@ -519,9 +519,10 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
 #undef OR3_CSWAP
   const float tl2 = s.tmax * 1.0000010f;
   if (key[0] < inf2 && key[0] <= tl2) {
+    // siblings beyond a hit found in this node's leaves are pruned when popped
 #pragma unroll
     for (int j = 3; j >= 1; j--) {
-      if (key[j] < inf2 && key[j] <= tl2) {
+      if (key[j] < inf2) {
         if (s.sp < kStackSize) {
           stk.put(s.sp, kid[j], key[j]);
           s.sp++;

@@ -150,7 +150,9 @@ def test_compact_layout(pkg, ctx):
     assert img.shape == (10, 20, 3) and img.sum() > 0
 
 
-def test_stop_rendering_from_another_thread(pkg, ctx):
+@pytest.mark.parametrize("max_depth,wave_paths", [(0, 0), (8, 2000)])
+def test_stop_rendering_from_another_thread(pkg, ctx, max_depth, wave_paths):
+    """(8, 2000): many small waves per pass on the three wave lanes."""
     sd, cam, _ = pkg.workloads.cornell_box(64, 64)
     sid = ctx.upload(sd)
     seen = []
@@ -161,7 +163,8 @@ def test_stop_rendering_from_another_thread(pkg, ctx):
             threading.Thread(target=ctx.stop).start()
             threading.Event().wait(0.2)
 
-    ctx.render(sid, cam, supersamples=2, min_samples=1, max_samples=1000, step_samples=1, seed=2, callback=cb)
+    ctx.render(sid, cam, supersamples=2, min_samples=1, max_samples=1000, step_samples=1, seed=2, callback=cb,
+               max_depth=max_depth, wave_paths=wave_paths)
     ctx.reset_stop()
     _, samples = ctx.frame(cam.width, cam.height)
     ctx.release(sid)

@@ -510,6 +510,8 @@ int or3_context_destroy(or3_context *ctx) {
     if (ctx->ev_join[k]) cudaEventDestroy(ctx->ev_join[k]);
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  for (cudaEvent_t e : ctx->ev_poll)
+    if (e) cudaEventDestroy(e);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->tmp_pool) cudaMemPoolDestroy(ctx->tmp_pool);
   cudaStreamDestroy(ctx->stream);
@@ -1077,9 +1079,9 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // a depth bound of at most 32 enqueues every bounce of a wave at once
   const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;
   const int chunk = whole ? prm->max_depth : 8;
-  // extra wave lanes: waves round robin over 1 + nx streams (only where
-  // nothing per wave or per kernel is read back)
-  const bool multi = whole && !(prm->tuning & OR3_TUNE_ONE_LANE) &&
+  // extra wave lanes: waves round robin over 1 + nx streams (not where a
+  // wave's paths or per-kernel times are read back)
+  const bool multi = !(prm->tuning & OR3_TUNE_ONE_LANE) &&
                      !(prm->flags & (OR3_FLAG_KEEP_PATHS | OR3_FLAG_TIME_KERNELS | OR3_FLAG_COUNT_TRAVERSAL));
   int nx = !multi ? 0 : (prm->tuning & OR3_TUNE_TWO_LANES) ? 1 : (prm->tuning & OR3_TUNE_FOUR_LANES) ? 3 : 2;
   Queues qx[kExtraLanes] = {};
@@ -1114,16 +1116,16 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   for (int32_t next = prm->min_samples; next <= prm->max_samples; next += prm->step_samples) {
     if (ctx->stop.load()) { stopped = true; break; }
     size_t kused = 0;  // timing events used in this pass
-    uint32_t wave_index = 0;
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
     if (two) {
       OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
       for (int k = 0; k < nx; k++) OR3_CUDA(ctx, cudaStreamWaitEvent(ctx->xl[k].stream, ctx->ev_fork, 0));
     }
-    // waves over [prev, next) samples
-    for (uint32_t s = (uint32_t)prev; s < (uint32_t)next && !stopped;) {
+    // The pass's waves: whole samples of the image, or row chunks of one sample.
+    std::vector<Wave> pw;
+    for (uint32_t s = (uint32_t)prev; s < (uint32_t)next;) {
       const uint32_t ns = (uint32_t)std::min<uint64_t>(ns_per_wave, (uint64_t)next - s);
-      for (uint64_t p0 = 0; p0 < npix && !stopped; p0 += npix_per_wave) {
+      for (uint64_t p0 = 0; p0 < npix; p0 += npix_per_wave) {
         const uint64_t np = std::min<uint64_t>(npix_per_wave, npix - p0);
         Wave w{};
         w.g_first = ((uint64_t)s * npix + p0) * ss2;
@@ -1132,60 +1134,126 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         w.pix0 = (uint32_t)p0;
         w.npix = (uint32_t)np;
         w.ns = ns;
-        const int lane = two ? (int)(wave_index++ % (uint32_t)(1 + nx)) : 0;
-        const Queues &ql = lane ? qx[lane - 1] : q;
-        cudaStream_t sl = lane ? ctx->xl[lane - 1].stream : st;
-        double *lsum = lane ? ctx->xl[lane - 1].pix_sum : ctx->pix_sum;
-        double *lsq = lane ? ctx->xl[lane - 1].pix_sumsq : ctx->pix_sumsq;
-        launch_raygen(rcst, w, ql, 0, 0, block, sl);
-        // Bounces are enqueued in chunks without a host round trip: every
-        // kernel reads its queue length on the device, so a bounce after the
-        // last ray is a few empty launches.  With a depth bound the chunk is
-        // the whole path (no read-back at all); without one, the live count
-        // is read after each chunk of 8 (or the bound is above 32).
-        int in = 0;
-        for (int chunks = 0;; chunks++) {
-          for (int b = 0; b < chunk; b++) {
-            cudaEvent_t e4[4] = {};
-            if (timek) {
-              while (ctx->kpool.size() < kused + 4) {
-                cudaEvent_t e;
-                OR3_CUDA(ctx, cudaEventCreate(&e));
-                ctx->kpool.push_back(e);
-              }
-              for (int k = 0; k < 4; k++) e4[k] = ctx->kpool[kused + k];
-              kused += 4;
-            }
-            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[0], st));
-            launch_extend(sg->view, ql, in, grid_ext, block, smem_nodes, countk, variant, sl);
-            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[1], st));
-            launch_shade(sg->view, rcst, w, ql, in, grid_sh, block, sl, nee4);
-            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
-            if (shadows)
-              launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl);
-            if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
-            launch_reset_count(ql, in, sl);
-            in ^= 1;
-            stats.extend_launches++;
-            stats.shade_launches++;
-            if (shadows) stats.shadow_launches++;
-          }
-          if (whole) break;
-          OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t),
-                                        cudaMemcpyDeviceToHost, st));
-          OR3_CUDA(ctx, cudaStreamSynchronize(st));
-          if (ctx->host_counters[in] == 0 || ctx->host_counters[2] || chunks > 100000) break;
-        }
-        launch_accumulate(ql, w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, (uint64_t)ctx->num_sms * 64),
-                          block, sl);
-        stats.waves++;
-        stats.camera_paths += w.num_paths;
-        ctx->last_wave_paths = w.num_paths;
-        if (ctx->host_counters[2]) break;
+        pw.push_back(w);
       }
       s += ns;
-      if (ctx->host_counters[2]) break;
-      if (ctx->stop.load() && s < (uint32_t)next) stopped = true;
+    }
+    // Waves go round robin to the lanes.  Bounces are enqueued in chunks
+    // without a host round trip: every kernel reads its queue length on the
+    // device, so a bounce after the last ray is a few empty launches.  With a
+    // depth bound of at most 32 the chunk is the whole path and nothing is
+    // read back; without one each lane's live count is read after each chunk
+    // of 8, the host visiting the lanes in turn while the others run.
+    const int nlanes = 1 + nx;
+    struct LaneRun {
+      int wave = -1, in = 0, chunks = 0;
+    } lr[1 + kExtraLanes];
+    size_t next_wave = 0;
+    auto lane_q = [&](int l) -> const Queues & { return l ? qx[l - 1] : q; };
+    auto lane_st = [&](int l) { return l ? ctx->xl[l - 1].stream : st; };
+    auto lane_hc = [&](int l) { return l ? ctx->host_counters + 8 + 4 * (l - 1) : ctx->host_counters; };
+    auto enqueue_chunk = [&](int l) -> int {
+      const Queues &ql = lane_q(l);
+      cudaStream_t sl = lane_st(l);
+      const Wave &w = pw[(size_t)lr[l].wave];
+      for (int b = 0; b < chunk; b++) {
+        cudaEvent_t e4[4] = {};
+        if (timek) {  // one lane only
+          while (ctx->kpool.size() < kused + 4) {
+            cudaEvent_t e;
+            OR3_CUDA(ctx, cudaEventCreate(&e));
+            ctx->kpool.push_back(e);
+          }
+          for (int k = 0; k < 4; k++) e4[k] = ctx->kpool[kused + k];
+          kused += 4;
+        }
+        const int in = lr[l].in;
+        if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[0], st));
+        launch_extend(sg->view, ql, in, grid_ext, block, smem_nodes, countk, variant, sl);
+        if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[1], st));
+        launch_shade(sg->view, rcst, w, ql, in, grid_sh, block, sl, nee4);
+        if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
+        if (shadows)
+          launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl);
+        if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
+        launch_reset_count(ql, in, sl);
+        lr[l].in ^= 1;
+        stats.extend_launches++;
+        stats.shade_launches++;
+        if (shadows) stats.shadow_launches++;
+      }
+      lr[l].chunks++;
+      if (!whole) {
+        OR3_CUDA(ctx, cudaMemcpyAsync(lane_hc(l), ql.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, sl));
+        OR3_CUDA(ctx, cudaEventRecord(ctx->ev_poll[l], sl));
+      }
+      return OR3_OK;
+    };
+    auto finish_wave = [&](int l) {
+      const Wave &w = pw[(size_t)lr[l].wave];
+      const uint64_t np = w.npix;
+      double *lsum = l ? ctx->xl[l - 1].pix_sum : ctx->pix_sum;
+      double *lsq = l ? ctx->xl[l - 1].pix_sumsq : ctx->pix_sumsq;
+      launch_accumulate(lane_q(l), w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, (uint64_t)ctx->num_sms * 64),
+                        block, lane_st(l));
+      stats.waves++;
+      stats.camera_paths += w.num_paths;
+      ctx->last_wave_paths = w.num_paths;
+      lr[l].wave = -1;
+    };
+    // starts the next wave on lane l (whole mode: the wave in full); false when none is left
+    auto start_wave = [&](int l, int *rc_out) -> bool {
+      *rc_out = OR3_OK;
+      if (next_wave >= pw.size()) return false;
+      if (next_wave > 0 && ctx->stop.load()) {
+        stopped = true;
+        return false;
+      }
+      lr[l].wave = (int)next_wave++;
+      lr[l].in = 0;
+      lr[l].chunks = 0;
+      launch_raygen(rcst, pw[(size_t)lr[l].wave], lane_q(l), 0, 0, block, lane_st(l));
+      if ((*rc_out = enqueue_chunk(l))) return false;
+      if (whole) finish_wave(l);
+      return true;
+    };
+    if (!whole) {
+      for (int l = 0; l < nlanes; l++)
+        if (!ctx->ev_poll[l]) OR3_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_poll[l], cudaEventDisableTiming));
+    }
+    int live = 0;
+    for (int l = 0; l < nlanes; l++) {
+      int r = OR3_OK;
+      if (start_wave(l, &r)) live++;
+      if (r) return r;
+    }
+    if (whole) {
+      for (int l = 0;; l = (l + 1) % nlanes) {
+        int r = OR3_OK;
+        if (!start_wave(l, &r)) {
+          if (r) return r;
+          break;
+        }
+      }
+    } else {
+      bool dev_error = false;
+      while (live > 0) {
+        for (int l = 0; l < nlanes; l++) {
+          if (lr[l].wave < 0) continue;
+          OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev_poll[l]));
+          const uint32_t *hc = lane_hc(l);
+          if (hc[2]) dev_error = true;
+          if (!dev_error && hc[lr[l].in] != 0 && lr[l].chunks < 100000) {
+            if (int r = enqueue_chunk(l)) return r;
+            continue;
+          }
+          finish_wave(l);
+          live--;
+          int r = OR3_OK;
+          if (!dev_error && start_wave(l, &r)) live++;
+          if (r) return r;
+        }
+      }
     }
     for (int k = 0; k < nx; k++) {  // join the extra lanes and fold their pixel sums into lane 0's
       or3_context::Lane &L = ctx->xl[k];

@@ -97,6 +97,7 @@ struct or3_context {
     size_t cap_paths = 0, cap_rays = 0, cap_pixels = 0;
   } xl[kExtraLanes];
   cudaEvent_t ev_fork = nullptr, ev_join[kExtraLanes] = {};
+  cudaEvent_t ev_poll[1 + kExtraLanes] = {};  // a lane's queue-count read-back has landed
 
   or3::BatchBuffers *batch = nullptr;  // batched form state (or3_batch.cu)
   or3::Server *server = nullptr;       // served form state (or3_batch.cu)

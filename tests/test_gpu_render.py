@@ -150,9 +150,9 @@ def test_compact_layout(pkg, ctx):
     assert img.shape == (10, 20, 3) and img.sum() > 0
 
 
-@pytest.mark.parametrize("max_depth,wave_paths", [(0, 0), (8, 2000)])
+@pytest.mark.parametrize("max_depth,wave_paths", [(0, 0), (8, 2000), (0, 2000)])
 def test_stop_rendering_from_another_thread(pkg, ctx, max_depth, wave_paths):
-    """(8, 2000): many small waves per pass on the three wave lanes."""
+    """wave_paths 2000: many small waves per pass on the three wave lanes."""
     sd, cam, _ = pkg.workloads.cornell_box(64, 64)
     sid = ctx.upload(sd)
     seen = []
@@ -185,15 +185,18 @@ def test_waves_do_not_change_the_image(pkg, ctx):
     np.testing.assert_allclose(s1, s2, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("nee,tuning", [(False, 0), (True, 0), (True, 0x200), (True, 0x400)])
-def test_wave_lanes_match_one(pkg, ctx, nee, tuning):
+@pytest.mark.parametrize("nee,tuning,depth", [(False, 0, 8), (True, 0, 8), (True, 0x200, 8), (True, 0x400, 8),
+                                              (False, 0, 0), (True, 0, 0)])
+def test_wave_lanes_match_one(pkg, ctx, nee, tuning, depth):
     """Waves run round robin on three (two: 0x200, four: 0x400) streams with their own
     queues and pixel sums, merged at the end of each pass: the image, the moments and the ray counts
     equal the one-stream render's (up to the order of float additions: FP64
     pixel sums, and FP32 atomics of light samples into a path's radiance)."""
     sd, cam = pkg.workloads.sky_floor(48, 32) if nee else pkg.workloads.icosphere_in_box(48, 32, level=3)[:2]
     sid = ctx.upload(sd)
-    kw = dict(supersamples=4, min_samples=2, max_samples=6, step_samples=2, seed=5, max_depth=8,
+    # depth 0: the reference's rules (Russian roulette only), each lane's live
+    # count read back per chunk of bounces
+    kw = dict(supersamples=4, min_samples=2, max_samples=6, step_samples=2, seed=5, max_depth=depth,
               wave_paths=3000, next_event_estimation=nee)
     try:
         s2 = ctx.render(sid, cam, tuning=tuning, **kw)

@@ -445,6 +445,33 @@ int or3_mesh_transform(or3_mesh *mesh, const double position[3], const double sc
                        const double rotation[3]);
 void or3_mesh_free(or3_mesh *mesh);
 
+/* ---- scene files: the reference's text scene format to a scene descriptor
+ * (SceneFromExternalFile::ReadFromFile, src/scenes/SceneFromExternalFile.cpp:
+ * 66-182, and its object readers, :214-529).  Header "Base Dir", "IBL",
+ * "Space Partitioning" up to "Objects:", then "Obj Mesh", "Sphere",
+ * "SphereLight", "Floor" and "InfiniteFloor" blocks.  Meshes are read with
+ * or3_mesh_load_obj (flip_v 0) and placed with or3_mesh_transform; the IBL
+ * .hdr is read with or3_read_hdr into desc.env_rgbe.  Object ids follow the
+ * file (a mesh's triangles in file order).  Every sphere and triangle goes in
+ * the BVH ("Space Partitioning: False" objects are tested after the BVH by
+ * the reference, which differs only for hits at exactly equal distance).
+ * Materials with a texture keep texture = -1 and name the image in
+ * texture_paths[material] (loading it stays with the caller).  The descriptor
+ * and everything it points to live until or3_scene_file_free. */
+typedef struct or3_scene_file {
+  or3_scene_desc desc;
+  uint32_t num_meshes;          /* "Obj Mesh" blocks read */
+  char space_partitioning[16];  /* the header's value ("BVH", "QBVH", or "") */
+  char **texture_paths;         /* [desc.num_materials] image path, or NULL */
+  char *ibl_path;               /* the IBL file read, or NULL */
+} or3_scene_file;
+/* threads: for the .obj files (0 = all host threads).  OR3_ERR_NOT_FOUND for
+   a missing scene, mesh or IBL file, OR3_ERR_INVALID_ARGUMENT for anything the
+   reference's reader rejects, or an object without a Material; err (may be
+   NULL) gets a one-line reason. */
+int or3_scene_load_file(const char *path, uint32_t threads, or3_scene_file **file_out, char *err, size_t err_len);
+void or3_scene_file_free(or3_scene_file *file);
+
 /* ---- rendering without allocating (no counterpart in the reference) ------
  * For callers that must not allocate device memory while they render: code
  * running in a host callback enqueued on a CUDA stream (CUDA calls that

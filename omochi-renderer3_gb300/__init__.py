@@ -5,5 +5,5 @@ in include/or3.h); this package only builds it, loads it and mirrors the
 reference's render interface on top of it.
 """
 from . import abi, build, scene, workloads  # noqa: F401
-from .renderer import Context, GpuPathTracer, Or3Error, ScreenPixels, load_obj, read_hdr  # noqa: F401
+from .renderer import Context, GpuPathTracer, Or3Error, ScreenPixels, load_obj, load_scene_file, read_hdr  # noqa: F401
 from .scene import Camera, SceneDesc  # noqa: F401

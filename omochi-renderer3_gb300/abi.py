@@ -138,6 +138,11 @@ class MeshC(ctypes.Structure):
                 ("material_names", P(ctypes.c_char_p)), ("texture_paths", P(ctypes.c_char_p))]
 
 
+class SceneFileC(ctypes.Structure):
+    _fields_ = [("desc", SceneDescC), ("num_meshes", ctypes.c_uint32), ("space_partitioning", ctypes.c_char * 16),
+                ("texture_paths", P(ctypes.c_char_p)), ("ibl_path", ctypes.c_char_p)]
+
+
 JOB_FRAME8_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, P(ctypes.c_uint8),
                                  ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32)
 JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, f64p, ctypes.c_size_t,
@@ -201,6 +206,9 @@ PROTOTYPES = {
     "or3_mesh_free": (None, [P(MeshC)]),
     "or3_read_hdr": (ctypes.c_int, [P(ctypes.c_uint8), ctypes.c_size_t, P(ctypes.c_uint32), P(ctypes.c_uint32),
                                     P(ctypes.c_uint8), ctypes.c_size_t]),
+    "or3_scene_load_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, P(P(SceneFileC)), ctypes.c_char_p,
+                                           ctypes.c_size_t]),
+    "or3_scene_file_free": (None, [P(SceneFileC)]),
     "or3_server_submit": (ctypes.c_int, [ctypes.c_void_p, P(BatchJobC), P(ctypes.c_uint64)]),
     "or3_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, P(JobStatusC)]),
     "or3_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

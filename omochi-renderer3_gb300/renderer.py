@@ -60,6 +60,17 @@ class Context:
         self._check(self.lib.or3_scene_upload(self.h, ctypes.byref(d), ctypes.byref(sid)))
         return sid.value
 
+    def upload_file(self, path, threads=0, build=0):
+        """A scene file straight from or3_scene_load_file to or3_scene_upload (no Python copy)."""
+        lib, fp = _scene_file_open(path, threads)
+        try:
+            fp.contents.desc.build = build
+            sid = ctypes.c_int32()
+            self._check(self.lib.or3_scene_upload(self.h, ctypes.byref(fp.contents.desc), ctypes.byref(sid)))
+        finally:
+            lib.or3_scene_file_free(fp)
+        return sid.value
+
     def release(self, scene):
         self._check(self.lib.or3_scene_release(self.h, scene))
 
@@ -441,3 +452,58 @@ def load_obj(path, flip_v=False, threads=0, position=None, scaling=(1.0, 1.0, 1.
     finally:
         lib.or3_mesh_free(mp)
     return out
+
+
+def _scene_file_open(path, threads):
+    lib = abi.load_library()
+    fp = ctypes.POINTER(abi.SceneFileC)()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.or3_scene_load_file(str(path).encode(), threads, ctypes.byref(fp), err, len(err))
+    if rc != abi.OR3_OK:
+        raise Or3Error(rc, "or3_scene_load_file(%s): %s" % (path, err.value.decode(errors="replace")))
+    return lib, fp
+
+
+def load_scene_file(path, threads=0):
+    """The reference's text scene file (SceneFromExternalFile) -> (SceneDesc, info).
+
+    or3_scene_load_file on the host; the arrays are copied into a SceneDesc
+    with the file's object ids.  info: space_partitioning, ibl_path, meshes,
+    textures (image path per material, or None).
+    """
+    from .scene import SceneDesc
+    lib, fp = _scene_file_open(path, threads)
+    try:
+        f = fp.contents
+        d = f.desc
+        sd = SceneDesc()
+        for i in range(d.num_materials):
+            m = d.materials[i]
+            sd.material(m.type, tuple(m.color), tuple(m.emission), m.ior, m.phong_exponent, m.texture)
+        sd.layer_material = [d.layer_material[i] for i in range(d.num_layers)]
+        sd.layer_rate = [d.layer_rate[i] for i in range(d.num_layers)]
+        n = d.num_triangles
+        if n:
+            arr = np.ctypeslib.as_array
+            sd.tris.append((arr(d.tri_vertices, shape=(n, 3, 3)).copy(), arr(d.tri_normals, shape=(n, 3, 3)).copy(),
+                            arr(d.tri_uvs, shape=(n, 3, 2)).copy(), arr(d.tri_layers, shape=(n, 2)).copy(),
+                            arr(d.tri_ids, shape=(n,)).copy()))
+        for i in range(d.num_spheres):
+            sd.spheres.append((*(d.spheres[4 * i + k] for k in range(4)), d.sphere_layers[2 * i],
+                               d.sphere_layers[2 * i + 1], d.sphere_flags[i], d.sphere_ids[i]))
+        for i in range(d.num_planes):
+            sd.planes.append((*(d.planes[4 * i + k] for k in range(4)), d.plane_layers[2 * i],
+                              d.plane_layers[2 * i + 1], d.plane_ids[i]))
+        sd._next_id = n + d.num_spheres + d.num_planes
+        if d.env_rgbe:
+            sd.set_env_rgbe(np.ctypeslib.as_array(d.env_rgbe, shape=(d.env_height, d.env_width, 4)).copy())
+        info = {
+            "space_partitioning": f.space_partitioning.decode(),
+            "ibl_path": f.ibl_path.decode() if f.ibl_path else None,
+            "meshes": f.num_meshes,
+            "textures": [(f.texture_paths[i].decode() if f.texture_paths[i] else None)
+                         for i in range(d.num_materials)],
+        }
+    finally:
+        lib.or3_scene_file_free(fp)
+    return sd, info

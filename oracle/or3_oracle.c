@@ -788,6 +788,15 @@ orc_scene *orc_scene_create(const or3_scene_desc *d, int use_bvh) {
     s->envh = (int)d->env_height;
     s->env = (float *)malloc(sizeof(float) * 3 * (size_t)s->envw * s->envh);
     memcpy(s->env, d->env_rgb, sizeof(float) * 3 * (size_t)s->envw * s->envh);
+  } else if (d->env_rgbe) { /* RGBE bytes: HDRImage::RGBE2Color per texel (exact in FP32) */
+    s->envw = (int)d->env_width;
+    s->envh = (int)d->env_height;
+    const size_t np = (size_t)s->envw * s->envh;
+    double *tmp = (double *)malloc(sizeof(double) * 3 * np);
+    orc_decode_rgbe(np, d->env_rgbe, tmp);
+    s->env = (float *)malloc(sizeof(float) * 3 * np);
+    for (size_t i = 0; i < 3 * np; i++) s->env[i] = (float)tmp[i];
+    free(tmp);
   }
   s->bg = ld(d->background);
   s->ntex = (int)d->num_textures;

@@ -183,6 +183,8 @@ class Reference:
         lib.orref_write_hdr.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, f64p]
         lib.orref_read_hdr.argtypes = [ctypes.c_char_p, i32p, i32p, f64p, ctypes.c_size_t]
         lib.orref_load_obj.restype = ctypes.c_long
+        lib.orref_load_scene_file.restype = ctypes.c_long
+        lib.orref_load_scene_file.argtypes = [ctypes.c_char_p, f64p, ctypes.c_long, f64p]
         lib.orref_load_obj.argtypes = [ctypes.c_char_p, ctypes.c_int, f64p, f64p, f64p, f64p, f64p, f64p, f64p,
                                        ctypes.c_long]
         self.lib = lib
@@ -228,6 +230,18 @@ class Reference:
                                 _np(tri, ctypes.c_double), _np(nrm, ctypes.c_double), _np(uv, ctypes.c_double),
                                 _np(mat, ctypes.c_double), n)
         return tri, nrm, uv, mat
+
+    def load_scene_file(self, path):
+        """SceneFromExternalFile: (records [n, 67], ibl [5]) or None when the reference rejects the file.
+        Record: kind, in BVH, layers, geometry 24, then 4 x (type, emission 3, colour 3, ior, rate, texture)."""
+        ibl = np.zeros(5)
+        z = np.zeros(1)
+        n = self.lib.orref_load_scene_file(path.encode(), _np(z, ctypes.c_double), 0, _np(ibl, ctypes.c_double))
+        if n < 0:
+            return None
+        rec = np.zeros((n, 67))
+        self.lib.orref_load_scene_file(path.encode(), _np(rec, ctypes.c_double), n, _np(ibl, ctypes.c_double))
+        return rec, ibl
 
     def read_hdr(self, path):
         w, h = ctypes.c_int32(), ctypes.c_int32()

@@ -56,6 +56,7 @@
 #include "renderer/SphereLight.h"
 #include "renderer/Model.h"
 #include "scenes/Scene.h"
+#include "scenes/SceneFromExternalFile.h"
 #include "tools/FileSaver.h"
 #include "tools/Matrix.h"
 #include "tools/HDRImage.h"
@@ -188,17 +189,23 @@ void *orref_scene_create(const or3_scene_desc *d, int use_bvh) {
     s->idOf[obj] = (int32_t)r.id;
   }
 
-  if (d->env_rgb && d->env_width && d->env_height) {
+  if ((d->env_rgb || d->env_rgbe) && d->env_width && d->env_height) {
     // The IBL constructor only reads a .hdr file; feed the float image instead
-    // (no RGBE quantisation).
+    // (no RGBE quantisation), or RGBE bytes through HDRImage::RGBE2Color.
     std::streambuf *old = std::cerr.rdbuf(nullptr);
     IBL *ibl = new IBL("");
     std::cerr.rdbuf(old);
     ibl->m_image.m_width = d->env_width;
     ibl->m_image.m_height = d->env_height;
     ibl->m_image.m_image.resize((size_t)d->env_width * d->env_height);
-    for (size_t p = 0; p < (size_t)d->env_width * d->env_height; p++)
-      ibl->m_image.m_image[p] = Color(d->env_rgb[3 * p], d->env_rgb[3 * p + 1], d->env_rgb[3 * p + 2]);
+    for (size_t p = 0; p < (size_t)d->env_width * d->env_height; p++) {
+      if (d->env_rgb) {
+        ibl->m_image.m_image[p] = Color(d->env_rgb[3 * p], d->env_rgb[3 * p + 1], d->env_rgb[3 * p + 2]);
+      } else {
+        unsigned char b[4] = {d->env_rgbe[4 * p], d->env_rgbe[4 * p + 1], d->env_rgbe[4 * p + 2], d->env_rgbe[4 * p + 3]};
+        HDRImage::RGBE2Color(b, ibl->m_image.m_image[p]);
+      }
+    }
     s->m_ibl.reset(ibl);
   }
   if (use_bvh && !s->m_inBVHObjects.empty()) s->ConstructBVH();
@@ -417,6 +424,73 @@ long orref_load_obj(const char *path, int flip_v, const double *pos, const doubl
       mat[5 * n + 1] = m.color.x; mat[5 * n + 2] = m.color.y; mat[5 * n + 3] = m.color.z;
       mat[5 * n + 4] = m.refraction_rate;
     }
+  }
+  return n;
+}
+
+// SceneFromExternalFile (src/scenes/SceneFromExternalFile.cpp:47-182): the
+// scene a text scene file describes, one record of kSceneRec doubles per
+// object in Scene::m_objects order: kind (0 polygon, 1 sphere, 2 sphere
+// light, 3 infinite floor, 4 other), in BVH, layer count, 24 of geometry
+// (polygon: world vertices 9, normals 9, uvs 6; sphere: centre, radius;
+// infinite floor: y), then up to 4 layers of (type, emission 3, colour 3,
+// ior, rate, has texture).  ibl[0..1] get the IBL image's width and height
+// (0 without one) and ibl[2..4] the sum of its texels.  Returns the object
+// count, or -1 when the reference rejects the file.
+static const int kSceneRec = 67;
+long orref_load_scene_file(const char *path, double *rec, long cap, double *ibl) {
+  std::streambuf *old = std::cerr.rdbuf(nullptr);
+  SceneFromExternalFile scene(path);
+  std::cerr.rdbuf(old);
+  if (!scene.IsValid()) return -1;
+  long n = 0;
+  for (const auto &info : scene.m_objects) {
+    if (n >= cap) { n++; continue; }
+    double *r = rec + (size_t)kSceneRec * n;
+    std::fill(r, r + kSceneRec, 0.0);
+    const SceneObject *o = info.object;
+    r[1] = info.inBVH ? 1 : 0;
+    if (const Polygon *p = dynamic_cast<const Polygon *>(o)) {
+      r[0] = 0;
+      const Vector3 v0 = p->m_posAndEdges[0] + p->position_;
+      const Vector3 v[3] = {v0, v0 + p->m_posAndEdges[1], v0 + p->m_posAndEdges[2]};
+      const Vector3 n0 = p->m_normalAndDiffs[0];
+      const Vector3 nn[3] = {n0, n0 + p->m_normalAndDiffs[1], n0 + p->m_normalAndDiffs[2]};
+      const Vector3 u0 = p->m_uvOrigAndEdges[0];
+      const Vector3 uu[3] = {u0, u0 + p->m_uvOrigAndEdges[1], u0 + p->m_uvOrigAndEdges[2]};
+      for (int k = 0; k < 3; k++) {
+        r[3 + 3 * k] = v[k].x; r[4 + 3 * k] = v[k].y; r[5 + 3 * k] = v[k].z;
+        r[12 + 3 * k] = nn[k].x; r[13 + 3 * k] = nn[k].y; r[14 + 3 * k] = nn[k].z;
+        r[21 + 2 * k] = uu[k].x; r[22 + 2 * k] = uu[k].y;
+      }
+    } else if (const Sphere *sp = dynamic_cast<const Sphere *>(o)) {
+      r[0] = dynamic_cast<const SphereLight *>(o) ? 2 : 1;
+      r[3] = sp->position_.x; r[4] = sp->position_.y; r[5] = sp->position_.z; r[6] = sp->m_radius;
+    } else if (const InfiniteFloor *f = dynamic_cast<const InfiniteFloor *>(o)) {
+      r[0] = 3;
+      r[3] = f->y;
+    } else {
+      r[0] = 4;
+    }
+    r[2] = (double)o->GetMaterialCount();
+    for (size_t l = 0; l < o->GetMaterialCount() && l < 4; l++) {
+      const SceneObject::MultiMaterialElem *e = o->GetMaterial(l);
+      double *m = r + 27 + 10 * l;
+      m[0] = (double)e->material_.reflection_type;
+      m[1] = e->material_.emission.x; m[2] = e->material_.emission.y; m[3] = e->material_.emission.z;
+      m[4] = e->material_.color.x; m[5] = e->material_.color.y; m[6] = e->material_.color.z;
+      m[7] = e->material_.refraction_rate;
+      m[8] = e->rate_;
+      m[9] = e->material_.texture_id != ImageHandler::INVALID_IMAGE_ID ? 1 : 0;
+    }
+    n++;
+  }
+  ibl[0] = ibl[1] = ibl[2] = ibl[3] = ibl[4] = 0;
+  if (scene.m_ibl.get()) {
+    const Image &im = scene.m_ibl->m_image;
+    ibl[0] = (double)im.GetWidth();
+    ibl[1] = (double)im.GetHeight();
+    for (const Color &c : im.m_image) { ibl[2] += c.x; ibl[3] += c.y; ibl[4] += c.z; }
   }
   return n;
 }

@@ -20,6 +20,10 @@ committed and are all the GPU tests need.
                         Color2RGBE and RGBE2Color on seeded colours and bytes,
                         and two .hdr files its writer produced (one run-length
                         encoded, one flat) with what its reader decodes
+  scene_ref.npz         the reference's SceneFromExternalFile on
+                        tests/golden/scene/full.scene.in (one record per
+                        scene object, the IBL's size and texel sum) and its
+                        accept/reject verdict on each file of scene/cases.py
 Each fixture stores a digest of the flattened scene it was made from.
 """
 import argparse
@@ -151,6 +155,23 @@ def make_obj():
     print(dest, out["tri_0"].shape)
 
 
+def make_scene():
+    import tempfile
+    sys.path.insert(0, os.path.join(HERE, "scene"))
+    import cases
+    ref = O.Reference()
+    with tempfile.TemporaryDirectory() as td:
+        rec, ibl = ref.load_scene_file(cases.stage_scene_dir(td))
+        verdict = []
+        for name in sorted(cases.CASES):
+            r = ref.load_scene_file(cases.write(name, td))
+            verdict.append(-1 if r is None else r[0].shape[0])
+    dest = os.path.join(HERE, "scene_ref.npz")
+    np.savez_compressed(dest, records=rec, ibl=ibl, case_names=np.array(sorted(cases.CASES)),
+                        case_objects=np.array(verdict))
+    print(dest, rec.shape, dict(zip(sorted(cases.CASES), verdict)))
+
+
 def make_image_codec():
     import tempfile
     ref = O.Reference()
@@ -196,8 +217,12 @@ if __name__ == "__main__":
     if a.only == "obj":
         make_obj()
         sys.exit(0)
+    if a.only == "scene":
+        make_scene()
+        sys.exit(0)
     make_image_codec()
     make_obj()
+    make_scene()
     for nm in CLOSEST_SCENES:
         if not a.only or a.only == nm:
             make_closest(nm)

@@ -136,36 +136,69 @@ __global__ void k_clear_level(uint32_t ntasks, uint32_t *tbox, uint32_t *bins) {
 
 constexpr int kChunk = 1024;  // positions per block in the level passes (256 threads x 4)
 
-// Bounds of every large node of the level.
+// Bounds of every large node of the level.  Positions of one node are
+// contiguous, so a warp whose 32 positions lie in one node reduces them by
+// shuffles and issues one set of atomics; a block whose 1024 positions lie in
+// one node reduces across its warps in shared memory first.
 __global__ void __launch_bounds__(256) k_bounds(uint32_t n, const uint32_t *idx, const uint32_t *ptask,
                                                 const BuildPrim *prims, uint32_t *tbox) {
+  __shared__ float red[8][12];
   const uint32_t c0 = blockIdx.x * kChunk;
   if (c0 >= n) return;
   const uint32_t c1 = min(c0 + kChunk, n);
   const uint32_t t0 = ptask[c0], t1 = ptask[c1 - 1];
   const bool uniform = t0 == t1 && t0 != kNone;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   float v[12];
   for (int k = 0; k < 12; k++) v[k] = (k < 3 || (k >= 6 && k < 9)) ? FLT_MAX : -FLT_MAX;
-  for (uint32_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-    const uint32_t t = ptask[i];
-    if (t == kNone) continue;
-    const BuildPrim p = prims[idx[i]];
-    float c[3];
-    cent(p, c);
-    if (uniform) {
+  // warp-uniform trip count: every lane takes part in the shuffles
+  for (uint32_t base = c0 + warp * 32; base < c1; base += blockDim.x) {
+    const uint32_t i = base + lane;
+    const uint32_t t = i < c1 ? ptask[i] : kNone;
+    float u[12];
+    for (int k = 0; k < 12; k++) u[k] = (k < 3 || (k >= 6 && k < 9)) ? FLT_MAX : -FLT_MAX;
+    if (t != kNone) {
+      const BuildPrim p = prims[idx[i]];
+      float c[3];
+      cent(p, c);
       for (int a = 0; a < 3; a++) {
-        v[a] = fminf(v[a], p.lo[a]);
-        v[3 + a] = fmaxf(v[3 + a], p.hi[a]);
-        v[6 + a] = fminf(v[6 + a], c[a]);
-        v[9 + a] = fmaxf(v[9 + a], c[a]);
+        u[a] = p.lo[a];
+        u[3 + a] = p.hi[a];
+        u[6 + a] = c[a];
+        u[9 + a] = c[a];
       }
-    } else {
+    }
+    if (uniform) {
+      for (int k = 0; k < 12; k++) {
+        const bool mn = k < 3 || (k >= 6 && k < 9);
+        v[k] = mn ? fminf(v[k], u[k]) : fmaxf(v[k], u[k]);
+      }
+      continue;
+    }
+    const uint32_t tl = __shfl_sync(0xFFFFFFFFu, t, 0);
+    if (__all_sync(0xFFFFFFFFu, t == tl) && tl != kNone) {
+      for (int k = 0; k < 12; k++) {
+        const bool mn = k < 3 || (k >= 6 && k < 9);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float w = __shfl_xor_sync(0xFFFFFFFFu, u[k], o);
+          u[k] = mn ? fminf(u[k], w) : fmaxf(u[k], w);
+        }
+      }
+      if (lane == 0) {
+        uint32_t *b = tbox + 12 * (size_t)tl;
+        for (int k = 0; k < 12; k++) {
+          const bool mn = k < 3 || (k >= 6 && k < 9);
+          if (mn) atomicMin(b + k, f2o(u[k]));
+          else atomicMax(b + k, f2o(u[k]));
+        }
+      }
+    } else if (t != kNone) {
       uint32_t *b = tbox + 12 * (size_t)t;
-      for (int a = 0; a < 3; a++) {
-        atomicMin(b + a, f2o(p.lo[a]));
-        atomicMax(b + 3 + a, f2o(p.hi[a]));
-        atomicMin(b + 6 + a, f2o(c[a]));
-        atomicMax(b + 9 + a, f2o(c[a]));
+      for (int k = 0; k < 12; k++) {
+        const bool mn = k < 3 || (k >= 6 && k < 9);
+        if (mn) atomicMin(b + k, f2o(u[k]));
+        else atomicMax(b + k, f2o(u[k]));
       }
     }
   }
@@ -178,13 +211,17 @@ __global__ void __launch_bounds__(256) k_bounds(uint32_t n, const uint32_t *idx,
       v[k] = mn ? fminf(v[k], w) : fmaxf(v[k], w);
     }
   }
-  if ((threadIdx.x & 31u) == 0) {
+  if (lane == 0)
+    for (int k = 0; k < 12; k++) red[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int k = threadIdx.x;
+    const bool mn = k < 3 || (k >= 6 && k < 9);
+    float r = red[0][k];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) r = mn ? fminf(r, red[w][k]) : fmaxf(r, red[w][k]);
     uint32_t *b = tbox + 12 * (size_t)t0;
-    for (int k = 0; k < 12; k++) {
-      const bool mn = k < 3 || (k >= 6 && k < 9);
-      if (mn) atomicMin(b + k, f2o(v[k]));
-      else atomicMax(b + k, f2o(v[k]));
-    }
+    if (mn) atomicMin(b + k, f2o(r));
+    else atomicMax(b + k, f2o(r));
   }
 }
 
@@ -232,11 +269,18 @@ __global__ void __launch_bounds__(256) k_bin(uint32_t n, const uint32_t *idx, co
   }
 }
 
-// One thread per large node: node record, split choice, children.
-__global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbox, const uint32_t *bins,
-                         int leaf_max, double ct, DNode *nodes, Decision *dec, Task *next, Task *small, Counters *ctr) {
-  const uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ti >= ntasks) return;
+// One warp per large node: node record, split choice, children.  Lane b
+// evaluates the split after bin b of each axis; the box unions left and right
+// of it come from shuffle scans (min/max are exact, so the costs equal a
+// sequential scan's), and ties go to the lowest (axis, bin) as in one.
+constexpr int kDecideWarps = 4;
+__global__ void __launch_bounds__(32 * kDecideWarps) k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbox,
+                                                              const uint32_t *bins, int leaf_max, double ct,
+                                                              DNode *nodes, Decision *dec, Task *next, Task *small,
+                                                              Counters *ctr) {
+  const uint32_t ti = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (ti >= ntasks) return;  // warp-uniform
   const Task t = tasks[ti];
   const uint32_t *tb = tbox + 12 * (size_t)ti;
   float lo[3], hi[3], cblo[3], cbhi[3];
@@ -246,15 +290,6 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
     cblo[a] = o2f(tb[6 + a]);
     cbhi[a] = o2f(tb[9 + a]);
   }
-  DNode &nd = nodes[t.node];
-  for (int a = 0; a < 3; a++) {
-    nd.lo[a] = lo[a];
-    nd.hi[a] = hi[a];
-  }
-  nd.first = t.first;
-  nd.count = t.count;
-  nd.left = nd.right = -1;
-  atomicMax(&ctr->bin_depth, t.depth);
   Decision d;
   d.axis = -1;
   d.bin = 0;
@@ -266,48 +301,72 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
     // cost x parent area: ct * A + A_left * n_left + A_right * n_right
     const float parent = fmaxf(box_area_f(lo, hi), 1e-30f), ctp = (float)ct * parent;
     float best = FLT_MAX;
-    float rarea[kBins];
-    uint32_t rcnt[kBins];
     const uint32_t *B = bins + (size_t)kBinWords * ti;
     for (int a = 0; a < 3; a++) {
       const float ext = cbhi[a] - cblo[a];
-      if (!(ext > 0.f)) continue;
-      float alo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, ahi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-      uint32_t cnt = 0;
-      for (int b = kBins - 1; b > 0; b--) {
-        const uint32_t *w = B + (a * kBins + b) * 7;
-        if (w[6]) {
+      if (!(ext > 0.f)) continue;  // warp-uniform
+      float blo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+      uint32_t bc = 0;
+      if (lane < (uint32_t)kBins) {
+        const uint32_t *w = B + (a * kBins + lane) * 7;
+        bc = w[6];
+        if (bc)
           for (int k = 0; k < 3; k++) {
-            alo[k] = fminf(alo[k], o2f(w[k]));
-            ahi[k] = fmaxf(ahi[k], o2f(w[3 + k]));
+            blo[k] = o2f(w[k]);
+            bhi[k] = o2f(w[3 + k]);
           }
-        }
-        cnt += w[6];
-        rarea[b] = box_area_f(alo, ahi);
-        rcnt[b] = cnt;
       }
+      // inclusive prefix (bins 0..b) and suffix (bins b..kBins-1) unions
+      float plo[3], phi[3], slo[3], shi[3];
+      uint32_t pc = bc, sc = bc;
       for (int k = 0; k < 3; k++) {
-        alo[k] = FLT_MAX;
-        ahi[k] = -FLT_MAX;
+        plo[k] = slo[k] = blo[k];
+        phi[k] = shi[k] = bhi[k];
       }
-      cnt = 0;
-      for (int b = 0; b < kBins - 1; b++) {
-        const uint32_t *w = B + (a * kBins + b) * 7;
-        if (w[6]) {
-          for (int k = 0; k < 3; k++) {
-            alo[k] = fminf(alo[k], o2f(w[k]));
-            ahi[k] = fmaxf(ahi[k], o2f(w[3 + k]));
+#pragma unroll
+      for (int o = 1; o < kBins; o <<= 1) {
+        const uint32_t upc = __shfl_up_sync(0xFFFFFFFFu, pc, o), dnc = __shfl_down_sync(0xFFFFFFFFu, sc, o);
+        const bool up = lane >= (uint32_t)o, dn = lane + o < (uint32_t)kBins;
+        for (int k = 0; k < 3; k++) {
+          const float ul = __shfl_up_sync(0xFFFFFFFFu, plo[k], o), uh = __shfl_up_sync(0xFFFFFFFFu, phi[k], o);
+          const float dl = __shfl_down_sync(0xFFFFFFFFu, slo[k], o), dh = __shfl_down_sync(0xFFFFFFFFu, shi[k], o);
+          if (up) {
+            plo[k] = fminf(plo[k], ul);
+            phi[k] = fmaxf(phi[k], uh);
+          }
+          if (dn) {
+            slo[k] = fminf(slo[k], dl);
+            shi[k] = fmaxf(shi[k], dh);
           }
         }
-        cnt += w[6];
-        if (cnt == 0 || rcnt[b + 1] == 0) continue;
-        const float cost = ctp + box_area_f(alo, ahi) * (float)cnt + rarea[b + 1] * (float)rcnt[b + 1];
-        if (cost < best) {
-          best = cost;
-          d.axis = a;
-          d.bin = b;
-          d.nleft = cnt;
+        if (up) pc += upc;
+        if (dn) sc += dnc;
+      }
+      // split after bin `lane`: left = prefix[lane], right = suffix[lane + 1]
+      const float rarea = __shfl_down_sync(0xFFFFFFFFu, box_area_f(slo, shi), 1);
+      const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc, 1);
+      float cost = FLT_MAX;
+      if (lane < (uint32_t)(kBins - 1) && pc != 0 && rc != 0) {
+        cost = ctp + box_area_f(plo, phi) * (float)pc + rarea * (float)rc;
+        if (!(cost < FLT_MAX)) cost = FLT_MAX;
+      }
+      float mc = cost;
+      uint32_t ml = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oc = __shfl_xor_sync(0xFFFFFFFFu, mc, o);
+        const uint32_t ol = __shfl_xor_sync(0xFFFFFFFFu, ml, o);
+        if (oc < mc || (oc == mc && ol < ml)) {
+          mc = oc;
+          ml = ol;
         }
+      }
+      const uint32_t nl = __shfl_sync(0xFFFFFFFFu, pc, ml);
+      if (mc < best) {
+        best = mc;
+        d.axis = a;
+        d.bin = (int)ml;
+        d.nleft = nl;
       }
     }
     if (d.axis >= 0) {
@@ -315,6 +374,15 @@ __global__ void k_decide(uint32_t ntasks, const Task *tasks, const uint32_t *tbo
       d.scale = (float)kBins / (cbhi[d.axis] - cblo[d.axis]);
     }
   }
+  if (lane != 0) return;
+  DNode &nd = nodes[t.node];
+  for (int a = 0; a < 3; a++) {
+    nd.lo[a] = lo[a];
+    nd.hi[a] = hi[a];
+  }
+  nd.first = t.first;
+  nd.count = t.count;
+  atomicMax(&ctr->bin_depth, t.depth);
   // large nodes always split (a leaf needs at most leaf_max <= kSmallTask primitives)
   const int l = (int)atomicAdd(&ctr->nodes, 2u);
   nd.left = l;
@@ -975,7 +1043,8 @@ bool build_wide_bvh_device(const BuildPrim *prims, uint32_t n, int leaf_max, cud
       k_bounds<<<nblk, 256, 0, st>>>(n, idx, pt, prims, tbox);
       k_bin<<<nblk, 256, 0, st>>>(n, idx, pt, prims, tbox, bins);
       cudaMemsetAsync(&ctr->next_tasks, 0, sizeof(uint32_t), st);
-      k_decide<<<(ntasks + 127) / 128, 128, 0, st>>>(ntasks, tasks, tbox, bins, leaf_max, trav_cost, nodes, dec, next, small, ctr);
+      k_decide<<<(ntasks + kDecideWarps - 1) / kDecideWarps, 32 * kDecideWarps, 0, st>>>(
+          ntasks, tasks, tbox, bins, leaf_max, trav_cost, nodes, dec, next, small, ctr);
       k_flags<<<(n + 255) / 256, 256, 0, st>>>(n, idx, pt, tasks, dec, prims, flags);
       k_scan_blocks<<<nsb, 256, 0, st>>>(n, flags, scan, sums);
       k_scan_sums<<<1, 1024, 0, st>>>(nsb, sums);

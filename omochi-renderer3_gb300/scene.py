@@ -14,6 +14,13 @@ import numpy as np
 from . import abi
 
 
+def _cat(blocks):
+    """One contiguous array of the blocks; a single contiguous block is passed through uncopied."""
+    if len(blocks) == 1:
+        return np.ascontiguousarray(blocks[0])
+    return np.ascontiguousarray(np.concatenate(blocks))
+
+
 def _ptr(a, ctype):
     if a is None:
         return None
@@ -172,7 +179,7 @@ class SceneDesc:
         a["layer_material"] = np.asarray(self.layer_material, np.uint32)
         a["layer_rate"] = np.asarray(self.layer_rate, np.float64)
         if self.tris:
-            a["tri_vertices"] = np.ascontiguousarray(np.concatenate([t[0] for t in self.tris]))
+            a["tri_vertices"] = _cat([t[0] for t in self.tris])
             n_tot = a["tri_vertices"].shape[0]
             if any(t[1] is not None for t in self.tris):
                 norms = []
@@ -184,16 +191,16 @@ class SceneDesc:
                         c = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
                         c /= np.linalg.norm(c, axis=1, keepdims=True)
                         norms.append(np.repeat(c[:, None, :], 3, axis=1))
-                a["tri_normals"] = np.ascontiguousarray(np.concatenate(norms))
+                a["tri_normals"] = _cat(norms)
             else:
                 a["tri_normals"] = None
             if any(t[2] is not None for t in self.tris):
-                a["tri_uvs"] = np.ascontiguousarray(np.concatenate(
-                    [t[2] if t[2] is not None else np.zeros((t[0].shape[0], 3, 2)) for t in self.tris]))
+                a["tri_uvs"] = _cat([t[2] if t[2] is not None else np.zeros((t[0].shape[0], 3, 2))
+                                     for t in self.tris])
             else:
                 a["tri_uvs"] = None
-            a["tri_layers"] = np.ascontiguousarray(np.concatenate([t[3] for t in self.tris]))
-            a["tri_ids"] = np.ascontiguousarray(np.concatenate([t[4] for t in self.tris]))
+            a["tri_layers"] = _cat([t[3] for t in self.tris])
+            a["tri_ids"] = _cat([t[4] for t in self.tris])
             assert a["tri_layers"].shape == (n_tot, 2)
         else:
             for k in ("tri_vertices", "tri_normals", "tri_uvs", "tri_layers", "tri_ids"):

@@ -755,6 +755,13 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     sg->allocs.push_back(dbvh.fnodes);
     tmp.p.push_back(dbvh.order);
   }
+  // the traversal stack (kStackSize entries, at most 3 pushed per wide level)
+  // relies on the builders' depth bound
+  if ((on_device ? dbvh.wide_depth : bvh.wide_depth) > kMaxBinaryDepth / 2) {
+    free_scene(sg);
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "BVH deeper than the traversal stack allows (%d wide levels)",
+                on_device ? dbvh.wide_depth : bvh.wide_depth);
+  }
   auto t1 = std::chrono::steady_clock::now();
 
   // ---- records in leaf order (the device build gathers them on the device)

@@ -31,6 +31,7 @@ constexpr float kPi = 3.14159265358979323846f;
 
 constexpr int kStackSize = 64;       // traversal stack entries per ray
 constexpr int kMaxBinaryDepth = 40;  // builder bound: wide depth <= 20, stack <= 61
+static_assert(3 * (kMaxBinaryDepth / 2) < kStackSize, "a path of wide nodes pushes at most 3 entries per level");
 
 // Wide node.  For child i and axis a the box is
 //   origin[a] + q[a][i] * 2^(exp[a]-127),  q in [0, 255]

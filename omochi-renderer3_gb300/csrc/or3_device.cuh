@@ -496,11 +496,9 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
       if (key[j] < inf2) {
         if (nxt == kNoEntry) {
           nxt = kid[j];
-        } else if (s.sp < kStackSize) {
-          stk.put(s.sp, kid[j], key[j]);
-          s.sp++;
         } else {
-          atomicOr(err, 1u);
+          stk.put(s.sp, kid[j], key[j]);  // index below kStackSize: see the push below
+          s.sp = min(s.sp + 1, kStackSize - 1);
         }
       }
     }
@@ -523,12 +521,11 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
 #pragma unroll
     for (int j = 3; j >= 1; j--) {
       if (key[j] < inf2) {
-        if (s.sp < kStackSize) {
-          stk.put(s.sp, kid[j], key[j]);
-          s.sp++;
-        } else {
-          atomicOr(err, 1u);
-        }
+        // at most 3 entries per wide level and wide depth <= kMaxBinaryDepth / 2
+        // (checked at upload), so sp stays below kStackSize; the clamp keeps
+        // the index in bounds without a branch
+        stk.put(s.sp, kid[j], key[j]);
+        s.sp = min(s.sp + 1, kStackSize - 1);
       }
     }
     s.entry = kid[0];

@@ -107,8 +107,9 @@ def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx, one_lane):
     ctx.server_start(keep_moments=True, frame_every_samples=1, wave_paths=1 << 16, on_frame=on_frame,
                      one_lane=one_lane)
     try:
+        # later arrivals join while the first job runs: submitted right behind it
+        # (microseconds), while the first job takes many waves and frame callbacks
         ids = [ctx.server_submit(*jobs[0][:2], **jobs[0][2])]
-        time.sleep(0.05)  # later arrivals join while the first job runs
         ids += [ctx.server_submit(j[0], j[1], **j[2]) for j in jobs[1:]]
         ctx.server_drain(120.0)
         stats = ctx.server_stats()
@@ -142,7 +143,8 @@ def test_server_budget_admission_and_cancel(pkg, ctx):
     # gets in because nothing else is running
     ctx.server_start(hbm_budget_bytes=80000, wave_paths=1 << 16)
     try:
-        long_id = ctx.server_submit(bsid, big[1], supersamples=2, min_samples=400, max_samples=400, seed=1)
+        # long enough (4000 passes) to be running still when it is cancelled
+        long_id = ctx.server_submit(bsid, big[1], supersamples=2, min_samples=4000, max_samples=4000, seed=1)
         ids = [ctx.server_submit(j[0], j[1], **j[2]) for j in jobs]
         time.sleep(0.05)
         ctx.server_cancel(long_id)

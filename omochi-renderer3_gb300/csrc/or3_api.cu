@@ -1353,6 +1353,30 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   return OR3_OK;
 }
 
+namespace {
+// Host copy of a frame: large frames (a 1024x768 reference-layout frame is
+// 37.7 MB) are cut into 64-byte-aligned pieces copied on up to 8 host threads.
+void copy_frame(void *dst, const void *src, size_t bytes) {
+  constexpr size_t kPiece = 4u << 20;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = (unsigned)std::min<size_t>({(size_t)8, (size_t)hw, bytes / kPiece});
+  if (nt <= 1) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const size_t per = (bytes / nt + 63) & ~(size_t)63;
+  auto part = [&](unsigned k) {
+    const size_t b = std::min(bytes, per * k), e = std::min(bytes, b + per);
+    std::memcpy(static_cast<char *>(dst) + b, static_cast<const char *>(src) + b, e - b);
+  };
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (unsigned k = 1; k < nt; k++) th.emplace_back(part, k);
+  part(0);
+  for (auto &t : th) t.join();
+}
+}  // namespace
+
 int or3_get_frame(or3_context *ctx, double *rgb, size_t capacity, int32_t *samples_out) {
   if (!ctx) return OR3_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(ctx->frame_mu);
@@ -1360,7 +1384,7 @@ int or3_get_frame(or3_context *ctx, double *rgb, size_t capacity, int32_t *sampl
   if (ctx->front_doubles == 0) return fail(ctx, OR3_ERR_NOT_FOUND, "no frame rendered yet");
   if (!rgb || capacity < ctx->front_doubles)
     return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "frame needs %zu doubles", ctx->front_doubles);
-  std::memcpy(rgb, ctx->frame_front, ctx->front_doubles * sizeof(double));
+  copy_frame(rgb, ctx->frame_front, ctx->front_doubles * sizeof(double));
   return OR3_OK;
 }
 

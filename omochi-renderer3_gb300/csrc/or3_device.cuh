@@ -401,6 +401,9 @@ __device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint3
 // query may take them in slot order.
 // FN: test the node's FP32 child boxes (S.fnodes); false: the quantised
 // boxes (S.nodes, optionally staged in shared memory as snodes[0..ns)).
+// The stack cannot overflow here (depth bound checked at upload, push index
+// clamped), so `err` is not written on this path; the signature matches
+// trav_step's.
 template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true>
 __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, STK &stk,
                                                  const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {

@@ -435,9 +435,10 @@ __device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s
       const float tny = fmaf(nya[i], s.inv.y, s.oi.y), tfy = fmaf(fya[i], s.inv.y, s.oi.y);
       const float tnz = fmaf(nza[i], s.inv.z, s.oi.z), tfz = fmaf(fza[i], s.inv.z, s.oi.z);
       const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
-      const float tf = fminf(fminf(tfx, tfy), tfz) * 1.0000010f;
+      // one compare against min(far, tlimit): tn <= far && tn <= tlimit
+      const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * 1.0000010f, tlimit);
       const bool internal = (imask >> i) & 1u;
-      const bool hitbox = tn <= tf && tn <= tlimit;  // never for an empty slot (+inf / -inf planes)
+      const bool hitbox = tn <= tf;  // never for an empty slot (+inf / -inf planes)
       key[i] = (hitbox && internal) ? tn : kInf * 2.f;
       kid[i] = cha[i];
       if (hitbox && !internal) leafmask |= 1u << i;

@@ -187,3 +187,39 @@ def test_oracle_agrees_with_reference_on_the_scene_file_scene(pkg, orc, ref, tmp
     assert (ids_o == ids_r).mean() >= 0.999 and (ids_o >= 0).sum() > n // 4
     same = ids_o == ids_r
     np.testing.assert_allclose(t_o[same & (ids_o >= 0)], t_r[same & (ids_o >= 0)], rtol=1e-12)
+
+
+def test_scene_file_mutations_never_crash(pkg, tmp_path):
+    """Seeded mutations of the full scene (lines dropped, repeated or cut, delimiters
+    planted) load or fail with a status; the reader never crashes or hangs."""
+    path = stage_scene_dir(str(tmp_path))
+    text = open(path).read()
+    lines = text.split("\n")
+    rng = np.random.default_rng(17)
+    outcomes = {"ok": 0, "error": 0}
+    for k in range(300):
+        ls = list(lines)
+        for _ in range(int(rng.integers(1, 4))):
+            j = int(rng.integers(0, len(ls)))
+            op = int(rng.integers(0, 5))
+            if op == 0:
+                del ls[j]
+            elif op == 1:
+                ls.insert(j, ls[j])
+            elif op == 2:
+                ls[j] = ls[j][:int(rng.integers(0, len(ls[j]) + 1))]
+            elif op == 3 and ls[j]:
+                c = int(rng.integers(0, len(ls[j])))
+                ls[j] = ls[j][:c] + "{}:,#"[int(rng.integers(0, 5))] + ls[j][c + 1:]
+            else:
+                ls.insert(j, "")
+        p = tmp_path / ("m%03d.scene" % k)
+        p.write_text("\n".join(ls))
+        try:
+            sd, _ = pkg.load_scene_file(str(p))
+            assert sd.num_objects >= 0
+            outcomes["ok"] += 1
+        except pkg.Or3Error as e:
+            assert e.code in (pkg.abi.OR3_ERR_INVALID_ARGUMENT, pkg.abi.OR3_ERR_NOT_FOUND)
+            outcomes["error"] += 1
+    assert outcomes["ok"] > 0 and outcomes["error"] > 0, outcomes

@@ -104,11 +104,12 @@ __device__ __forceinline__ bool isect_triangle(const float4 a, const float4 b, c
   const V3 Q = cross(T, e1);
   const float v = dot(Q, d);
   if (!(v >= 0.f && u + v <= det)) return false;
-  const float tt = dot(Q, e2) / det;
+  const float inv = 1.0f / det;  // one division for t, u and v
+  const float tt = dot(Q, e2) * inv;
   if (!(tt >= kEps) || !(tt < tbest)) return false;
   t = tt;
-  ur = u / det;
-  vr = v / det;
+  ur = u * inv;
+  vr = v * inv;
   return true;
 }
 

@@ -42,11 +42,11 @@ METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency whe
 # grow with the rays; profiles/k_extend_mesh_512x384.md,
 # profiles/k_traversal_terrain_480x270.md); roofline.traffic is this times
 # the rays of an average launch.
-EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.2, "terrain": 52.2}
+EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.3, "terrain": 52.1}
 # The bounding roofline of a scene that stays in L2 is the SM issue rate: the
 # share of issue slots the extend kernel used on its active cycles
 # (smsp__issue_active), first and second launch of the same captures.
-EXTEND_ISSUE_ACTIVE = {"mesh": (0.753, 0.668), "terrain": (0.736, 0.750)}
+EXTEND_ISSUE_ACTIVE = {"mesh": (0.755, 0.646), "terrain": (0.733, 0.744)}
 
 
 def workload(pkg, name):

@@ -4,9 +4,14 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload mesh|cornell|terrain]
 
 A step is one full render (or3_render) of the workload: by default the
-displaced level-6 icosphere (81,920 triangles, Lambert + Phong layers) in the
-Cornell box, 1024x768, 16x16 sub-pixel grid = 256 samples per pixel, max
-depth 10 -- 201,326,592 camera paths per step.  Synthetic, seeded scenes.
+largest single-GPU scene, the IBL terrain (1,048,576-triangle height field,
+64 glass spheres, 2048x1024 float sky with a 1e4 sun importance-sampled
+through its marginal/conditional CDF, next-event estimation), 1920x1080 with
+a 32x32 sub-pixel grid = 1024 samples per pixel, max depth 12 --
+2,123,366,400 camera paths per step.  `--workload mesh` is the displaced
+level-6 icosphere (81,920 triangles, Lambert + Phong layers) in the Cornell
+box, 1024x768, 256 spp, max depth 10; `--workload cornell` the reference's
+CPU-runnable Cornell box.  Synthetic, seeded scenes.
 
 value      camera paths / device time of the passes (CUDA events on the
            library's stream, scene resident in HBM), Mpaths/s
@@ -37,16 +42,20 @@ import __graft_entry__ as ge  # noqa: E402
 
 METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency when served"
 
-# DRAM bytes (read + write) per ray of the extend kernel, from one ncu capture
-# per workload on a smaller image of the same scene (camera rays: queue bytes
-# grow with the rays; profiles/k_extend_mesh_512x384.md,
-# profiles/k_traversal_terrain_480x270.md); roofline.traffic is this times
-# the rays of an average launch.
-EXTEND_DRAM_BYTES_PER_RAY = {"mesh": 48.3, "terrain": 52.1}
-# The bounding roofline of a scene that stays in L2 is the SM issue rate: the
-# share of issue slots the extend kernel used on its active cycles
-# (smsp__issue_active), first and second launch of the same captures.
-EXTEND_ISSUE_ACTIVE = {"mesh": (0.755, 0.646), "terrain": (0.733, 0.744)}
+# Figures that come from an ncu capture, not from this run (ncu cannot run
+# inside the timed bench).  Per workload: DRAM bytes (read + write) per ray of
+# the extend kernel, from dram__bytes_read.sum + dram__bytes_write.sum of one
+# `ncu --set full` capture of its first two launches on a smaller image of the
+# same scene (queue bytes grow with the rays, the scene stays in L2), and the
+# share of issue slots the kernel used on its active cycles
+# (smsp__issue_active) in the same launches.  roofline.traffic is the bytes
+# per ray times the rays of an average launch of this run.
+NCU_EXTEND = {
+    "mesh": {"dram_bytes_per_ray": 48.3, "issue_active": (0.755, 0.646),
+             "source": "ncu --set full, k_extend launches 1-2, mesh scene at 512x384, 8x8 sub-pixel grid"},
+    "terrain": {"dram_bytes_per_ray": 52.1, "issue_active": (0.733, 0.744),
+                "source": "ncu --set full, k_extend launches 1-2, terrain scene at 480x270, 8x8 sub-pixel grid"},
+}
 
 
 def workload(pkg, name):
@@ -378,7 +387,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mesh", choices=["mesh", "cornell", "terrain"])
+    ap.add_argument("--workload", default="terrain", choices=["mesh", "cornell", "terrain"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -454,14 +463,14 @@ def main():
     torch.cuda.synchronize()
     render_ms = 0.0
     shadow_rays = 0
-    launches_all = paths = ext_rays = bounces = waves = passes = 0
+    launches = paths = ext_rays = bounces = waves = passes = 0
     w0 = time.perf_counter()
     for i in range(args.steps):
         flush.zero_()  # L2 (129 MB) flushed between steps
         s = ctx.render(sid, cam, seed=i, **kw)
         render_ms += s["render_ms"]
         shadow_rays += s["shadow_rays"]
-        launches_all += s["extend_launches"]
+        launches += s["kernel_launches"]
         paths += s["camera_paths"]
         ext_rays += s["extension_rays"]
         bounces += s["bounces"]
@@ -497,8 +506,6 @@ def main():
     e2e_s = max_over_ranks(dist, time.perf_counter() - e0)
     e2e_paths = sum_over_ranks(dist, float(paths / args.steps * e2e_steps))
 
-    # per wave raygen + accumulate; per bounce extend, shade, reset (+ shadow); per pass frame (+ merge)
-    launches = 2 * waves + (4 if shadow_rays else 3) * launches_all + 2 * passes
     avg_ext_ms = ext_ms / max(ext_launches, 1)
     achieved = alg_bytes_per_ray * t_ext_rays / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else None
     peak, peak_kind = load_peaks()
@@ -509,7 +516,10 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": render_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "dtype_note": "FP32 arithmetic and hit distances, as the target path specifies; the reference "
+                          "computes in FP64 (its Vector3 is double), so parity with it is statistical",
+            "data": "synthetic (seeded scene generators)",
             "config": {"workload": desc, "paths_per_step": paths // args.steps,
                        "extension_rays_per_step": ext_rays // args.steps, "triangles": int(info["num_primitives"]),
                        "wide_nodes": int(info["num_nodes"]), "scene_upload_ms": upload_s * 1000.0,
@@ -528,16 +538,24 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,
-                         "traffic": (EXTEND_DRAM_BYTES_PER_RAY[args.workload] * t_ext_rays / max(ext_launches, 1)
-                                     if args.workload in EXTEND_DRAM_BYTES_PER_RAY else None),
+                         "traffic": (NCU_EXTEND[args.workload]["dram_bytes_per_ray"] * t_ext_rays /
+                                     max(ext_launches, 1) if args.workload in NCU_EXTEND else None),
                          "traffic_unit": "bytes per launch",
+                         "traffic_source": (NCU_EXTEND[args.workload]["source"] + ", DRAM bytes per ray scaled "
+                                            "to this run's rays per launch" if args.workload in NCU_EXTEND
+                                            else None),
                          "alg_bytes_per_launch": alg_bytes_per_ray * t_ext_rays / max(ext_launches, 1),
                          "alg_bytes_per_ray": alg_bytes_per_ray, "avg_launch_ms": avg_ext_ms,
                          "launches": ext_launches,
-                         "sm_issue_active_ncu": EXTEND_ISSUE_ACTIVE.get(args.workload)},
+                         "sm_issue_active_ncu": (NCU_EXTEND[args.workload]["issue_active"]
+                                                 if args.workload in NCU_EXTEND else None),
+                         "sm_issue_active_source": (NCU_EXTEND[args.workload]["source"]
+                                                    if args.workload in NCU_EXTEND else None)},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
+            "gpu_launches_how": "sum of or3_render_stats.kernel_launches over the timed steps (the library "
+                                "counts every kernel it launches)",
         }
         print(json.dumps(line), flush=True)
     ctx.release(sid)

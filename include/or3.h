@@ -224,6 +224,7 @@ typedef struct or3_render_stats {
   uint64_t shadow_launches;
   uint32_t lanes;          /* wave lanes (streams) the render used */
   uint32_t reserved;
+  uint64_t kernel_launches; /* kernels this call launched (every kind, counted at each launch) */
 } or3_render_stats;
 
 typedef struct or3_scene_info {
@@ -473,11 +474,13 @@ int or3_scene_load_file(const char *path, uint32_t threads, or3_scene_file **fil
 void or3_scene_file_free(or3_scene_file *file);
 
 /* ---- rendering without allocating (no counterpart in the reference) ------
- * For callers that must not allocate device memory while they render: code
- * running in a host callback enqueued on a CUDA stream (CUDA calls that
- * allocate are not allowed there), engines that give the whole device to
- * their own pool at start-up (cudaMalloc would fail or fragment it), and
- * frame loops that cannot afford cudaMalloc/cudaFree synchronising the device.
+ * For callers that must not allocate device memory while they render:
+ * engines that give the whole device to their own pool at start-up (a
+ * cudaMalloc would fail or fragment that pool), and frame loops that cannot
+ * afford cudaMalloc/cudaFree synchronising the device.  Call it from ordinary
+ * host code: it launches kernels, copies and waits, so it must not be called
+ * from a host function or callback enqueued on a CUDA stream (CUDA forbids
+ * CUDA calls there).
  *
  * Traces camera paths g in [first_path, first_path + num_paths) of the render
  * that `camera` and `params` describe (the path order of or3_get_path_radiance;
@@ -490,10 +493,17 @@ void or3_scene_file_free(or3_scene_file *file);
  * library until the process exits); larger num_paths is rejected with
  * OR3_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a
  * device looks up that array's device address, so make that first call before
- * any stream capture.  Every call shares the array and it keeps the previous
- * call's contents (the call clears what must start at zero); calls that
- * overlap on the GPU -- from two host threads, or on two streams -- race on it.
- * Blocks until the result is in radiance_dev.  stream NULL = the context's. */
+ * any stream capture.  The address is kept for the life of the process: after
+ * cudaDeviceReset (or any reset of the device's primary context) it is stale,
+ * so do not call this entry again in that process.  Every call shares the
+ * array and it keeps the previous call's contents (the call clears what must
+ * start at zero); calls that overlap on the GPU -- from two host threads, or
+ * on two streams -- race on it.
+ * Blocks: every call synchronises `stream` (several times: it reads the queue
+ * lengths back to the host between bounce chunks) and returns once the
+ * result is in radiance_dev.  It makes the context's GPU current while it
+ * runs and restores the caller's current device before it returns.
+ * stream NULL = the context's. */
 #define OR3_NOALLOC_MAX_PATHS 4096u
 int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *camera,
                              const or3_render_params *params, uint64_t first_path, uint32_t num_paths,

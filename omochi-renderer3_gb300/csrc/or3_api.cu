@@ -1185,6 +1185,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
         launch_reset_count(ql, in, sl);
         lr[l].in ^= 1;
+        stats.kernel_launches += shadows ? 4 : 3;
         stats.extend_launches++;
         stats.shade_launches++;
         if (shadows) stats.shadow_launches++;
@@ -1203,6 +1204,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       double *lsq = l ? ctx->xl[l - 1].pix_sumsq : ctx->pix_sumsq;
       launch_accumulate(lane_q(l), w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, (uint64_t)ctx->num_sms * 64),
                         block, lane_st(l));
+      stats.kernel_launches++;
       stats.waves++;
       stats.camera_paths += w.num_paths;
       ctx->last_wave_paths = w.num_paths;
@@ -1220,6 +1222,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       lr[l].in = 0;
       lr[l].chunks = 0;
       launch_raygen(rcst, pw[(size_t)lr[l].wave], lane_q(l), 0, 0, block, lane_st(l));
+      stats.kernel_launches++;
       if ((*rc_out = enqueue_chunk(l))) return false;
       if (whole) finish_wave(l);
       return true;
@@ -1267,6 +1270,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       OR3_CUDA(ctx, cudaEventRecord(ctx->ev_join[k], L.stream));
       OR3_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join[k], 0));
       launch_merge_sums(npix * 3, ctx->pix_sum, ctx->pix_sumsq, L.pix_sum, L.pix_sumsq, ctx->num_sms * 16, st);
+      stats.kernel_launches++;
       OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8 + 4 * k, L.counters, 4 * sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, st));
     }
@@ -1302,6 +1306,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     // frame = running mean over `next` samples (PathTracer.cpp:169-170)
     const double scale = 1.0 / ((double)next * ss2);
     launch_frame(ctx->pix_sum, W, H, prm->output_layout, scale, ctx->frame_dev, st);
+    stats.kernel_launches++;
     if (frame_doubles > ctx->cap_back) {  // the back buffer is never read by another thread
       cudaStreamSynchronize(st);
       cudaFreeHost(ctx->frame_pinned);
@@ -1509,12 +1514,16 @@ int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *
   rc.max_depth = prm->max_depth;
   rc.seed_lo = (uint32_t)prm->seed;
   rc.seed_hi = (uint32_t)(prm->seed >> 32);
+  // the caller's current device is put back before returning
+  int caller_device = -1;
+  if (cudaGetDevice(&caller_device) != cudaSuccess) caller_device = -1;
   cudaSetDevice(ctx->device);
   std::string err;
   const int rcode = render_paths_noalloc(it->second->view, it->second->has_split, rc, first, num_paths,
                                          (uint32_t)prev, ctx->device, ctx->num_sms * ctx->occ_extend,
                                          ctx->num_sms * (rc.nee ? ctx->occ_shade_nee : ctx->occ_shade), radiance_dev,
                                          stream ? (cudaStream_t)stream : ctx->stream, &err);
+  if (caller_device >= 0 && caller_device != ctx->device) cudaSetDevice(caller_device);
   if (rcode != OR3_OK) return fail(ctx, rcode, "%s", err.c_str());
   return OR3_OK;
 }

@@ -1,15 +1,16 @@
 // or3_noalloc.cu -- or3_render_paths_noalloc: the wavefront path loop on a
 // fixed, statically allocated scratch area instead of cudaMalloc'd queues.
 //
-// Some callers cannot allocate device memory when they render: code running
-// inside a host callback enqueued on a stream (CUDA forbids CUDA calls that
-// allocate there), engines that hand the whole device to their own memory pool
-// up front (cudaMalloc would fail or fragment the pool), and frame loops with
-// a latency budget (cudaMalloc/cudaFree can synchronise the device).  For
-// them this entry point keeps every queue of the bounce loop in one
-// file-scope __device__ array, sized for kMaxPaths camera paths; the scene
-// must already be resident (or3_scene_upload, done at set-up) and the caller
-// passes the output buffer.
+// Some callers cannot allocate device memory when they render: engines that
+// hand the whole device to their own memory pool up front (cudaMalloc would
+// fail or fragment the pool), and frame loops with a latency budget
+// (cudaMalloc/cudaFree can synchronise the device).  For them this entry
+// point keeps every queue of the bounce loop in one file-scope __device__
+// array, sized for kMaxPaths camera paths; the scene must already be
+// resident (or3_scene_upload, done at set-up) and the caller passes the
+// output buffer.  It is called from ordinary host code and blocks: it
+// launches kernels, copies counters to the host and synchronises its stream,
+// none of which CUDA allows inside a host function enqueued on a stream.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -53,7 +54,9 @@ __global__ void k_copy_radiance(uint32_t n, float *out) {
 
 // Per-device set-up: the array's device address, taken once with the device
 // current.  (In host code `g_scratch` names a host-side stand-in, not device
-// memory, so it must never be passed to a kernel.)
+// memory, so it must never be passed to a kernel.)  The address is cached for
+// the life of the process; a cudaDeviceReset (a new primary context) would
+// make it stale, which the entry point's documentation states.
 cudaError_t scratch_for(int device, Scratch **out) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_mu);

@@ -17,7 +17,20 @@ ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libor3ref.so")
 REF_CFG_LIB = os.path.join(ORACLE_DIR, "_ref", "libor3ref_cfg.so")
-REFERENCE_SRC = os.environ.get("OR3_REFERENCE_DIR", "/root/reference")
+
+
+def _reference_dir():
+    """The reference checkout: $OR3_REFERENCE_DIR, else the one `make ref`
+    last compiled (recorded in _ref/source_dir), else none."""
+    if os.environ.get("OR3_REFERENCE_DIR"):
+        return os.environ["OR3_REFERENCE_DIR"]
+    rec = os.path.join(ORACLE_DIR, "_ref", "source_dir")
+    if os.path.exists(rec):
+        return open(rec).read().strip()
+    return ""
+
+
+REFERENCE_SRC = _reference_dir()
 
 f64p = ctypes.POINTER(ctypes.c_double)
 i32p = ctypes.POINTER(ctypes.c_int32)
@@ -30,11 +43,13 @@ class OrcParams(ctypes.Structure):
                 ("max_depth", ctypes.c_int32), ("pad", ctypes.c_int32), ("seed", ctypes.c_uint64)]
 
 
-def build_oracle(reference=True):
-    """make -C oracle (C restatement) and, where the reference sources exist, make ref."""
+def build_oracle(reference=True, reference_dir=None):
+    """make -C oracle (C restatement) and, when a reference checkout is named
+    (reference_dir, else $OR3_REFERENCE_DIR) and holds the sources, make ref."""
     subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
-    if reference and os.path.isdir(os.path.join(REFERENCE_SRC, "src")):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF=%s" % REFERENCE_SRC, "-j8"], check=True)
+    ref = reference_dir or REFERENCE_SRC
+    if reference and ref and os.path.isdir(os.path.join(ref, "src")):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF=%s" % ref, "-j8"], check=True)
 
 
 def reference_available():

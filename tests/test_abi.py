@@ -59,7 +59,7 @@ int main(void) {
   O(or3_scene_desc, env_rgb) O(or3_scene_desc, background) O(or3_scene_desc, texture_rgb)
   S(or3_camera) O(or3_camera, position) O(or3_camera, aperture_radius)
   S(or3_render_params) O(or3_render_params, seed) O(or3_render_params, flags)
-  S(or3_render_stats) O(or3_render_stats, render_ms) O(or3_render_stats, passes) O(or3_render_stats, lanes)
+  S(or3_render_stats) O(or3_render_stats, render_ms) O(or3_render_stats, passes) O(or3_render_stats, lanes) O(or3_render_stats, kernel_launches)
   S(or3_scene_info) O(or3_scene_info, build_ms) O(or3_scene_info, tree_depth) O(or3_scene_info, flatten_ms)
   return 0;
 }

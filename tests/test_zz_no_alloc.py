@@ -1,11 +1,12 @@
 """or3_render_paths_noalloc -- rendering camera paths with no device allocation.
 
 The entry point is for callers that cannot allocate device memory while they
-render (a host callback enqueued on a stream, an engine that owns the whole
-device through its own pool, a frame loop that cannot let cudaMalloc stall
-the device).  It keeps its ray queues in a fixed array compiled into the
-library, so it must give the same radiance, path for path, as the allocating
-or3_render, and keep doing so call after call on the shared array.
+render (an engine that owns the whole device through its own pool, a frame
+loop that cannot let cudaMalloc stall the device).  It keeps its ray queues
+in a fixed array compiled into the library, so it must give the same
+radiance, path for path, as the allocating or3_render, and keep doing so call
+after call on the shared array.  It also puts the caller's current device
+back before it returns.
 
 This file is collected last so that a failure here leaves every other test
 already run.
@@ -41,7 +42,9 @@ def test_noalloc_matches_render_on_consecutive_calls(pkg):
         got = []
         for first in firsts:
             out.fill_(-1.0)
+            dev_before = torch.cuda.current_device()
             ctx.render_paths_noalloc(sid, cam, first, n, out.data_ptr(), **SETTINGS)
+            assert torch.cuda.current_device() == dev_before
             torch.cuda.synchronize()
             got.append(out.cpu().numpy().reshape(n, 3).astype(np.float64))
         for first, g in zip(firsts, got):

@@ -146,21 +146,29 @@ def cpu_baseline(pkg, sd, cam, st, target_s=15.0, nthreads=None):
               step_samples=st["step_samples"], rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"], seed=1,
               next_event_estimation=st.get("next_event_estimation", False))
     chunks = 64
-    # calibrate
-    probe = 4096
-    t0 = time.perf_counter()
-    for c in range(8):
-        scene.path_radiance(cam, (total // 8) * c, probe // 8, nthreads=nthreads, **kw)
-    rate = probe / max(time.perf_counter() - t0, 1e-6)
-    n = int(min(max(rate * target_s, 65536), total))
-    per = max(n // chunks, 1)
+    stride = max(total // chunks, 1)
+    # calibrate on a sample spread over the workload
+    probe = 512
     t0 = time.perf_counter()
     for c in range(chunks):
-        scene.path_radiance(cam, (total // chunks) * c, per, nthreads=nthreads, **kw)
-    sec = time.perf_counter() - t0
-    return {"value": per * chunks / sec / 1e6, "unit": "Mpaths/s", "cores": nthreads, "kind": "port",
-            "sample": "%d camera paths in %d evenly spaced runs of the %d-path workload, FP64 C oracle, "
-                      "reference BVH, %.1f s" % (per * chunks, chunks, total, sec)}
+        scene.path_radiance(cam, stride * c, probe, nthreads=nthreads, **kw)
+    rate = probe * chunks / max(time.perf_counter() - t0, 1e-6)
+    # rounds of `chunks` evenly spaced runs, each round about an eighth of the
+    # target, until the target time is used (or the workload is exhausted)
+    per = int(min(max(rate * target_s / 8 / chunks, 256), stride))
+    done = rounds = 0
+    t0 = time.perf_counter()
+    while True:
+        for c in range(chunks):
+            scene.path_radiance(cam, stride * c + rounds * per, per, nthreads=nthreads, **kw)
+        done += per * chunks
+        rounds += 1
+        sec = time.perf_counter() - t0
+        if sec >= target_s or (rounds + 1) * per > stride:
+            break
+    return {"value": done / sec / 1e6, "unit": "Mpaths/s", "cores": nthreads, "kind": "port",
+            "sample": "%d camera paths in %d rounds of %d evenly spaced runs of the %d-path workload, FP64 C "
+                      "oracle, reference BVH, %.1f s" % (done, rounds, chunks, total, sec)}
 
 
 def dist_setup(args):

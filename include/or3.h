@@ -287,6 +287,19 @@ int or3_trace_closest_device(or3_context *ctx, int32_t scene, size_t n, const fl
 int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *origins_host,
                        const float *dirs_host, const float *tmax_host, uint8_t *occluded_host);
 
+/* ---- lookups the shading uses, for n inputs at a time --------------------
+   or3_env_sample: IBL::Sample(dir) (src/renderer/IBL.h:30-45), the
+   nearest-texel equirect lookup a missed ray returns (the scene's background
+   colour when it has no environment map); dirs are unit vectors.
+   or3_texture_sample: Image::GetPixelByUV(u, v) (src/tools/Image.h:21-31) of
+   the scene's texture `texture` (clamp to [0, 1], x 0.99999, nearest texel),
+   the factor GetTexturedColor (src/renderer/PathTracer.cpp:327-346) applies
+   to a textured layer's colour.  3 floats out per input.  Both run the
+   device functions of the render's shade kernel.  n < 2^31. */
+int or3_env_sample(or3_context *ctx, int32_t scene, size_t n, const float *dirs_host, float *rgb_host);
+int or3_texture_sample(or3_context *ctx, int32_t scene, int32_t texture, size_t n, const float *uv_host,
+                       float *rgb_host);
+
 /* ---- batched form (no counterpart in the reference) ----------------------
  * Many renders ("jobs": scene, camera, sample budget) traced together: every
  * wave of the wavefront holds camera paths of several jobs, so small jobs fill

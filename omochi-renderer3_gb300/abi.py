@@ -183,6 +183,9 @@ PROTOTYPES = {
     "or3_trace_closest_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_void_p]),
+    "or3_env_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, f32p, f32p]),
+    "or3_texture_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_size_t, f32p,
+                                          f32p]),
     "or3_trace_occluded": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t, f32p, f32p, f32p,
                                           P(ctypes.c_uint8)]),
     "or3_render_paths_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, P(CameraC), P(RenderParamsC),

@@ -1528,6 +1528,58 @@ int or3_render_paths_noalloc(or3_context *ctx, int32_t scene, const or3_camera *
   return OR3_OK;
 }
 
+}  // extern "C"
+
+// Shared by or3_env_sample / or3_texture_sample: n inputs of `in_floats`
+// floats each to the device, one lookup kernel, 3 floats each back.
+template <class Launch>
+static int lookup_query(or3_context *ctx, size_t n, const float *in, size_t in_floats, float *rgb, Launch launch) {
+  char *buf = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&buf, n * (in_floats + 3) * sizeof(float)));
+  float *ind = (float *)buf, *outd = ind + in_floats * n;
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(ind, in, n * in_floats * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    launch((uint32_t)n, ind, outd, st);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rgb, outd, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "lookup: %s", cudaGetErrorString(e));
+  return OR3_OK;
+}
+
+extern "C" {
+
+int or3_env_sample(or3_context *ctx, int32_t scene, size_t n, const float *dirs, float *rgb) {
+  if (!ctx || (n && (!dirs || !rgb))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  if (n >= ((size_t)1 << 31)) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "n too large");
+  if (n == 0) return OR3_OK;
+  cudaSetDevice(ctx->device);
+  const DevScene S = it->second->view;
+  return lookup_query(ctx, n, dirs, 3, rgb, [&](uint32_t m, const float *i, float *o, cudaStream_t st) {
+    launch_env_sample(S, m, i, o, st);
+  });
+}
+
+int or3_texture_sample(or3_context *ctx, int32_t scene, int32_t texture, size_t n, const float *uv, float *rgb) {
+  if (!ctx || (n && (!uv || !rgb))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
+  auto it = ctx->scenes.find(scene);
+  if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
+  const DevScene S = it->second->view;
+  if (texture < 0 || (uint32_t)texture >= S.num_textures)
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "texture %d not in the scene (%u textures)", texture, S.num_textures);
+  if (n >= ((size_t)1 << 31)) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "n too large");
+  if (n == 0) return OR3_OK;
+  cudaSetDevice(ctx->device);
+  return lookup_query(ctx, n, uv, 2, rgb, [&](uint32_t m, const float *i, float *o, cudaStream_t st) {
+    launch_texture_sample(S, texture, m, i, o, st);
+  });
+}
+
 int or3_trace_occluded(or3_context *ctx, int32_t scene, size_t n, const float *o, const float *d,
                        const float *tmax, uint8_t *occ) {
   if (!ctx || (n && (!o || !d || !tmax || !occ))) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");

@@ -828,6 +828,28 @@ __global__ void __launch_bounds__(256) k_trace_occluded(DevScene S, uint32_t n, 
 
 int g_query_grid = 1;  // set from the device's SM count and occupancy when a context is created
 
+// IBL::Sample(dir) (src/renderer/IBL.h:30-45) for a set of directions: the
+// render's own env_lookup, so its parity test covers the miss shading.
+__global__ void k_env_sample(DevScene S, uint32_t n, const float *dir, float *rgb) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const V3 c = env_lookup(S, v3(dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]));
+  rgb[3 * (size_t)i] = c.x;
+  rgb[3 * (size_t)i + 1] = c.y;
+  rgb[3 * (size_t)i + 2] = c.z;
+}
+
+// Image::GetPixelByUV (src/tools/Image.h:21-31) of texture `tex` at n (u, v)
+// pairs: the render's own texel().
+__global__ void k_texture_sample(DevScene S, int tex, uint32_t n, const float *uv, float *rgb) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const V3 c = texel(S, tex, uv[2 * (size_t)i], uv[2 * (size_t)i + 1]);
+  rgb[3 * (size_t)i] = c.x;
+  rgb[3 * (size_t)i + 1] = c.y;
+  rgb[3 * (size_t)i + 2] = c.z;
+}
+
 // ---------------------------------------------------------------- batched form kernels
 
 __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
@@ -1070,6 +1092,14 @@ void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const
     k_trace_occluded<<<g_query_grid, 256, 0, st>>>(S, m, orig + 3 * b, dir + 3 * b, tmax + b, occ + b, counters,
                                                    sn);
   }
+}
+
+void launch_env_sample(const DevScene &S, uint32_t n, const float *dir, float *rgb, cudaStream_t st) {
+  if (n) k_env_sample<<<(n + 255) / 256, 256, 0, st>>>(S, n, dir, rgb);
+}
+
+void launch_texture_sample(const DevScene &S, int tex, uint32_t n, const float *uv, float *rgb, cudaStream_t st) {
+  if (n) k_texture_sample<<<(n + 255) / 256, 256, 0, st>>>(S, tex, n, uv, rgb);
 }
 
 const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }

@@ -144,6 +144,8 @@ void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t
 // counters: the context's counter block ([2] error bits, [8] query fetch counter)
 void launch_trace_closest(const DevScene &S, size_t n, const float *orig, const float *dir, int32_t *prim,
                           float *t, float *normal, uint32_t *counters, cudaStream_t st);
+void launch_env_sample(const DevScene &S, uint32_t n, const float *dir, float *rgb, cudaStream_t st);
+void launch_texture_sample(const DevScene &S, int tex, uint32_t n, const float *uv, float *rgb, cudaStream_t st);
 void launch_trace_occluded(const DevScene &S, size_t n, const float *orig, const float *dir,
                            const float *tmax, uint8_t *occ, uint32_t *counters, cudaStream_t st);
 void set_query_grid(int grid);

@@ -313,6 +313,22 @@ class Context:
                                                t.ctypes.data_as(abi.f32p), nrm.ctypes.data_as(abi.f32p)))
         return prim, t, nrm
 
+    def env_sample(self, scene, dirs):
+        """IBL::Sample per unit direction (n x 3) -> n x 3 float32."""
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        out = np.zeros((d.shape[0], 3), np.float32)
+        self._check(self.lib.or3_env_sample(self.h, scene, d.shape[0], d.ctypes.data_as(abi.f32p),
+                                            out.ctypes.data_as(abi.f32p)))
+        return out
+
+    def texture_sample(self, scene, texture, uv):
+        """Image::GetPixelByUV of a scene texture per (u, v) (n x 2) -> n x 3 float32."""
+        u = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        out = np.zeros((u.shape[0], 3), np.float32)
+        self._check(self.lib.or3_texture_sample(self.h, scene, texture, u.shape[0], u.ctypes.data_as(abi.f32p),
+                                                out.ctypes.data_as(abi.f32p)))
+        return out
+
     def trace_occluded(self, scene, origins, dirs, tmax):
         o = np.ascontiguousarray(origins, np.float32)
         d = np.ascontiguousarray(dirs, np.float32)

@@ -11,6 +11,8 @@
                           float sky (gradient + 0.5 degree sun of 1e4 + log-normal
                           background) sampled through its CDF (next-event
                           estimation on); 1920x1080, ss=32 (1024 spp), max depth 12
+  cornell_lens()          the Cornell box through a thin lens (CircleAperture)
+  textured_scene()        textured Lambert quad and sphere under a white background
   reference_cornell()     the reference's own built-in CornellBoxScene
                           (src/scenes/CornellBoxScene.cpp:10-36): axis floors,
                           a two-layer sphere, a SphereLight
@@ -65,6 +67,45 @@ def cornell_box(width=256, height=256):
     sd.add_sphere((70.0, 16.5, 60.0), 16.5, sd.layers(glass))
     settings = dict(supersamples=8, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=3, max_depth=8)
     return sd, cornell_camera(width, height), settings
+
+
+def cornell_lens(width=128, height=128, aperture=1.3, focal=300.0):
+    """The Cornell box seen through a thin lens: CircleAperture(radius) with
+    the focal plane `focal` along z from the eye (Camera.h:65-93,
+    Aperture.h:23-35).  The reference's main() always installs
+    CircleAperture(1.3) with focal distance 300 (src/main.cpp:98-99)."""
+    sd, cam, settings = cornell_box(width, height)
+    cam.aperture_radius = float(aperture)
+    cam.focal_distance = float(focal)
+    return sd, cam, settings
+
+
+def textured_scene(width=96, height=64, seed=9):
+    """Textured Lambert layers under a constant white background: a quad whose
+    uv runs past [0, 1] on every side (the clamp and the x0.99999 rule of
+    Image::GetPixelByUV, src/tools/Image.h:21-31) and a sphere with the
+    reference's lat-long uv (Sphere.h:61-75).  The sphere lies behind the
+    quad's plane and the quad is single-sided, so no bounce from one reaches
+    the other: every camera path's radiance is exactly colour x texel
+    (GetTexturedColor, src/renderer/PathTracer.cpp:327-346) and pixel means
+    have no Monte Carlo noise.  Textures are 37x23 and 29x16 texels of seeded
+    colours."""
+    rng = np.random.default_rng(seed)
+    sd = SceneDesc()
+    t0 = sd.add_texture(rng.uniform(0.05, 1.0, (23, 37, 3)))
+    t1 = sd.add_texture(rng.uniform(0.05, 1.0, (16, 29, 3)))
+    mq = sd.material(abi.OR3_LAMBERT, (0.9, 0.8, 0.7), texture=t0)
+    ms = sd.material(abi.OR3_LAMBERT, (0.85, 0.9, 0.95), texture=t1)
+    c0, c1, c2, c3 = (-60.0, -25.0, 0.0), (-5.0, -25.0, 0.0), (-5.0, 25.0, 0.0), (-60.0, 25.0, 0.0)
+    u0, u1, v0, v1 = -0.2, 1.15, 1.25, -0.1  # uv at x = -60 / -5 and y = -25 / 25
+    uv = {c0: (u0, v0), c1: (u1, v0), c2: (u1, v1), c3: (u0, v1)}
+    tris = [(c0, c1, c2), (c0, c2, c3)]  # face normal +z, toward the camera
+    sd.add_triangles([list(t) for t in tris], sd.layers(mq), uvs=[[uv[c] for c in t] for t in tris])
+    sd.add_sphere((35.0, 0.0, -30.0), 22.0, sd.layers(ms))
+    sd.background = (1.0, 1.0, 1.0)
+    cam = Camera.from_fov(width, height, (0.0, 0.0, 150.0), (0.0, 0.0, 0.0), 34.0)
+    settings = dict(supersamples=2, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=0)
+    return sd, cam, settings
 
 
 def sphere_light_box(width=64, height=64):

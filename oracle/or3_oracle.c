@@ -892,6 +892,28 @@ static v3 texel(const orc_scene *s, int tex, double u, double v) {
   return mk(p[0], p[1], p[2]);
 }
 
+/* The two lookups on their own, for the pin tests: IBL::Sample(dir)
+   (src/renderer/IBL.h:30-45) and Image::GetPixelByUV (src/tools/Image.h:21-31). */
+void orc_env_sample(const orc_scene *s, size_t n, const double *dir, double *rgb) {
+  for (size_t i = 0; i < n; i++) {
+    const v3 c = env_sample(s, mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]));
+    rgb[3 * i] = c.x;
+    rgb[3 * i + 1] = c.y;
+    rgb[3 * i + 2] = c.z;
+  }
+}
+
+int orc_texel(const orc_scene *s, int tex, size_t n, const double *uv, double *rgb) {
+  if (tex < 0 || tex >= s->ntex) return -1;
+  for (size_t i = 0; i < n; i++) {
+    const v3 c = texel(s, tex, uv[2 * i], uv[2 * i + 1]);
+    rgb[3 * i] = c.x;
+    rgb[3 * i + 1] = c.y;
+    rgb[3 * i + 2] = c.z;
+  }
+  return 0;
+}
+
 typedef struct {
   const orc_scene *s;
   const orc_params *p;

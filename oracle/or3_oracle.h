@@ -68,6 +68,9 @@ void orc_encode_rgbe(size_t n, const double *rgb, uint8_t *out);
 void orc_decode_rgbe(size_t n, const uint8_t *rgbe, double *out);
 
 /* Philox4x32-10 as the kernels use it (for the RNG known-answer test). */
+/* IBL::Sample(dir) and Image::GetPixelByUV of texture `tex`, 3 doubles out per input. */
+void orc_env_sample(const orc_scene *s, size_t n, const double *dir, double *rgb);
+int orc_texel(const orc_scene *s, int tex, size_t n, const double *uv, double *rgb);
 void orc_philox(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
 
 #ifdef __cplusplus

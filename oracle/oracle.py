@@ -90,6 +90,8 @@ class CRestatement:
                                    f64p, f64p, f64p]
         lib.orc_philox.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.POINTER(ctypes.c_uint32)]
+        lib.orc_env_sample.argtypes = [ctypes.c_void_p, ctypes.c_size_t, f64p, f64p]
+        lib.orc_texel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, f64p, f64p]
         self.lib = lib
 
     def encode_rgb8(self, rgb, gamma=True):
@@ -155,6 +157,19 @@ class _OracleScene:
                                          _np(d, ctypes.c_double), _np(t, ctypes.c_double))
         return t
 
+    def env_sample(self, dirs):
+        d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+        out = np.zeros((d.shape[0], 3), np.float64)
+        self.orc.lib.orc_env_sample(self.h, d.shape[0], _np(d, ctypes.c_double), _np(out, ctypes.c_double))
+        return out
+
+    def texel(self, tex, uv):
+        u = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+        out = np.zeros((u.shape[0], 3), np.float64)
+        if self.orc.lib.orc_texel(self.h, tex, u.shape[0], _np(u, ctypes.c_double), _np(out, ctypes.c_double)):
+            raise ValueError("no texture %d" % tex)
+        return out
+
     def path_radiance(self, camera, first, count, nthreads=0, **settings):
         cam = camera.to_c()
         p = _params(**settings)
@@ -187,6 +202,8 @@ class Reference:
         lib.orref_scene_create.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.orref_scene_destroy.argtypes = [ctypes.c_void_p]
         lib.orref_closest.argtypes = [ctypes.c_void_p, ctypes.c_size_t, f64p, f64p, i32p, f64p, f64p, f64p]
+        lib.orref_ibl_sample.argtypes = [ctypes.c_void_p, ctypes.c_size_t, f64p, f64p]
+        lib.orref_texel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, f64p, f64p]
         lib.orref_render_moments.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6 + [f64p, f64p, f64p]
         lib.orref_render_scene.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6 + [f64p, f64p]
         if cfg:
@@ -299,6 +316,20 @@ class _RefScene:
                                    _np(ids, ctypes.c_int32), _np(t, ctypes.c_double), _np(nrm, ctypes.c_double),
                                    _np(pos, ctypes.c_double))
         return ids, t, nrm
+
+    def ibl_sample(self, dirs):
+        d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+        out = np.zeros((d.shape[0], 3), np.float64)
+        if self.ref.lib.orref_ibl_sample(self.h, d.shape[0], _np(d, ctypes.c_double), _np(out, ctypes.c_double)):
+            raise ValueError("scene has no IBL")
+        return out
+
+    def texel(self, tex, uv):
+        u = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+        out = np.zeros((u.shape[0], 3), np.float64)
+        if self.ref.lib.orref_texel(self.h, tex, u.shape[0], _np(u, ctypes.c_double), _np(out, ctypes.c_double)):
+            raise ValueError("no texture %d" % tex)
+        return out
 
     def render_moments(self, camera, supersamples=1, min_samples=1, max_samples=1, step_samples=1, nthreads=0,
                        next_event_estimation=False, **_):

@@ -85,6 +85,7 @@ class HarnessScene : public Scene {
   void add(SceneObject *obj, bool inBVH) { AddObject(obj, true, inBVH); }
   Color m_bg;
   std::vector<SceneObject *> byId;  // object id -> object
+  std::vector<int> texIds;          // or3 texture index -> ImageHandler id
   std::unordered_map<const SceneObject *, int32_t> idOf;
 };
 
@@ -128,6 +129,7 @@ void *orref_scene_create(const or3_scene_desc *d, int use_bvh) {
       img->m_image[p] = Color(src[3 * p], src[3 * p + 1], src[3 * p + 2]);
     texIds.push_back(id);
   }
+  s->texIds = texIds;
 
   // (id, class, index) sorted by id = the reference's insertion order.
   struct Rec { uint32_t id; int cls; uint32_t idx; };
@@ -213,6 +215,31 @@ void *orref_scene_create(const or3_scene_desc *d, int use_bvh) {
 }
 
 void orref_scene_destroy(void *p) { delete static_cast<HarnessScene *>(p); }
+
+// IBL::Sample(const Vector3 &) (src/renderer/IBL.h:30-45) of the scene's IBL
+// for n directions (used as given, unit length expected); -1 without an IBL.
+int orref_ibl_sample(void *p, size_t n, const double *dir, double *rgb) {
+  HarnessScene *s = static_cast<HarnessScene *>(p);
+  if (!s->m_ibl.get()) return -1;
+  for (size_t i = 0; i < n; i++) {
+    const Color &c = s->m_ibl->Sample(V(dir + 3 * i));
+    rgb[3 * i] = c.x; rgb[3 * i + 1] = c.y; rgb[3 * i + 2] = c.z;
+  }
+  return 0;
+}
+
+// Image::GetPixelByUV (src/tools/Image.h:20-31) of the scene's texture `tex`.
+int orref_texel(void *p, int tex, size_t n, const double *uv, double *rgb) {
+  HarnessScene *s = static_cast<HarnessScene *>(p);
+  if (tex < 0 || tex >= (int)s->texIds.size()) return -1;
+  Image *img = ImageHandler::GetInstance().GetImage(s->texIds[tex]);
+  if (!img) return -1;
+  for (size_t i = 0; i < n; i++) {
+    const Color &c = img->GetPixelByUV(uv[2 * i], uv[2 * i + 1]);
+    rgb[3 * i] = c.x; rgb[3 * i + 1] = c.y; rgb[3 * i + 2] = c.z;
+  }
+  return 0;
+}
 
 // Closest hit of n rays through Scene::CheckIntersection.
 int orref_closest(void *p, size_t n, const double *orig, const double *dir, int32_t *id,

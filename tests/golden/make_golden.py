@@ -20,6 +20,14 @@ committed and are all the GPU tests need.
                         Color2RGBE and RGBE2Color on seeded colours and bytes,
                         and two .hdr files its writer produced (one run-length
                         encoded, one flat) with what its reader decodes
+  ibl_ref.npz           the reference's IBL::Sample(dir) on seeded directions
+                        (z < 0, the x axis, near the poles, on texel lines) over
+                        two index-coded equirect maps: the texel each one reads
+  texel_ref.npz         the reference's Image::GetPixelByUV on the textured
+                        scene's textures at seeded and edge (u, v)
+  render_textured.npz   the reference's render of the textured scene (no
+                        noise: per-pixel means in float32)
+  render_lens_*.npz     the Cornell box through the reference's thin lens
   scene_ref.npz         the reference's SceneFromExternalFile on
                         tests/golden/scene/full.scene.in (one record per
                         scene object, the IBL's size and texel sum) and its
@@ -104,6 +112,12 @@ RENDERS = {
                     dict(supersamples=8, min_samples=1, max_samples=16, step_samples=1), (3, 8)),
     "refcornell": (lambda: W.reference_cornell(160, 120),
                    dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
+    # thin lens: the reference main()'s CircleAperture(1.3) at focal distance
+    # 300, and a strong depth of field (radius 6, focal plane through the spheres)
+    "lens_main": (lambda: W.cornell_lens(128, 128, 1.3, 300.0),
+                  dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
+    "lens_dof": (lambda: W.cornell_lens(128, 128, 6.0, 200.0),
+                 dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
 }
 
 
@@ -122,9 +136,117 @@ def make_render(name):
     np.savez_compressed(path, digest=scene_digest(sd), mean=mean.astype(np.float16),
                         se=np.sqrt(var).astype(np.float16), n=n, width=cam.width, height=cam.height,
                         rr_min_depth=cfg[0] if cfg else 5, max_depth=cfg[1] if cfg else 0,
+                        aperture=cam.aperture_radius, focal=cam.focal_distance,
                         seconds=sec, **{k: v for k, v in settings.items()})
     print("%s: %dx%d, %d paths/pixel, %.1fs (%.2f Mpaths/s)" % (path, cam.width, cam.height, n, time.time() - t0,
                                                                cam.width * cam.height * n / sec / 1e6))
+
+
+def make_textured():
+    """The reference's render of the textured scene.  Every path's radiance is
+    colour x texel (no noise), so the per-pixel means are stored in float32 and
+    compared by value."""
+    sd, cam, st = W.textured_scene()
+    ref = O.Reference()
+    s, q, sec = ref.scene(sd, use_bvh=False).render_moments(cam, nthreads=os.cpu_count(), **st)
+    n = st["supersamples"] ** 2 * st["max_samples"]
+    path = os.path.join(HERE, "render_textured.npz")
+    np.savez_compressed(path, digest=scene_digest(sd), mean=(s / n).astype(np.float32), n=n,
+                        width=cam.width, height=cam.height, **st)
+    print(path)
+
+
+def _unit_f32(v):
+    v = np.asarray(v, np.float64)
+    v = v / np.linalg.norm(v, axis=1, keepdims=True)
+    return v.astype(np.float32).astype(np.float64)
+
+
+IBL_SIZES = ((64, 32), (37, 19))
+
+
+def ibl_scene(w, h):
+    """A scene with only an index-coded equirect map: texel (x, y) holds
+    (x, y, y * w + x), so a lookup's colour names the texel it read."""
+    sd = W.SceneDesc()
+    m = sd.material(W.abi.OR3_LAMBERT, (0.5, 0.5, 0.5))
+    sd.add_sphere((0.0, 0.0, 0.0), 1.0, sd.layers(m))
+    yy, xx = np.mgrid[0:h, 0:w]
+    sd.set_env(np.stack([xx, yy, yy * w + xx], axis=-1).astype(np.float32))
+    return sd
+
+
+def ibl_directions(seed=31):
+    """Seeded unit directions (FP32 values): uniform on the sphere, the z < 0
+    half and z = -0.0 (IBL::Sample mirrors phi there), the x axis (phi = 0 and
+    pi), near-pole directions, and directions on the texel grid's phi and
+    theta lines.  The exact poles are left out: there the reference takes
+    acos(0 / 0) and converts the NaN to int, which has no defined value."""
+    rng = np.random.default_rng(seed)
+    d = [rng.normal(size=(3000, 3))]
+    z = rng.normal(size=(500, 3))
+    z[:, 2] = -np.abs(z[:, 2])
+    d.append(z)
+    special = [[1, 0, 0], [-1, 0, 0], [1, 0, -0.0], [-1, 0, -0.0], [0, 0, 1], [0, 0, -1], [1, 1, 0], [1, -1, 0],
+               [1, 0.5, -1e-6], [1, 0.5, 1e-6], [-1, 0.5, -1e-6], [-1, -0.5, 1e-6]]
+    for e in (1e-3, 1e-4, 1e-5):
+        for sy in (1, -1):
+            for ang in (0.3, 2.0, 4.0, 5.5):
+                special.append([e * np.cos(ang), sy, e * np.sin(ang)])
+    d.append(np.asarray(special, np.float64))
+    for w, h in IBL_SIZES:  # on phi = 2 pi k / w and theta = pi j / h
+        k = np.arange(w)
+        ph = 2 * np.pi * k / w
+        d.append(np.stack([np.cos(ph) * 0.8, np.full(w, 0.3), np.sin(ph) * 0.8], axis=1))
+        j = np.arange(1, h)
+        th = np.pi * j / h
+        d.append(np.stack([np.sin(th) * 0.6, np.cos(th), np.sin(th) * 0.8], axis=1))
+    return _unit_f32(np.concatenate(d))  # the z = -0.0 entries keep their sign
+
+
+def make_ibl():
+    """IBL::Sample(dir) of the reference on index-coded maps of two sizes."""
+    ref = O.Reference()
+    dirs = ibl_directions()
+    out = dict(dirs=dirs.astype(np.float32), sizes=np.asarray(IBL_SIZES, np.int32))
+    for w, h in IBL_SIZES:
+        c = ref.scene(ibl_scene(w, h), use_bvh=False).ibl_sample(dirs)
+        out["texel_%dx%d" % (w, h)] = c[:, :2].astype(np.int32)
+        assert np.all(c[:, 2] == c[:, 1] * w + c[:, 0])
+    path = os.path.join(HERE, "ibl_ref.npz")
+    np.savez_compressed(path, **out)
+    print(path, dirs.shape)
+
+
+def texel_uvs(tex, seed=32):
+    """(u, v) pairs: seeded over [-0.3, 1.3]^2 (the clamp), the corners and
+    edges 0 and 1 (the x0.99999 rule keeps 1 on the last texel), and the
+    texel grid's lines k / w, k / h."""
+    rng = np.random.default_rng(seed)
+    h, w = tex.shape[:2]
+    uv = [rng.uniform(-0.3, 1.3, (3000, 2))]
+    e = np.array([0.0, 1.0, np.float32(1.0 - 2.0 ** -24), 1e-7, -0.0])
+    uv.append(np.stack(np.meshgrid(e, e), axis=-1).reshape(-1, 2))
+    ku = np.arange(w + 1) / w
+    kv = np.arange(h + 1) / h
+    uv.append(np.stack([ku, np.full(w + 1, 0.37)], axis=1))
+    uv.append(np.stack([np.full(h + 1, 0.61), kv], axis=1))
+    return np.concatenate(uv).astype(np.float32).astype(np.float64)
+
+
+def make_texel():
+    """Image::GetPixelByUV of the reference on the textured scene's two textures."""
+    ref = O.Reference()
+    sd, _, _ = W.textured_scene()
+    rs = ref.scene(sd, use_bvh=False)
+    out = dict(digest=scene_digest(sd))
+    for t, tex in enumerate(sd.textures):
+        uv = texel_uvs(tex, seed=32 + t)
+        out["uv_%d" % t] = uv.astype(np.float32)
+        out["rgb_%d" % t] = rs.texel(t, uv).astype(np.float32)
+    path = os.path.join(HERE, "texel_ref.npz")
+    np.savez_compressed(path, **out)
+    print(path)
 
 
 def make_rmse():
@@ -220,9 +342,18 @@ if __name__ == "__main__":
     if a.only == "scene":
         make_scene()
         sys.exit(0)
-    make_image_codec()
-    make_obj()
-    make_scene()
+    if a.only == "lookups":
+        make_ibl()
+        make_texel()
+        make_textured()
+        sys.exit(0)
+    if not a.only:
+        make_image_codec()
+        make_obj()
+        make_scene()
+        make_ibl()
+        make_texel()
+        make_textured()
     for nm in CLOSEST_SCENES:
         if not a.only or a.only == nm:
             make_closest(nm)

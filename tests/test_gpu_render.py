@@ -32,7 +32,8 @@ def _path_parity(pkg, ctx, orc, sd, cam, use_bvh=True, **settings):
     return gpu, ref, close
 
 
-@pytest.mark.parametrize("case", ["cornell", "cornell_refdepth", "refcornell", "ico_phong", "terrain_env"])
+@pytest.mark.parametrize("case", ["cornell", "cornell_refdepth", "refcornell", "ico_phong", "terrain_env",
+                                  "cornell_lens", "textured"])
 def test_paths_match_oracle(pkg, ctx, orc, case):
     W = pkg.workloads
     if case == "cornell":
@@ -43,6 +44,12 @@ def test_paths_match_oracle(pkg, ctx, orc, case):
         st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
     elif case == "refcornell":
         sd, cam, _ = W.reference_cornell(64, 48)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
+    elif case == "cornell_lens":
+        sd, cam, _ = W.cornell_lens(48, 48, 6.0, 200.0)
+        st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
+    elif case == "textured":
+        sd, cam, _ = W.textured_scene(48, 32)
         st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
     elif case == "ico_phong":
         sd, cam, _ = W.icosphere_in_box(64, 48, level=4)

@@ -72,6 +72,36 @@ def workload(pkg, name):
     return sd, cam, st, desc
 
 
+def rmse_vs_16k(ctx, cam, name):
+    """Image RMSE of the last render against the workload's 16384-spp
+    reference (tests/golden/rmse_*.npz: tiles of an FP64 oracle render for the
+    mesh and terrain, the reference's own full image for the Cornell box),
+    with the RMSE the two renders' noise alone predicts.  None without one."""
+    fname = {"cornell": "rmse_cornell_cfg.npz", "mesh": "rmse_mesh.npz", "terrain": "rmse_terrain.npz"}[name]
+    path = os.path.join(ROOT, "tests", "golden", fname)
+    if not os.path.exists(path):
+        return None
+    g = np.load(path)
+    s, q, n = ctx.moments(cam.width, cam.height)
+    m = s / n
+    se2 = np.maximum(q / n - m * m, 0.0) / n
+    if "tiles" in g.files:
+        H = m.shape[0]
+        d2, v, ref = [], [], []
+        for k, (x0, y0, w, h) in enumerate(g["tiles"].tolist()):
+            rows = H - 1 - (y0 + np.arange(h))
+            d2.append((m[rows, x0:x0 + w] - g["mean"][k]) ** 2)
+            v.append(se2[rows, x0:x0 + w] + g["se"][k].astype(np.float64) ** 2)
+            ref.append(g["mean"][k])
+        what = "16384-spp FP64 oracle render of five 32x32 tiles, same sub-pixel grid"
+    else:
+        d2, v, ref = [(m - g["mean"]) ** 2], [se2 * (1.0 + n / float(g["n"]))], [g["mean"]]
+        what = "the reference's own 16384-spp render of the whole image, same sub-pixel grid"
+    rmse = float(np.sqrt(np.mean(d2)))
+    return {"value": rmse, "expected_from_noise": float(np.sqrt(np.mean(v))),
+            "relative": rmse / float(np.mean(ref)), "spp": int(n), "reference": what}
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -488,6 +518,8 @@ def main():
     barrier(dist)
     wall_s = time.perf_counter() - w0
     clk = clocks.stop()
+    # image error of the last timed render (untimed read of its pixel moments)
+    rmse = rmse_vs_16k(ctx, cam, args.workload) if not (args.res or args.ss) else None
     # the kernel split: one more render of the same step with per-kernel CUDA
     # events (that flag keeps every wave on one stream), untimed
     flush.zero_()
@@ -559,6 +591,7 @@ def main():
                                                  if args.workload in NCU_EXTEND else None),
                          "sm_issue_active_source": (NCU_EXTEND[args.workload]["source"]
                                                     if args.workload in NCU_EXTEND else None)},
+            "rmse_vs_16k": rmse,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,

@@ -14,6 +14,10 @@ committed and are all the GPU tests need.
                         PathTracer::Radiance estimator (float16), sample counts
   rmse_cornell_cfg.npz  (--rmse) 16384-spp reference render of the Cornell
                         workload, the RMSE target
+  rmse_mesh.npz, rmse_terrain.npz  (--only rmse_mesh / rmse_terrain) 16384-spp
+                        FP64 oracle renders of five 32x32 tiles of the mesh and
+                        terrain workloads (their own sub-pixel grids), the RMSE
+                        targets of those workloads
   obj_ref.npz           the reference's Model::ReadFromObj + Transform of
                         tests/golden/obj/mesh.obj (with and without the v flip)
   image_codec.npz       the reference's 8-bit conversion (gamma on and off),
@@ -262,6 +266,56 @@ def make_rmse():
     print("%s: %d spp, %.0fs" % (path, n, sec))
 
 
+# 16384-spp references of the benchmark workloads, on five 32x32 tiles (the
+# four quadrant centres and the image centre), with the workload's own
+# sub-pixel grid (the estimator converges to the grid-sampled pixel), from the
+# FP64 C oracle: the mesh's Phong lobe and the terrain's light sampling have
+# no counterpart in the reference, and the oracle is pinned to the reference
+# wherever they overlap.
+RMSE_CONFIGS = {"mesh": lambda: W.icosphere_in_box(), "terrain": lambda: W.terrain_ibl()}
+RMSE_SEED = 0x5EED16
+
+
+def rmse_tiles(width, height, size=32):
+    cs = [(width // 4, height // 4), (3 * width // 4, height // 4), (width // 4, 3 * height // 4),
+          (3 * width // 4, 3 * height // 4), (width // 2, height // 2)]
+    return np.asarray([(cx - size // 2, cy - size // 2, size, size) for cx, cy in cs], np.int32)
+
+
+def make_rmse_config(name, spp=16384):
+    """Tiles (x0, y0 in camera rows counted from the bottom, w, h) of the
+    workload rendered at `spp` samples per pixel: per-pixel FP64 means and
+    standard errors, rows of each tile bottom-up."""
+    sd, cam, st = RMSE_CONFIGS[name]()
+    orc = O.CRestatement()
+    scene = orc.scene(sd, use_bvh=True)
+    ss2 = st["supersamples"] ** 2
+    samples = spp // ss2
+    kw = dict(supersamples=st["supersamples"], min_samples=1, max_samples=samples, step_samples=samples,
+              rr_min_depth=st["rr_min_depth"], max_depth=st["max_depth"], seed=RMSE_SEED,
+              next_event_estimation=st.get("next_event_estimation", False))
+    tiles = rmse_tiles(cam.width, cam.height)
+    S = np.zeros((len(tiles), 32, 32, 3))
+    Q = np.zeros_like(S)
+    t0 = time.time()
+    for k, (x0, y0, w, h) in enumerate(tiles.tolist()):  # Python ints: path indices pass 2^31
+        for j in range(h):
+            for s_ in range(samples):
+                g = ((s_ * cam.height + y0 + j) * cam.width + x0) * ss2
+                r = scene.path_radiance(cam, g, w * ss2, nthreads=os.cpu_count(), **kw).reshape(w, ss2, 3)
+                S[k, j] += r.sum(axis=1)
+                Q[k, j] += (r * r).sum(axis=1)
+    sec = time.time() - t0
+    n = samples * ss2
+    mean = S / n
+    se = np.sqrt(np.maximum(Q / n - mean * mean, 0.0) / n)
+    path = os.path.join(HERE, "rmse_%s.npz" % name)
+    np.savez_compressed(path, digest=scene_digest(sd), tiles=tiles, mean=mean.astype(np.float32),
+                        se=se.astype(np.float32), n=n, seconds=sec, seed=RMSE_SEED, width=cam.width,
+                        height=cam.height, **{k: v for k, v in kw.items() if k != "seed"})
+    print("%s: %d tiles, %d spp, %.0fs" % (path, len(tiles), n, sec))
+
+
 OBJ_TRANSFORM = dict(position=(10.0, -5.0, 3.0), scaling=(2.0, 1.0, 0.5), rotation=(0.3, -0.2, 0.7))
 
 
@@ -332,6 +386,9 @@ if __name__ == "__main__":
         O.build_oracle(reference=True)
     if a.rmse:
         make_rmse()
+        sys.exit(0)
+    if a.only.startswith("rmse_"):
+        make_rmse_config(a.only[5:])
         sys.exit(0)
     if a.only == "image_codec":
         make_image_codec()

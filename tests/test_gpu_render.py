@@ -114,6 +114,39 @@ def test_rmse_against_16k_reference(pkg, ctx):
     assert rmse > 0.5 * expect, (rmse, expect)
 
 
+def tile_rmse(fixture, m, se):
+    """RMSE of image moments (rows top-down) against a tiled 16384-spp
+    reference (tile rows counted from the bottom, as camera rows), and the
+    RMSE the two renders' own noise predicts."""
+    H = m.shape[0]
+    d2, v = [], []
+    for k, (x0, y0, w, h) in enumerate(fixture["tiles"].tolist()):
+        rows = H - 1 - (y0 + np.arange(h))
+        d2.append((m[rows, x0:x0 + w] - fixture["mean"][k]) ** 2)
+        v.append(se[rows, x0:x0 + w] ** 2 + fixture["se"][k].astype(np.float64) ** 2)
+    return float(np.sqrt(np.mean(d2))), float(np.sqrt(np.mean(v)))
+
+
+@pytest.mark.parametrize("name", ["mesh", "terrain"])
+def test_rmse_of_benchmark_workloads_against_16k_oracle(pkg, ctx, name):
+    # the full benchmark render (its resolution, sub-pixel grid, depth and
+    # light sampling) against the FP64 oracle's 16384-spp tiles
+    g = golden("rmse_%s.npz" % name)
+    sd, cam, st = pkg.workloads.icosphere_in_box() if name == "mesh" else pkg.workloads.terrain_ibl()
+    assert sd.digest() == str(g["digest"])
+    assert (int(g["width"]), int(g["height"]), int(g["supersamples"])) == (cam.width, cam.height,
+                                                                           st["supersamples"])
+    sid = ctx.upload(sd)
+    try:
+        ctx.render(sid, cam, seed=7, **st)
+        s, q, n = ctx.moments(cam.width, cam.height)
+    finally:
+        ctx.release(sid)
+    m, se = moments_to_mean_se(s, q, n)
+    rmse, expect = tile_rmse(g, m, se)
+    assert 0.7 * expect < rmse < 1.3 * expect, (rmse, expect)
+
+
 def test_frame_layout_and_progressive_callbacks(pkg, ctx):
     sd, cam, _ = pkg.workloads.cornell_box(40, 24)
     sid = ctx.upload(sd)

@@ -279,6 +279,22 @@ def run_batched(args, pkg):
     best = {}
     if args.autotune:
         best, _ = ctx.autotune_batch(jobs, sample_paths=1 << 25)
+    if args.wave_paths:
+        best["wave_paths"] = args.wave_paths
+    if args.one_lane:
+        best["flags"] = best.get("flags", 0) | pkg.abi.OR3_FLAG_ONE_LANE
+    if args.batch_flags:
+        best["flags"] = best.get("flags", 0) | args.batch_flags
+    if args.batch_only:
+        # the batched form alone (a small-footprint run for profiling): no plain renders
+        for _ in range(max(args.warmup, 1)):
+            ctx.render_batch(jobs[:4], **best)
+        ms = [ctx.render_batch(jobs, **best)[0]["render_ms"] for _ in range(args.steps)]
+        print(json.dumps({"form": "batched", "batch_only": True, "value": paths / float(np.median(ms)) / 1e3,
+                          "unit": "Mpaths/s", "ms": float(np.median(ms)), "jobs": len(jobs),
+                          "camera_paths": int(paths), "triangles_total": int(tris), "tuning": best}), flush=True)
+        ctx.close()
+        return
     for _ in range(max(args.warmup, 1)):
         ctx.render_batch(jobs[:4], **best)
         for sid, cam, st in jobs[:4]:
@@ -438,6 +454,12 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--wave-paths", type=int, default=0, help="batched form: camera paths per wave (0 = library default)")
+    ap.add_argument("--one-lane", action="store_true", help="batched form: every wave on one stream")
+    ap.add_argument("--batch-flags", type=int, default=0,
+                    help="batched form: extra or3_batch_params.flags (OR3_FLAG_QUANTISED_NODES 128, "
+                         "OR3_FLAG_RELOAD_SCENE 256)")
+    ap.add_argument("--batch-only", action="store_true", help="batched form only, no plain renders (profiling)")
     ap.add_argument("--mix", default="config", choices=["config", "small"],
                     help="batched jobs: the stated mix, or small jobs (64-256 px, 16-64 spp)")
     ap.add_argument("--scenes", type=int, default=32)

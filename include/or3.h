@@ -158,6 +158,10 @@ typedef struct or3_camera {
 #define OR3_FLAG_TIME_KERNELS 16u      /* CUDA events around every extend/shade launch */
 #define OR3_FLAG_COUNT_TRAVERSAL 32u   /* count nodes and primitives visited (slower) */
 #define OR3_FLAG_ONE_LANE 64u          /* batched form: every wave on one stream (default: three that overlap) */
+#define OR3_FLAG_QUANTISED_NODES 128u  /* batched form: traverse the 64-byte nodes with 8-bit child boxes
+                                          (default: the 128-byte FP32-box nodes) */
+#define OR3_FLAG_RELOAD_SCENE 256u     /* batched form: read each ray's node array through its scene
+                                          descriptor every step (default: copied to registers per ray) */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */

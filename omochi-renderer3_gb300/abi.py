@@ -30,6 +30,8 @@ OR3_FLAG_NO_GRAPH = 4
 OR3_FLAG_TIME_KERNELS = 16
 OR3_FLAG_COUNT_TRAVERSAL = 32
 OR3_FLAG_ONE_LANE = 64
+OR3_FLAG_QUANTISED_NODES = 128
+OR3_FLAG_RELOAD_SCENE = 256
 
 API_VERSION = 1
 OR3_API_VERSION = API_VERSION

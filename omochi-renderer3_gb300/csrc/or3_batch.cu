@@ -265,13 +265,15 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
 
   // the bounce loop, captured once per call and lane
   auto lane_batch = [&](int l) { return Batch{B.scenes, B.jobs, B.lanes[l].segs, B.lanes[l].info}; };
+  // traversal variant: node layout and how a ray's node array is reached
+  const int tvar = ((bp->flags & OR3_FLAG_QUANTISED_NODES) ? 1 : 0) | ((bp->flags & OR3_FLAG_RELOAD_SCENE) ? 2 : 0);
   auto launch_bounces = [&](int l) {
     const Batch b = lane_batch(l);
     for (int k = 0; k < unroll; k++) {
       const int in = k & 1;
-      launch_extend_batch(b, ql[l], in, grid_ext, count, sl[l]);
+      launch_extend_batch(b, ql[l], in, grid_ext, count, tvar, sl[l]);
       launch_shade_batch(b, ql[l], in, grid_sh, shadows, sl[l]);
-      if (shadows) launch_shadow_batch(b, ql[l], grid_ext, sl[l]);
+      if (shadows) launch_shadow_batch(b, ql[l], grid_ext, tvar, sl[l]);
       launch_reset_count(ql[l], in, sl[l]);
     }
   };

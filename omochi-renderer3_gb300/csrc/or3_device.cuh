@@ -365,9 +365,21 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &s, uint3
   return !trav_pop(s, stk_e, stk_t);
 }
 
+// What a traversal step reads of a scene (fnodes or nodes every step, prims
+// per leaf): a DevScene, or a TravView for the batched kernels, whose rays
+// each name their scene.  TravView holds the node array in registers, copied
+// once when a lane takes a ray, so the dependent node fetch of every step
+// does not wait on a reload of the scene descriptor; the record array is
+// read through the descriptor (`prims` refers to its field), once per leaf.
+struct TravView {
+  const float4 *fnodes;
+  const uint4 *nodes;
+  const float4 *const &prims;
+};
+
 // Tests the primitives of one leaf slot (triangles then spheres).
-template <bool COUNT>
-__device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint32_t first, uint32_t c,
+template <bool COUNT, class SV>
+__device__ __forceinline__ void trav_leaf(const SV &S, TravState &s, uint32_t first, uint32_t c,
                                           uint32_t *cnt) {
   const uint32_t ntri = c & 15u, nsph = c >> 4;
   if (COUNT) {
@@ -405,8 +417,8 @@ __device__ __forceinline__ void trav_leaf(const DevScene &S, TravState &s, uint3
 // The stack cannot overflow here (depth bound checked at upload, push index
 // clamped), so `err` is not written on this path; the signature matches
 // trav_step's.
-template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true>
-__device__ __forceinline__ bool trav_step_inline(const DevScene &S, TravState &s, STK &stk,
+template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true, class SV = DevScene>
+__device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK &stk,
                                                  const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
   const uint32_t e = s.entry;
   if (e == kNoEntry) return true;

@@ -875,14 +875,20 @@ __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
 }
 
 // persistent_trace (STEP 2) with the scene chosen per ray by its segment
-// (src.load also returns the ray's segment).
-template <bool ANY, bool COUNT, class Src, class Sink>
+// (src.load also returns the ray's segment).  The scene's node and record
+// arrays are copied into registers when a lane takes a ray (TravView), so a
+// step's node fetch does not wait on a reload of the scene descriptor.
+// FN: the FP32-box nodes (else the 64-byte quantised ones).  HOIST false:
+// every step reads the node array through the scene descriptor instead.
+template <bool ANY, bool COUNT, class Src, class Sink, bool FN = true, bool HOIST = true>
 __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t *fetch, const Src &src,
                                             const Sink &sink, uint32_t *cnt, uint32_t *err) {
   uint2 stk_p[kStackSize];
   PairStack stk{stk_p};
   TravState st;
-  const DevScene *sp = nullptr;
+  const DevScene *sp = b.scenes;  // the ray's scene
+  const float4 *fnodes = nullptr;
+  const uint4 *nodes = nullptr;
   uint32_t r = kNoEntry;
   bool drained = false;  // warp-uniform: the shared fetch counter has passed n
   const uint32_t lane = threadIdx.x & 31u;
@@ -901,6 +907,10 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
         uint32_t tag;
         src.load(idx, o, d, tmax, tag);
         sp = &b.scenes[b.jobs[b.segs[tag].job].scene];
+        if (HOIST) {
+          fnodes = sp->fnodes;
+          nodes = sp->nodes;
+        }
         trav_init(st, o, d, tmax, sp->num_nodes);
         r = idx;
       }
@@ -909,7 +919,14 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
       break;
     }
     if (r != kNoEntry) {
-      if (trav_step_inline<ANY, COUNT, true, PairStack>(*sp, st, stk, nullptr, 0u, cnt, err)) {
+      bool done;
+      if (HOIST) {
+        const TravView tv{fnodes, nodes, sp->prims};
+        done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(tv, st, stk, nullptr, 0u, cnt, err);
+      } else {
+        done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(*sp, st, stk, nullptr, 0u, cnt, err);
+      }
+      if (done) {
         sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);
         r = kNoEntry;
       }
@@ -935,7 +952,7 @@ struct BatchShadowSrc {
   }
 };
 
-template <bool COUNT>
+template <bool COUNT, bool FN = true, bool HOIST = true>
 __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int in) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -943,8 +960,9 @@ __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int 
     if (n) atomicAdd(&q.stats[2], 1ull);
   }
   uint32_t cnt[3] = {0u, 0u, 0u};
-  batch_trace<false, COUNT>(b, n, &q.counters[4 + in], BatchQueueSrc{q.orig[in], q.dir[in], q.beta[in]},
-                            HitSink{q.hits}, cnt, &q.counters[2]);
+  batch_trace<false, COUNT, BatchQueueSrc, HitSink, FN, HOIST>(
+      b, n, &q.counters[4 + in], BatchQueueSrc{q.orig[in], q.dir[in], q.beta[in]}, HitSink{q.hits}, cnt,
+      &q.counters[2]);
   if (COUNT) {
     unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];
 #pragma unroll
@@ -961,11 +979,13 @@ __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int 
   }
 }
 
+template <bool FN = true, bool HOIST = true>
 __global__ void __launch_bounds__(256, 4) k_shadow_batch(Batch b, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  batch_trace<true, false>(b, n, &q.counters[6], BatchShadowSrc{q.sorig, q.sdir, q.scontrib},
-                           ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, &q.counters[2]);
+  batch_trace<true, false, BatchShadowSrc, ShadowSink, FN, HOIST>(
+      b, n, &q.counters[6], BatchShadowSrc{q.sorig, q.sdir, q.scontrib}, ShadowSink{q.sorig, q.scontrib, q.pathL},
+      nullptr, &q.counters[2]);
 }
 
 // One thread per pixel-sample group (ss2 consecutive paths of one pixel and
@@ -1049,8 +1069,13 @@ void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, 
   else k_shadow<true, true><<<grid, 256, 0, st>>>(S, q);
 }
 
-void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st) {
-  k_shadow_batch<<<grid, 256, 0, st>>>(b, q);
+void launch_shadow_batch(const Batch &b, const Queues &q, int grid, int variant, cudaStream_t st) {
+  switch (variant & 3) {
+    case 1: k_shadow_batch<false, true><<<grid, 256, 0, st>>>(b, q); break;
+    case 2: k_shadow_batch<true, false><<<grid, 256, 0, st>>>(b, q); break;
+    case 3: k_shadow_batch<false, false><<<grid, 256, 0, st>>>(b, q); break;
+    default: k_shadow_batch<true, true><<<grid, 256, 0, st>>>(b, q); break;
+  }
 }
 
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
@@ -1114,9 +1139,20 @@ void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, in
   k_raygen_batch<<<(num_paths + 255) / 256 > 0 ? (num_paths + 255) / 256 : 1, 256, 0, st>>>(b, num_paths, q, out);
 }
 
-void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, cudaStream_t st) {
-  if (count) k_extend_batch<true><<<grid, 256, 0, st>>>(b, q, in);
-  else k_extend_batch<false><<<grid, 256, 0, st>>>(b, q, in);
+// variant bit 0: quantised 64-byte nodes; bit 1: node array read through the
+// scene descriptor every step (the form before it was hoisted)
+void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, int variant,
+                         cudaStream_t st) {
+  if (count) {
+    k_extend_batch<true><<<grid, 256, 0, st>>>(b, q, in);
+    return;
+  }
+  switch (variant & 3) {
+    case 1: k_extend_batch<false, false, true><<<grid, 256, 0, st>>>(b, q, in); break;
+    case 2: k_extend_batch<false, true, false><<<grid, 256, 0, st>>>(b, q, in); break;
+    case 3: k_extend_batch<false, false, false><<<grid, 256, 0, st>>>(b, q, in); break;
+    default: k_extend_batch<false, true, true><<<grid, 256, 0, st>>>(b, q, in); break;
+  }
 }
 
 void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool nee, cudaStream_t st) {

@@ -104,7 +104,8 @@ struct Batch {
 };
 
 void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, int out, cudaStream_t st);
-void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, cudaStream_t st);
+void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, int variant,
+                         cudaStream_t st);
 // nee: some job samples lights (the light-sampling instance of the kernel)
 void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool nee, cudaStream_t st);
 void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st);
@@ -134,7 +135,7 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);
-void launch_shadow_batch(const Batch &b, const Queues &q, int grid, cudaStream_t st);
+void launch_shadow_batch(const Batch &b, const Queues &q, int grid, int variant, cudaStream_t st);
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st);
 void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,

@@ -561,9 +561,9 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
       return bail(fail(ctx, OR3_ERR_CUDA, "graph capture"));
     for (int k = 0; k < S->unroll; k++) {
       const int in = k & 1;
-      launch_extend_batch(b, L.q, in, ctx->num_sms * ctx->occ_extend, false, L.st);
+      launch_extend_batch(b, L.q, in, ctx->num_sms * ctx->occ_extend, false, 0, L.st);
       launch_shade_batch(b, L.q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows, L.st);
-      if (shadows) launch_shadow_batch(b, L.q, ctx->num_sms * ctx->occ_extend, L.st);
+      if (shadows) launch_shadow_batch(b, L.q, ctx->num_sms * ctx->occ_extend, 0, L.st);
       launch_reset_count(L.q, in, L.st);
     }
     if (cudaStreamEndCapture(L.st, &graph) != cudaSuccess || cudaGraphInstantiate(&L.graph, graph, 0) != cudaSuccess) {

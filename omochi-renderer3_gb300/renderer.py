@@ -480,6 +480,37 @@ def _scene_file_open(path, threads):
     return lib, fp
 
 
+def scene_from_desc(d):
+    """A SceneDesc holding a copy of an or3_scene_desc's arrays (ids kept;
+    triangles need their normal, uv and id arrays; textures are not copied)."""
+    from .scene import SceneDesc
+    sd = SceneDesc()
+    for i in range(d.num_materials):
+        m = d.materials[i]
+        sd.material(m.type, tuple(m.color), tuple(m.emission), m.ior, m.phong_exponent, m.texture)
+    sd.layer_material = [d.layer_material[i] for i in range(d.num_layers)]
+    sd.layer_rate = [d.layer_rate[i] for i in range(d.num_layers)]
+    n = d.num_triangles
+    if n:
+        arr = np.ctypeslib.as_array
+        sd.tris.append((arr(d.tri_vertices, shape=(n, 3, 3)).copy(), arr(d.tri_normals, shape=(n, 3, 3)).copy(),
+                        arr(d.tri_uvs, shape=(n, 3, 2)).copy(), arr(d.tri_layers, shape=(n, 2)).copy(),
+                        arr(d.tri_ids, shape=(n,)).copy()))
+    for i in range(d.num_spheres):
+        sd.spheres.append((*(d.spheres[4 * i + k] for k in range(4)), d.sphere_layers[2 * i],
+                           d.sphere_layers[2 * i + 1], d.sphere_flags[i] if d.sphere_flags else 0, d.sphere_ids[i]))
+    for i in range(d.num_planes):
+        sd.planes.append((*(d.planes[4 * i + k] for k in range(4)), d.plane_layers[2 * i],
+                          d.plane_layers[2 * i + 1], d.plane_ids[i]))
+    sd._next_id = n + d.num_spheres + d.num_planes
+    sd.background = tuple(d.background)
+    if d.env_rgbe:
+        sd.set_env_rgbe(np.ctypeslib.as_array(d.env_rgbe, shape=(d.env_height, d.env_width, 4)).copy())
+    elif d.env_rgb:
+        sd.set_env(np.ctypeslib.as_array(d.env_rgb, shape=(d.env_height, d.env_width, 3)).copy())
+    return sd
+
+
 def load_scene_file(path, threads=0):
     """The reference's text scene file (SceneFromExternalFile) -> (SceneDesc, info).
 
@@ -487,32 +518,11 @@ def load_scene_file(path, threads=0):
     with the file's object ids.  info: space_partitioning, ibl_path, meshes,
     textures (image path per material, or None).
     """
-    from .scene import SceneDesc
     lib, fp = _scene_file_open(path, threads)
     try:
         f = fp.contents
         d = f.desc
-        sd = SceneDesc()
-        for i in range(d.num_materials):
-            m = d.materials[i]
-            sd.material(m.type, tuple(m.color), tuple(m.emission), m.ior, m.phong_exponent, m.texture)
-        sd.layer_material = [d.layer_material[i] for i in range(d.num_layers)]
-        sd.layer_rate = [d.layer_rate[i] for i in range(d.num_layers)]
-        n = d.num_triangles
-        if n:
-            arr = np.ctypeslib.as_array
-            sd.tris.append((arr(d.tri_vertices, shape=(n, 3, 3)).copy(), arr(d.tri_normals, shape=(n, 3, 3)).copy(),
-                            arr(d.tri_uvs, shape=(n, 3, 2)).copy(), arr(d.tri_layers, shape=(n, 2)).copy(),
-                            arr(d.tri_ids, shape=(n,)).copy()))
-        for i in range(d.num_spheres):
-            sd.spheres.append((*(d.spheres[4 * i + k] for k in range(4)), d.sphere_layers[2 * i],
-                               d.sphere_layers[2 * i + 1], d.sphere_flags[i], d.sphere_ids[i]))
-        for i in range(d.num_planes):
-            sd.planes.append((*(d.planes[4 * i + k] for k in range(4)), d.plane_layers[2 * i],
-                              d.plane_layers[2 * i + 1], d.plane_ids[i]))
-        sd._next_id = n + d.num_spheres + d.num_planes
-        if d.env_rgbe:
-            sd.set_env_rgbe(np.ctypeslib.as_array(d.env_rgbe, shape=(d.env_height, d.env_width, 4)).copy())
+        sd = scene_from_desc(d)
         info = {
             "space_partitioning": f.space_partitioning.decode(),
             "ibl_path": f.ibl_path.decode() if f.ibl_path else None,

@@ -40,10 +40,11 @@ def _plain(ctx, sid, cam, st):
     return s, q, n, img
 
 
-@pytest.mark.parametrize("wave_paths,flags", [(0, 0), (3000, 0), (3000, 64)])
+@pytest.mark.parametrize("wave_paths,flags", [(0, 0), (3000, 0), (3000, 64), (3000, 256)])
 def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags):
     """flags 64 = OR3_FLAG_ONE_LANE (every wave on one stream; the default
-    deals waves to three lanes)."""
+    deals waves to three lanes); 256 = OR3_FLAG_RELOAD_SCENE (the node array
+    read through the scene descriptor every step: the same traversal)."""
     sids, jobs = _jobs(pkg, ctx)
     try:
         alone = [_plain(ctx, *j) for j in jobs]
@@ -63,6 +64,28 @@ def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags):
     finally:
         for s in sids:
             ctx.release(s)
+
+
+@pytest.mark.parametrize("flags", [128, 128 | 256])
+def test_batch_over_quantised_nodes(pkg, ctx, flags):
+    """OR3_FLAG_QUANTISED_NODES: the 64-byte nodes bound the same leaves more
+    loosely, so the same closest hits are found in another order; only hits at
+    exactly equal distance (shared edges) can resolve to the other primitive."""
+    sids, jobs = _jobs(pkg, ctx)
+    try:
+        ctx.render_batch(jobs, wave_paths=3000)
+        ref = [ctx.batch_moments(k, c.width, c.height) for k, (_, c, _) in enumerate(jobs)]
+        ctx.render_batch(jobs, wave_paths=3000, flags=flags)
+        for k, (sid, cam, st) in enumerate(jobs):
+            s, q, n = ctx.batch_moments(k, cam.width, cam.height)
+            s0, _, n0 = ref[k]
+            assert n == n0
+            off = np.abs(s - s0) > 1e-5 * np.abs(s0) + 1e-6
+            assert off.mean() < 0.005, (k, off.mean())
+            assert abs(s.sum() - s0.sum()) <= 2e-3 * abs(s0.sum())
+    finally:
+        for s_ in sids:
+            ctx.release(s_)
 
 
 def test_batch_without_graph_and_autotune(pkg, ctx):

@@ -154,7 +154,9 @@ def sky_floor(width=64, height=64, env=(256, 128), seed=3, constant=None):
     return sd, cam
 
 
-def icosphere_in_box(width=1024, height=768, level=6, seed=2):
+def icosphere_in_box(width=1024, height=768, level=6, seed=2, glossy_faces=True):
+    """glossy_faces False: every face Lambert 0.8 (a scene the reference's own
+    integrator can render, which has no glossy lobe)."""
     rng = np.random.default_rng(seed)
     sd = SceneDesc()
     white = sd.material(abi.OR3_LAMBERT, (0.75, 0.75, 0.75))
@@ -173,6 +175,8 @@ def icosphere_in_box(width=1024, height=768, level=6, seed=2):
     lam = sd.layers(diffuse)
     mix = sd.layers([(diffuse, 0.5), (gloss, 0.5)])
     glossy = rng.random(len(f)) < 0.5
+    if not glossy_faces:
+        glossy[:] = False
     lay = np.where(glossy[:, None], np.array(mix, np.uint32), np.array(lam, np.uint32)).astype(np.uint32)
     sd.add_triangles(pos[f], lay, normals=vn[f])
     settings = dict(supersamples=16, min_samples=1, max_samples=1, step_samples=1, rr_min_depth=5, max_depth=10)

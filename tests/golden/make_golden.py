@@ -117,10 +117,11 @@ RENDERS = {
     "refcornell": (lambda: W.reference_cornell(160, 120),
                    dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
     # thin lens: the reference main()'s CircleAperture(1.3) at focal distance
-    # 300, and a strong depth of field (radius 6, focal plane through the spheres)
+    # 300, and a strong depth of field (radius 20, focal plane at the box's
+    # front z = 100: the spheres blur over ~5 pixels, the back wall over ~9)
     "lens_main": (lambda: W.cornell_lens(128, 128, 1.3, 300.0),
                   dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
-    "lens_dof": (lambda: W.cornell_lens(128, 128, 6.0, 200.0),
+    "lens_dof": (lambda: W.cornell_lens(128, 128, 20.0, 150.0),
                  dict(supersamples=4, min_samples=1, max_samples=64, step_samples=1), None),
 }
 

@@ -12,7 +12,8 @@
   * Camera::SampleRayForPixel with CircleAperture (Camera.h:65-93,
     Aperture.h:23-35): per-pixel 3-SE agreement with the reference's renders
     through the lens of its main() (radius 1.3, focal distance 300) and a
-    strong depth of field (radius 6, focal plane through the spheres), one
+    strong depth of field (radius 20, focal plane at the box's front, the
+    back wall blurred over ~9 pixels), one
     lens sample per sub-pixel per pass as in the reference.
 """
 import sys
@@ -74,7 +75,8 @@ def test_texture_sample_matches_reference(pkg, ctx):
             got = ctx.texture_sample(sid, t, uv)
             h, w = tex.shape[:2]
             cu = np.clip(uv.astype(np.float64), 0.0, 1.0) * 0.99999
-            tie = _near_edge(cu[:, 0] * w, 2e-5) | _near_edge(cu[:, 1] * h, 2e-5)
+            # an edge inside the texture (a coordinate clamped to 0 reads texel 0 on both sides)
+            tie = (_near_edge(cu[:, 0] * w, 2e-5) & (cu[:, 0] > 0)) | (_near_edge(cu[:, 1] * h, 2e-5) & (cu[:, 1] > 0))
             bad = np.any(got != g["rgb_%d" % t], axis=1) & ~tie
             assert not bad.any(), (t, np.nonzero(bad)[0][:8], uv[bad][:4])
             assert tie.mean() < 0.05
@@ -109,7 +111,7 @@ def test_textured_render_matches_reference(pkg, ctx):
 
 
 @pytest.mark.parametrize("fixture,aperture,focal", [("render_lens_main.npz", 1.3, 300.0),
-                                                     ("render_lens_dof.npz", 6.0, 200.0)])
+                                                     ("render_lens_dof.npz", 20.0, 150.0)])
 def test_thin_lens_render_matches_reference(pkg, ctx, fixture, aperture, focal):
     g = golden(fixture)
     sd, cam, _ = pkg.workloads.cornell_lens(int(g["width"]), int(g["height"]), aperture, focal)
@@ -146,4 +148,5 @@ def test_lens_changes_the_image(pkg, ctx):
         ctx.release(sid)
     m, se = moments_to_mean_se(s, q, n)
     z = zscores(m, se, n, g["mean"], g["se"], int(g["n"]))
-    assert np.mean(np.abs(z) > 3) > 0.05, np.mean(np.abs(z) > 3)
+    # the reference-render test allows 1% of pixels beyond 3 SE, so a pinhole would fail it
+    assert np.mean(np.abs(z) > 3) > 0.02, np.mean(np.abs(z) > 3)

@@ -46,7 +46,7 @@ def test_paths_match_oracle(pkg, ctx, orc, case):
         sd, cam, _ = W.reference_cornell(64, 48)
         st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
     elif case == "cornell_lens":
-        sd, cam, _ = W.cornell_lens(48, 48, 6.0, 200.0)
+        sd, cam, _ = W.cornell_lens(48, 48, 20.0, 150.0)
         st = dict(supersamples=4, rr_min_depth=5, max_depth=0)
     elif case == "textured":
         sd, cam, _ = W.textured_scene(48, 32)

@@ -47,7 +47,7 @@ def test_oracle_textured_render_matches_reference(pkg, orc):
 
 
 def test_lens_fixtures_carry_their_camera(pkg):
-    for name, ap, foc in (("render_lens_main.npz", 1.3, 300.0), ("render_lens_dof.npz", 6.0, 200.0)):
+    for name, ap, foc in (("render_lens_main.npz", 1.3, 300.0), ("render_lens_dof.npz", 20.0, 150.0)):
         g = golden(name)
         sd, cam, _ = pkg.workloads.cornell_lens(int(g["width"]), int(g["height"]), ap, foc)
         assert sd.digest() == str(g["digest"])
@@ -60,7 +60,7 @@ def test_oracle_thin_lens_matches_reference(pkg, orc):
     # thin-lens render: per-pixel 3-SE agreement
     from conftest import moments_to_mean_se, zscores
     g = golden("render_lens_dof.npz")
-    sd, cam, _ = pkg.workloads.cornell_lens(int(g["width"]), int(g["height"]), 6.0, 200.0)
+    sd, cam, _ = pkg.workloads.cornell_lens(int(g["width"]), int(g["height"]), 20.0, 150.0)
     s, q, _ = orc.scene(sd, use_bvh=False).render(cam, nthreads=os.cpu_count(), supersamples=int(g["supersamples"]),
                                                    min_samples=1, max_samples=int(g["max_samples"]), step_samples=1,
                                                    seed=17, rr_min_depth=5, max_depth=0)

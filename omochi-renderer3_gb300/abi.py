@@ -162,6 +162,8 @@ OR3_TUNE_SHADE_NEE_OCC4 = 0x80
 OR3_TUNE_ONE_LANE = 0x100
 OR3_TUNE_TWO_LANES = 0x200
 OR3_TUNE_FOUR_LANES = 0x400
+OR3_TUNE_SORTED_SHADE = 0x800
+OR3_TUNE_BLOCK_APPEND = 0x1000
 
 # name -> (restype, argtypes); every function declared in include/or3.h
 PROTOTYPES = {

@@ -211,7 +211,9 @@ int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   cudaFree(ctx->sorig);
   cudaFree(ctx->sdir);
   cudaFree(ctx->scontrib);
+  cudaFree(ctx->slist);
   ctx->hits = ctx->pathL = ctx->sorig = ctx->sdir = ctx->scontrib = nullptr;
+  ctx->slist = nullptr;
   ctx->cap_paths = ctx->cap_rays = 0;
   for (int k = 0; k < 2; k++) {
     OR3_CUDA(ctx, cudaMalloc(&ctx->qorig[k], rays * sizeof(float4)));
@@ -223,6 +225,7 @@ int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   OR3_CUDA(ctx, cudaMalloc(&ctx->sorig, rays * sizeof(float4)));
   OR3_CUDA(ctx, cudaMalloc(&ctx->sdir, rays * sizeof(float4)));
   OR3_CUDA(ctx, cudaMalloc(&ctx->scontrib, rays * sizeof(float4)));
+  OR3_CUDA(ctx, cudaMalloc(&ctx->slist, rays * sizeof(uint32_t)));
   ctx->cap_paths = paths;
   ctx->cap_rays = rays;
   return OR3_OK;
@@ -260,6 +263,7 @@ Queues make_queues(or3_context *ctx) {
   q.sorig = ctx->sorig;
   q.sdir = ctx->sdir;
   q.scontrib = ctx->scontrib;
+  q.slist = ctx->slist;
   q.counters = ctx->counters;
   q.stats = ctx->dstats;
   q.capacity = (uint32_t)ctx->cap_rays;
@@ -288,6 +292,8 @@ int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixel
       cudaFree(*p);
       *p = nullptr;
     }
+    cudaFree(L.slist);
+    L.slist = nullptr;
     L.cap_paths = L.cap_rays = 0;
     for (int k = 0; k < 2; k++) {
       OR3_CUDA(ctx, cudaMalloc(&L.qorig[k], rays * sizeof(float4)));
@@ -299,6 +305,7 @@ int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixel
     OR3_CUDA(ctx, cudaMalloc(&L.sorig, rays * sizeof(float4)));
     OR3_CUDA(ctx, cudaMalloc(&L.sdir, rays * sizeof(float4)));
     OR3_CUDA(ctx, cudaMalloc(&L.scontrib, rays * sizeof(float4)));
+    OR3_CUDA(ctx, cudaMalloc(&L.slist, rays * sizeof(uint32_t)));
     L.cap_paths = paths;
     L.cap_rays = rays;
   }
@@ -325,6 +332,8 @@ void free_lane_buffers(or3_context::Lane &L) {
     cudaFree(*p);
     *p = nullptr;
   }
+  cudaFree(L.slist);
+  L.slist = nullptr;
   cudaFree(L.pix_sum);
   cudaFree(L.pix_sumsq);
   L.pix_sum = L.pix_sumsq = nullptr;
@@ -343,6 +352,7 @@ Queues lane_queues(const or3_context::Lane &L) {
   q.sorig = L.sorig;
   q.sdir = L.sdir;
   q.scontrib = L.scontrib;
+  q.slist = L.slist;
   q.counters = L.counters;
   q.stats = L.dstats;
   q.capacity = (uint32_t)L.cap_rays;
@@ -483,6 +493,7 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFree(ctx->sorig);
   cudaFree(ctx->sdir);
   cudaFree(ctx->scontrib);
+  cudaFree(ctx->slist);
   cudaFree(ctx->counters);
   cudaFree(ctx->dstats);
   cudaFreeHost(ctx->host_counters);
@@ -1082,6 +1093,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // sized for the shade instance launch_shade picks
   const bool nee4 = (prm->tuning & OR3_TUNE_SHADE_NEE_OCC4) != 0;
   const int grid_sh = ctx->num_sms * (shadows && !nee4 ? ctx->occ_shade_nee : ctx->occ_shade);
+  // material-sorted shade: classify, then one kernel instance per class list
+  const bool sorted_shade = (prm->tuning & OR3_TUNE_SORTED_SHADE) != 0;
 
   // a depth bound of at most 32 enqueues every bounce of a wave at once
   const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;
@@ -1178,7 +1191,14 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[0], st));
         launch_extend(sg->view, ql, in, grid_ext, block, smem_nodes, countk, variant, sl);
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[1], st));
-        launch_shade(sg->view, rcst, w, ql, in, grid_sh, block, sl, nee4);
+        if (sorted_shade) {
+          launch_shade_sorted(sg->view, rcst, w, ql, in, ctx->num_sms * 8, ctx->num_sms * ctx->occ_shade_nee,
+                              ctx->num_sms * ctx->occ_shade, sl);
+          stats.kernel_launches += shadows ? 2 : 1;
+        } else {
+          launch_shade(sg->view, rcst, w, ql, in, grid_sh, block, sl, nee4,
+                       (prm->tuning & OR3_TUNE_BLOCK_APPEND) != 0);
+        }
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
         if (shadows)
           launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl);

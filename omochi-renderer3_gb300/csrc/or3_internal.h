@@ -48,6 +48,7 @@ struct or3_context {
   float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
   float4 *hits = nullptr, *pathL = nullptr;
   float4 *sorig = nullptr, *sdir = nullptr, *scontrib = nullptr;  // shadow queue (cap_rays entries)
+  uint32_t *slist = nullptr;  // sorted shade: hit indices by material class (cap_rays entries)
   uint32_t *counters = nullptr;
   unsigned long long *dstats = nullptr;
   uint32_t *host_counters = nullptr;  // pinned
@@ -91,6 +92,7 @@ struct or3_context {
     cudaStream_t stream = nullptr;
     float4 *qorig[2] = {nullptr, nullptr}, *qdir[2] = {nullptr, nullptr}, *qbeta[2] = {nullptr, nullptr};
     float4 *hits = nullptr, *pathL = nullptr, *sorig = nullptr, *sdir = nullptr, *scontrib = nullptr;
+    uint32_t *slist = nullptr;
     uint32_t *counters = nullptr;
     unsigned long long *dstats = nullptr;
     double *pix_sum = nullptr, *pix_sumsq = nullptr;

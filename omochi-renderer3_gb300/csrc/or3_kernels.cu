@@ -402,6 +402,21 @@ __device__ __forceinline__ bool sample_light(const DevScene &S, uint4 rl, V3 x, 
   return true;
 }
 
+// The layer a vertex uses: the roulette over the object's layer rates
+// (PathTracer.cpp:370-382), val uniform in [0, 1).
+__device__ __forceinline__ uint32_t pick_layer(const DevScene &S, uint32_t begin, uint32_t count, float val) {
+  uint32_t sel = count - 1;
+  for (uint32_t k = 0; k < count; k++) {
+    const float rate = S.layers[begin + k].rate;
+    if (val <= rate) {
+      sel = k;
+      break;
+    }
+    val -= rate;
+  }
+  return sel;
+}
+
 // One path vertex: PathTracer::Radiance_internal (src/renderer/PathTracer.cpp:349-442)
 // and the three BSDFs (:445-591).  Writes 0, 1 or 2 continuation rays, and
 // with next-event estimation on, at most one shadow ray (has_sr).  NEE
@@ -440,16 +455,7 @@ __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &r
   const uint4 rn = philox(path_counter(w.g_first + path, leaf, depth, 0u), rc.seed_lo, rc.seed_hi);
 
   // material layer roulette (PathTracer.cpp:370-382)
-  float val = u01(rn.x);
-  uint32_t sel = s.layer_count - 1;
-  for (uint32_t k = 0; k < s.layer_count; k++) {
-    const float rate = S.layers[s.layer_begin + k].rate;
-    if (val <= rate) {
-      sel = k;
-      break;
-    }
-    val -= rate;
-  }
+  const uint32_t sel = pick_layer(S, s.layer_begin, s.layer_count, u01(rn.x));
   const MaterialDev &m = S.materials[S.layers[s.layer_begin + sel].material];
   V3 col = v3(m.color[0], m.color[1], m.color[2]);
   if (m.texture >= 0) col = col * texel(S, m.texture, s.uvx, s.uvy);  // GetTexturedColor (:327-346)
@@ -587,74 +593,204 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
   return lo;
 }
 
+// Shades queue entry i when `valid` and appends its continuation and shadow
+// rays (warp-aggregated: every lane of the warp calls this together).
 // BATCH: the ray's segment (beta.w) selects the job's scene, constants and
-// RNG numbering; continuation rays inherit it.
-template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4>
+// RNG numbering; continuation rays inherit it.  BLK: block-aggregated
+// appends (one atomic per queue and block iteration instead of per warp; the
+// queue lengths are single addresses every warp updates); every thread of
+// the block calls this together.
+template <bool BATCH, bool NEE, bool BLK = false>
+__device__ __forceinline__ void shade_item(const DevScene &S0, const RenderConst &rc0, const Wave &w0,
+                                           const Queues &q, int in, const Batch &b, bool valid, uint32_t i) {
+  const int out = in ^ 1;
+  const uint32_t lane = threadIdx.x & 31u;
+  NewRay r0, r1;
+  ShadowRay sr;
+  bool has_sr = false;
+  int cnt = 0;
+  uint32_t tag = 0;
+  if (valid) {
+    if (BATCH) {
+      tag = __float_as_uint(q.beta[in][i].w);
+      const Segment sg = b.segs[tag];
+      const JobDev &job = b.jobs[sg.job];
+      Wave w = w0;
+      w.g_first = sg.g_first - sg.wave_first;
+      cnt = shade_one<NEE>(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1, sr, has_sr);
+    } else {
+      cnt = shade_one<NEE>(S0, rc0, w0, q, in, i, r0, r1, sr, has_sr);
+    }
+  }
+  const unsigned sm = NEE ? __ballot_sync(0xFFFFFFFFu, has_sr) : 0u;
+  int incl = cnt;  // inclusive scan of the warp's continuation rays
+#pragma unroll
+  for (int ofs = 1; ofs < 32; ofs <<= 1) {
+    const int v = __shfl_up_sync(0xFFFFFFFFu, incl, ofs);
+    if ((int)lane >= ofs) incl += v;
+  }
+  const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  uint32_t sbase = 0, wbase = 0;
+  if (BLK) {
+    __shared__ uint32_t bc[2][8], bb[2];  // per queue: warp counts (then offsets), the block's base
+    const uint32_t warp = threadIdx.x >> 5;
+    if (lane == 0) {
+      bc[0][warp] = (uint32_t)total;
+      bc[1][warp] = (uint32_t)__popc(sm);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const uint32_t c = threadIdx.x;
+      uint32_t t = 0;
+      for (uint32_t k = 0; k < (blockDim.x >> 5); k++) {
+        const uint32_t v = bc[c][k];
+        bc[c][k] = t;
+        t += v;
+      }
+      bb[c] = t ? atomicAdd(&q.counters[c == 0 ? out : 3], t) : 0u;
+    }
+    __syncthreads();
+    wbase = bb[0] + bc[0][warp];
+    sbase = bb[1] + bc[1][warp];
+    __syncthreads();  // bc / bb are rewritten by the next call
+  } else {
+    if (sm) {
+      const int leader = __ffs(sm) - 1;
+      if ((int)lane == leader) sbase = atomicAdd(&q.counters[3], (uint32_t)__popc(sm));
+      sbase = __shfl_sync(0xFFFFFFFFu, sbase, leader);
+    }
+    if (lane == 31 && total > 0) wbase = atomicAdd(&q.counters[out], (uint32_t)total);
+    wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+  }
+  // append to the shadow queue
+  if (sm) {
+    if (has_sr) {
+      const uint32_t pos = sbase + (uint32_t)__popc(sm & ((1u << lane) - 1u));
+      if (pos < q.capacity) {
+        q.sorig[pos] = make_float4(sr.o.x, sr.o.y, sr.o.z, q.orig[in][i].w);
+        q.sdir[pos] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.tmax);
+        q.scontrib[pos] = make_float4(sr.c.x, sr.c.y, sr.c.z, __uint_as_float(tag));
+      } else {
+        atomicOr(&q.counters[2], kErrQueue);
+      }
+    }
+  }
+  // append to the output queue
+  uint32_t pos = wbase + (uint32_t)(incl - cnt);
+  const uint32_t pathbits = cnt ? __float_as_uint(q.orig[in][i].w) : 0u;
+  for (int k = 0; k < cnt; k++, pos++) {
+    const NewRay &r = k == 0 ? r0 : r1;
+    if (pos >= q.capacity) {
+      atomicOr(&q.counters[2], kErrQueue);
+      continue;
+    }
+    q.orig[out][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
+    q.dir[out][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
+    q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, __uint_as_float(tag));
+  }
+}
+
+// One path vertex for every queued ray (grid-stride; the loop bound is
+// uniform over the block, as BLK's barriers need).
+template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4, bool BLK = false>
 __global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in,
                                                             Batch b) {
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
-  const int out = in ^ 1;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    shade_item<BATCH, NEE, BLK>(S0, rc0, w0, q, in, b, i < n, i);
+  }
+}
+
+// Sorted shade, first step (after extend).  A missed ray is shaded here
+// (IBL::Sample or Scene::Background, PathTracer.cpp:357-364, counted as in
+// shade_one), and every surface hit is filed by the material of the layer its
+// roulette picks -- the reference dispatches on that layer's reflection type
+// (PathTracer.cpp:419-429): with next-event estimation, a Lambert layer that
+// does not emit or a Phong layer (a light sample is taken there) goes to the
+// front of q.slist, every other surface (mirror, glass, emitters, any
+// surface without light sampling) to the back.  The two lists are then shaded
+// by separate kernel instances, so no warp mixes misses, light-sampling
+// vertices and delta vertices.  The roulette is recomputed by the shade
+// kernel from the same Philox counter, so the path is unchanged.
+template <bool NEE>
+__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues q, int in) {
+  __shared__ uint32_t wcount[2][8], wbase[2];  // per class: warp counts (then offsets), the block's base
+  const uint32_t n = min(q.counters[in], q.capacity);
   const uint32_t lane = threadIdx.x & 31u;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
-    NewRay r0, r1;
-    ShadowRay sr;
-    bool has_sr = false;
-    int cnt = 0;
-    uint32_t tag = 0;
+    int cls = -1;  // -1: done here (a miss), 0: front list, 1: back list
     if (i < n) {
-      if (BATCH) {
-        tag = __float_as_uint(q.beta[in][i].w);
-        const Segment sg = b.segs[tag];
-        const JobDev &job = b.jobs[sg.job];
-        Wave w = w0;
-        w.g_first = sg.g_first - sg.wave_first;
-        cnt = shade_one<NEE>(b.scenes[job.scene], job.rc, w, q, in, i, r0, r1, sr, has_sr);
-      } else {
-        cnt = shade_one<NEE>(S0, rc0, w0, q, in, i, r0, r1, sr, has_sr);
-      }
-    }
-    // warp-aggregated append to the shadow queue
-    const unsigned sm = NEE ? __ballot_sync(0xFFFFFFFFu, has_sr) : 0u;
-    if (sm) {
-      const int leader = __ffs(sm) - 1;
-      uint32_t sbase = 0;
-      if ((int)lane == leader) sbase = atomicAdd(&q.counters[3], (uint32_t)__popc(sm));
-      sbase = __shfl_sync(0xFFFFFFFFu, sbase, leader);
-      if (has_sr) {
-        const uint32_t pos = sbase + (uint32_t)__popc(sm & ((1u << lane) - 1u));
-        if (pos < q.capacity) {
-          q.sorig[pos] = make_float4(sr.o.x, sr.o.y, sr.o.z, q.orig[in][i].w);
-          q.sdir[pos] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.tmax);
-          q.scontrib[pos] = make_float4(sr.c.x, sr.c.y, sr.c.z, __uint_as_float(tag));
-        } else {
-          atomicOr(&q.counters[2], kErrQueue);
+      const uint32_t rec = __float_as_uint(q.hits[i].y);
+      const float4 rd = q.dir[in][i];
+      const uint32_t meta = __float_as_uint(rd.w);
+      const uint32_t depth = meta & 0xFFFFu;
+      if (rec == kMissRec) {
+        if (!(rc.nee && depth > 0 && !(meta & kMetaSpec))) {
+          const float4 ro = q.orig[in][i], rb = q.beta[in][i];
+          add_radiance(q.pathL + __float_as_uint(ro.w), ld3(rb) * env_lookup(S, ld3(rd)));
         }
+      } else if (NEE) {
+        uint32_t lb, lc;
+        if (rec & kPlaneBit) {
+          const PlaneRec &pl = S.planes[rec & ~kPlaneBit];
+          lb = pl.layer_begin;
+          lc = pl.layer_count;
+        } else {
+          const PrimInfo &inf = S.info[rec];
+          lb = inf.layer_begin;
+          lc = inf.layer_count;
+        }
+        const uint32_t path = __float_as_uint(q.orig[in][i].w);
+        const uint4 rn = philox(path_counter(w.g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo,
+                                rc.seed_hi);
+        const MaterialDev &m = S.materials[S.layers[lb + pick_layer(S, lb, lc, u01(rn.x))].material];
+        cls = ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG) ? 0 : 1;
+      } else {
+        cls = 1;
       }
     }
-    // warp-aggregated append to the output queue
-    int incl = cnt;
-#pragma unroll
-    for (int ofs = 1; ofs < 32; ofs <<= 1) {
-      const int v = __shfl_up_sync(0xFFFFFFFFu, incl, ofs);
-      if ((int)lane >= ofs) incl += v;
+    // block-aggregated appends (one atomic per class and block iteration: the
+    // two list lengths are single addresses every block updates); the lists
+    // hold at most n <= capacity entries together
+    const unsigned m0 = __ballot_sync(0xFFFFFFFFu, cls == 0), m1 = __ballot_sync(0xFFFFFFFFu, cls == 1);
+    const uint32_t warp = threadIdx.x >> 5;
+    if (lane == 0) {
+      wcount[0][warp] = (uint32_t)__popc(m0);
+      wcount[1][warp] = (uint32_t)__popc(m1);
     }
-    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    uint32_t wbase = 0;
-    if (lane == 31 && total > 0) wbase = atomicAdd(&q.counters[out], (uint32_t)total);
-    wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
-    uint32_t pos = wbase + (uint32_t)(incl - cnt);
-    const uint32_t pathbits = cnt ? __float_as_uint(q.orig[in][i].w) : 0u;
-    for (int k = 0; k < cnt; k++, pos++) {
-      const NewRay &r = k == 0 ? r0 : r1;
-      if (pos >= q.capacity) {
-        atomicOr(&q.counters[2], kErrQueue);
-        continue;
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const uint32_t c = threadIdx.x;
+      uint32_t total = 0;
+      for (uint32_t k = 0; k < (blockDim.x >> 5); k++) {
+        const uint32_t v = wcount[c][k];
+        wcount[c][k] = total;  // exclusive prefix over the block's warps
+        total += v;
       }
-      q.orig[out][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
-      q.dir[out][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
-      q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, __uint_as_float(tag));
+      wbase[c] = total ? atomicAdd(&q.counters[10 + c], total) : 0u;
     }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+    if (cls == 0) q.slist[wbase[0] + wcount[0][warp] + (uint32_t)__popc(m0 & below)] = i;
+    else if (cls == 1) q.slist[q.capacity - 1u - (wbase[1] + wcount[1][warp] + (uint32_t)__popc(m1 & below))] = i;
+    __syncthreads();  // wcount / wbase are rewritten by the next iteration
+  }
+}
+
+// Sorted shade, second step: the entries of one list (back = 0: the front
+// list, light-sampling vertices; 1: the back list).
+template <bool NEE, int MINB = NEE ? 3 : 4>
+__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues q, int in,
+                                                          int back) {
+  const uint32_t cap = q.capacity;
+  const uint32_t n = min(q.counters[back ? 11 : 10], cap);
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t k = base + threadIdx.x;
+    const bool valid = k < n;
+    const uint32_t i = valid ? q.slist[back ? cap - 1u - k : k] : 0u;
+    shade_item<false, NEE, true>(S, rc, w, q, in, Batch{}, valid, i);
   }
 }
 
@@ -669,13 +805,15 @@ __global__ void k_merge_sums(size_t n, double *a, double *aq, double *b, double 
   }
 }
 
-// Clears a consumed queue's length and its extend fetch counter, and the
-// shadow queue's length and fetch counter.
+// Clears a consumed queue's length and its extend fetch counter, the shadow
+// queue's length and fetch counter, and the sorted shade's list lengths.
 __global__ void k_reset_count(uint32_t *counters, int which) {
   counters[which] = 0;
   counters[4 + which] = 0;
   counters[3] = 0;
   counters[6] = 0;
+  counters[10] = 0;
+  counters[11] = 0;
 }
 
 struct ShadowSrc {
@@ -1045,13 +1183,30 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
 }
 
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
-                  int grid, int block, cudaStream_t st, bool nee4) {
-  if (rc.nee && (S.num_lights > 0 || S.env_light != 0) && nee4)
+                  int grid, int block, cudaStream_t st, bool nee4, bool blk) {
+  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
+  if (nee && nee4)
     k_shade<false, true, 4><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
-  else if (rc.nee && (S.num_lights > 0 || S.env_light != 0))
+  else if (nee && blk)
+    k_shade<false, true, 3, true><<<grid, 256, 0, st>>>(S, rc, w, q, in, Batch{});
+  else if (nee)
     k_shade<false, true><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+  else if (blk)
+    k_shade<false, false, 4, true><<<grid, 256, 0, st>>>(S, rc, w, q, in, Batch{});
   else
     k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+}
+
+void launch_shade_sorted(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
+                         int grid_classify, int grid_nee, int grid_plain, cudaStream_t st) {
+  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
+  if (nee) {
+    k_classify<true><<<grid_classify, 256, 0, st>>>(S, rc, w, q, in);
+    k_shade_list<true><<<grid_nee, 256, 0, st>>>(S, rc, w, q, in, 0);
+  } else {
+    k_classify<false><<<grid_classify, 256, 0, st>>>(S, rc, w, q, in);
+  }
+  k_shade_list<false><<<grid_plain, 256, 0, st>>>(S, rc, w, q, in, 1);
 }
 
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st) {

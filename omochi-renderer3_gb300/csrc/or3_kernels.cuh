@@ -51,8 +51,12 @@ struct Queues {
   float4 *hits;
   float4 *pathL;  // per camera path radiance of the wave
   float4 *sorig, *sdir, *scontrib;
+  uint32_t *slist;            // sorted shade: indices of this bounce's hits by material class
+                              // (light-sampling surfaces from the front, the rest from the back);
+                              // null where the sorted shade is not used
   uint32_t *counters;         // [0],[1] queue lengths, [2] error bits, [3] shadow queue length,
-                              // [4],[5] extend fetch counters, [6] shadow fetch counter
+                              // [4],[5] extend fetch counters, [6] shadow fetch counter,
+                              // [10],[11] sorted shade: front and back list lengths
   unsigned long long *stats;  // [0] extension rays [1] shadow rays [2] bounces [3] nodes [4] tris [5] spheres
   uint32_t capacity;          // entries per queue (the shadow queue too)
   uint32_t pad;
@@ -128,10 +132,16 @@ inline int extend_variant(uint32_t tuning) {
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    int variant, cudaStream_t st);
 // nee4: the light-sampling instance limited to 64 registers (4 blocks per SM)
+// nee4: the light-sampling instance at 4 blocks/SM; blk: block-aggregated
+// queue appends (256-thread blocks)
 void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
-                  int grid, int block, cudaStream_t st, bool nee4 = false);
+                  int grid, int block, cudaStream_t st, bool nee4 = false, bool blk = false);
 void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 // a += b, b = 0 over n doubles (sums and sums of squares)
+// Material-sorted shade (k_classify, then k_shade_list per class list):
+// replaces launch_shade when chosen; 2 or 3 launches.
+void launch_shade_sorted(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
+                         int grid_classify, int grid_nee, int grid_plain, cudaStream_t st);
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);

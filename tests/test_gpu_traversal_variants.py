@@ -6,6 +6,8 @@ the order children are visited, on shared-memory node staging or on the
 lane refill threshold; only ties (two primitives at one distance) may
 resolve differently.  So each variant's per-path radiance must equal the
 default's for all but a handful of paths, shadow rays included (NEE on).
+The material-sorted shade (0x800) files hits by material class and shades
+each class with its own kernel instance; the paths are the same too.
 """
 import numpy as np
 import pytest
@@ -22,6 +24,8 @@ VARIANTS = {
     "shadow_unsorted": 0x20,
     "l2_window": 0x40,
     "shade_nee_4_blocks": 0x80,
+    "sorted_shade": 0x800,
+    "block_append": 0x1000,
 }
 
 
@@ -30,10 +34,18 @@ def _scenes(W):
         "ico_phong": (W.icosphere_in_box(64, 48, level=4)[:2], dict(rr_min_depth=5, max_depth=10)),
         "terrain_nee": (W.terrain_ibl(64, 36, cells_x=128, cells_z=64, spheres=16)[:2],
                         dict(rr_min_depth=5, max_depth=12, next_event_estimation=True)),
+        # mirror and glass (split paths), NEE off
+        "cornell": (W.cornell_box(48, 48)[:2], dict(rr_min_depth=3, max_depth=8)),
+        # a sphere light, a two-layer sphere and floors (planes) with NEE on
+        "refcornell_nee": (W.reference_cornell(48, 36)[:2], dict(rr_min_depth=5, max_depth=0,
+                                                                  next_event_estimation=True)),
+        # a constant background sampled as a light
+        "sky_constant": (W.sky_floor(48, 48, constant=(0.6, 0.7, 0.9)),
+                         dict(rr_min_depth=5, max_depth=8, next_event_estimation=True)),
     }
 
 
-@pytest.mark.parametrize("scene", ["ico_phong", "terrain_nee"])
+@pytest.mark.parametrize("scene", ["ico_phong", "terrain_nee", "cornell", "refcornell_nee", "sky_constant"])
 def test_variants_render_the_same_paths(pkg, ctx, scene):
     (sd, cam), st = _scenes(pkg.workloads)[scene]
     sid = ctx.upload(sd)

@@ -188,8 +188,9 @@ typedef struct or3_render_params {
                                       2 persistent, node steps with leaves in place, lanes refilled once
                                       16 are idle; 3 one ray per thread; 4, 5 as 2 refilling at 8 / 24
                                       idle lanes; 6 as 2 over the 8-bit quantised child boxes (shadow
-                                      rays too); 7 = 2.  2, 4, 5 test FP32 child boxes; 1, 3, 6 the
-                                      quantised ones */
+                                      rays too); 7 as 2 with the nearest internal child next and
+                                      its siblings pushed unsorted.  2, 4, 5, 7 test FP32 child
+                                      boxes; 1, 3, 6 the quantised ones */
 #define OR3_TUNE_SMEM_NODES 0x10u  /* stage the top quantised BVH nodes in shared memory (variants 1, 3, 6) */
 #define OR3_TUNE_SHADOW_UNSORTED 0x20u /* shadow rays take children in slot order (no distance sort) */
 #define OR3_TUNE_L2_PERSIST 0x40u      /* or3_render: L2 persisting access window over the BVH nodes */

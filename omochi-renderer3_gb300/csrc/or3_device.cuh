@@ -417,7 +417,11 @@ __device__ __forceinline__ void trav_leaf(const SV &S, TravState &s, uint32_t fi
 // The stack cannot overflow here (depth bound checked at upload, push index
 // clamped), so `err` is not written on this path; the signature matches
 // trav_step's.
-template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true, class SV = DevScene>
+// NEAREST (with SORT false): the nearest internal child hit is next and the
+// others go on the stack in slot order (an argmin instead of the sorting
+// network; popped entries are still pruned by their entry distance).
+template <bool ANY, bool COUNT, bool SORT = true, class STK = LocalStack, bool FN = true, class SV = DevScene,
+          bool NEAREST = false>
 __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK &stk,
                                                  const uint4 *snodes, uint32_t ns, uint32_t *cnt, uint32_t *err) {
   const uint32_t e = s.entry;
@@ -505,6 +509,31 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
   }
   if (ANY && s.rec != kMissRec) return true;
   const float inf2 = kInf * 2.f;
+  if (!SORT && NEAREST) {
+    float kmin = key[0];
+    uint32_t next = kid[0];
+    int jmin = 0;
+#pragma unroll
+    for (int j = 1; j < 4; j++) {
+      if (key[j] < kmin) {
+        kmin = key[j];
+        next = kid[j];
+        jmin = j;
+      }
+    }
+    if (kmin < inf2 && kmin <= s.tmax * 1.0000010f) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (j != jmin && key[j] < inf2) {
+          stk.put(s.sp, kid[j], key[j]);  // index below kStackSize: see the sorted push below
+          s.sp = min(s.sp + 1, kStackSize - 1);
+        }
+      }
+      s.entry = next;
+      return false;
+    }
+    return !trav_pop_stk(s, stk);
+  }
   if (!SORT) {
     // slot order: the first internal child hit is next, the others go on the stack
     uint32_t nxt = kNoEntry;

@@ -92,7 +92,8 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
 // nearest-first child order (off only for any-hit queries).  FN: STEP 2 over
 // the FP32-box nodes (else the quantised ones).
-template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, bool FN = true>
+template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, bool FN = true,
+          bool NEAREST = false>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
@@ -127,8 +128,8 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
     }
     if (r != kNoEntry) {
       const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                  : trav_step_inline<ANY, COUNT, SORT, PairStack, FN>(S, st, stk, snodes, ns,
-                                                                                      cnt, err);
+                                  : trav_step_inline<ANY, COUNT, SORT, PairStack, FN, DevScene, NEAREST>(
+                                        S, st, stk, snodes, ns, cnt, err);
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;
@@ -182,7 +183,8 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 // Closest hit for every queued ray.  COUNT adds the nodes, triangles and
 // spheres each ray touched to stats[3..5] (the algorithmic byte count).
 // VARIANT 0: gridstride_trace; 1: persistent_trace STEP 1; 2, 4, 5: STEP 2
-// refilling at 16, 8 or 24 idle lanes; 6: STEP 2 over the quantised nodes.
+// refilling at 16, 8 or 24 idle lanes; 6: STEP 2 over the quantised nodes;
+// 7: STEP 2, nearest internal child next and its siblings pushed unsorted.
 // 0, 1 and 6 read the quantised nodes (and may stage the top ones in shared
 // memory), 2, 4 and 5 the FP32-box nodes.
 template <bool COUNT, int VARIANT>
@@ -211,7 +213,7 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
   } else {
     constexpr int kStep = VARIANT == 1 ? 1 : 2;
     constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
-    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, true, VARIANT != 6>(
+    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, VARIANT != 7, VARIANT != 6, VARIANT == 7>(
         S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
         &q.counters[2]);
   }
@@ -1174,10 +1176,12 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
     case 4: k_extend<false, 4><<<grid, block, 0, st>>>(S, q, in, 0); break;
     case 5: k_extend<false, 5><<<grid, block, 0, st>>>(S, q, in, 0); break;
     case 6: k_extend<false, 6><<<grid, block, 0, st>>>(S, q, in, sn); break;
+    case 7: k_extend<false, 7><<<grid, block, 0, st>>>(S, q, in, 0); break;
     case 8: k_extend<true, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 9: k_extend<true, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
-    case 10: case 12: case 13: case 14: case 15:  // counting runs use the default traversal
+    case 10: case 12: case 13: case 14:  // counting runs use the default traversal
       k_extend<true, 2><<<grid, block, 0, st>>>(S, q, in, 0); break;
+    case 15: k_extend<true, 7><<<grid, block, 0, st>>>(S, q, in, 0); break;
     default: k_extend<false, 0><<<grid, block, 0, st>>>(S, q, in, sn); break;
   }
 }

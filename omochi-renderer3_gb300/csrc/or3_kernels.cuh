@@ -127,7 +127,7 @@ void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int ou
 // Maps OR3_TUNE_EXTEND_MASK to a kernel variant (0 = default = 2, 3 = grid-stride).
 inline int extend_variant(uint32_t tuning) {
   const uint32_t v = tuning & 0x7u;
-  return v == 0 || v == 7 ? 2 : v == 3 ? 0 : (int)v;  // 4, 5: refill thresholds; 6: quantised nodes
+  return v == 0 ? 2 : v == 3 ? 0 : (int)v;  // 4, 5: refill thresholds; 6: quantised nodes; 7: nearest first
 }
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    int variant, cudaStream_t st);

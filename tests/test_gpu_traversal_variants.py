@@ -20,6 +20,7 @@ VARIANTS = {
     "refill8": 4,
     "refill24": 5,
     "step2_quantised": 6,
+    "nearest_first": 7,
     "step2_quantised_smem": 6 | 0x10,
     "shadow_unsorted": 0x20,
     "l2_window": 0x40,

@@ -199,7 +199,10 @@ typedef struct or3_render_params {
 #define OR3_TUNE_TWO_LANES 0x200u      /* or3_render: waves round robin over two streams instead of three */
 #define OR3_TUNE_FOUR_LANES 0x400u     /* or3_render: waves round robin over four streams instead of three */
 #define OR3_TUNE_SORTED_SHADE 0x800u   /* or3_render: material-sorted shade (misses shaded while the hits are
-                                          filed by material class, then one shade kernel per class) */
+                                          filed by material class, then one shade kernel per class) also
+                                          without light sampling; with it, it is the default */
+#define OR3_TUNE_UNSORTED_SHADE 0x2000u /* or3_render: one shade kernel for every hit and miss even where
+                                          vertices sample lights */
 #define OR3_TUNE_BLOCK_APPEND 0x1000u  /* or3_render: the shade kernel appends rays with one atomic per block
                                           instead of one per warp */
 

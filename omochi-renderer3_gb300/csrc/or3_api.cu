@@ -1093,8 +1093,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // sized for the shade instance launch_shade picks
   const bool nee4 = (prm->tuning & OR3_TUNE_SHADE_NEE_OCC4) != 0;
   const int grid_sh = ctx->num_sms * (shadows && !nee4 ? ctx->occ_shade_nee : ctx->occ_shade);
-  // material-sorted shade: classify, then one kernel instance per class list
-  const bool sorted_shade = (prm->tuning & OR3_TUNE_SORTED_SHADE) != 0;
+  // material-sorted shade (classify, then one kernel instance per class
+  // list): the default where vertices sample lights, whose shade kernel then
+  // no longer carries the misses (measured +3.2% on the terrain); without
+  // light sampling it costs more than it saves (-5.6% on the mesh)
+  const bool sorted_shade = (prm->tuning & OR3_TUNE_SORTED_SHADE) != 0 ||
+                            (shadows && !(prm->tuning & OR3_TUNE_UNSORTED_SHADE));
 
   // a depth bound of at most 32 enqueues every bounce of a wave at once
   const bool whole = prm->max_depth > 0 && prm->max_depth <= 32;

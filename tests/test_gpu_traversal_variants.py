@@ -26,6 +26,7 @@ VARIANTS = {
     "l2_window": 0x40,
     "shade_nee_4_blocks": 0x80,
     "sorted_shade": 0x800,
+    "unsorted_shade": 0x2000,
     "block_append": 0x1000,
 }
 

@@ -429,6 +429,7 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
   if (COUNT) cnt[0]++;
   float key[4];
   uint32_t kid[4];
+  uint4 slots;  // the four child words; read by a runtime slot index below without a local-memory array
   uint32_t leafmask = 0, counts;
   if (FN) {
     // near / far planes picked by the ray's direction signs through the load offset
@@ -438,6 +439,7 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
     const float4 bny = __ldg(np + 2 + sy), bfy = __ldg(np + 3 - sy);
     const float4 bnz = __ldg(np + 4 + sz), bfz = __ldg(np + 5 - sz);
     const uint4 ch = __ldg(reinterpret_cast<const uint4 *>(np + 6));
+    slots = ch;
     const uint4 mt = __ldg(reinterpret_cast<const uint4 *>(np + 7));
     counts = mt.x;
     const uint32_t imask = mt.y;
@@ -486,6 +488,7 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
   const uint32_t wny = (s.signs & 2u) ? n2.x : n1.y, wfy = (s.signs & 2u) ? n1.y : n2.x;
   const uint32_t wnz = (s.signs & 4u) ? n2.y : n1.z, wfz = (s.signs & 4u) ? n1.z : n2.y;
   counts = n3.z;
+  slots = make_uint4(n2.z, n2.w, n3.x, n3.y);
   const float tlimit = s.tmax * 1.0000010f;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
@@ -505,7 +508,8 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
   while (leafmask) {
     const uint32_t i = __ffs(leafmask) - 1;
     leafmask &= leafmask - 1;
-    trav_leaf<COUNT>(S, s, kid[i], (counts >> (8 * i)) & 0xFFu, cnt);
+    const uint32_t first = i == 0 ? slots.x : i == 1 ? slots.y : i == 2 ? slots.z : slots.w;
+    trav_leaf<COUNT>(S, s, first, (counts >> (8 * i)) & 0xFFu, cnt);
   }
   if (ANY && s.rec != kMissRec) return true;
   const float inf2 = kInf * 2.f;

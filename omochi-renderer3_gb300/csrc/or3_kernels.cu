@@ -25,6 +25,24 @@ __device__ __forceinline__ void add_radiance(float4 *L, V3 v) {
 
 __device__ __forceinline__ V3 ld3(const float4 &f) { return v3(f.x, f.y, f.z); }
 
+// The queues with ray queue `in` in slot 0 and the other queue in slot 1.
+// Kernels orient their Queues parameter once and then index the ray pointer
+// pairs with constants only: indexing a parameter's array with a run-time
+// value makes the compiler copy the whole struct to local memory and load
+// every pointer from there.  Queue lengths stay indexed by the physical
+// queue (counters[in], counters[out]).
+__device__ __forceinline__ Queues oriented(const Queues &p, int in) {
+  Queues q = p;
+  const bool sw = in != 0;
+  q.orig[0] = sw ? p.orig[1] : p.orig[0];
+  q.orig[1] = sw ? p.orig[0] : p.orig[1];
+  q.dir[0] = sw ? p.dir[1] : p.dir[0];
+  q.dir[1] = sw ? p.dir[0] : p.dir[1];
+  q.beta[0] = sw ? p.beta[1] : p.beta[0];
+  q.beta[1] = sw ? p.beta[0] : p.beta[1];
+  return q;
+}
+
 // Camera::SampleRayForPixel (src/renderer/Camera.h:65-93) for sub-pixel
 // position (x + rx, y + ry), rx = (2 sx + 1) / (2 ss)
 // (PathTracer::scanPixelsOnYAndCastRays, src/renderer/PathTracer.cpp:156-161).
@@ -58,7 +76,8 @@ __device__ __forceinline__ void camera_ray(const RenderConst &rc, uint32_t x, ui
   }
 }
 
-__global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
+__global__ void k_raygen(RenderConst rc, Wave w, Queues qp, int out) {
+  const Queues q = oriented(qp, out);  // the queue written is slot 0
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     q.counters[out] = w.num_paths;
@@ -72,9 +91,9 @@ __global__ void k_raygen(RenderConst rc, Wave w, Queues q, int out) {
   const uint32_t x = pix % rc.W, y = pix / rc.W;
   V3 o, d;
   camera_ray(rc, x, y, sub % rc.ss, sub / rc.ss, pix * rc.ss2 + sub, w.pass_first, o, d);
-  q.orig[out][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
-  q.dir[out][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
-  q.beta[out][i] = make_float4(1.f, 1.f, 1.f, 0.f);
+  q.orig[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
+  q.dir[0][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+  q.beta[0][i] = make_float4(1.f, 1.f, 1.f, 0.f);
   q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -194,7 +213,7 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
 template <bool COUNT, int VARIANT>
 __global__ void __launch_bounds__(256, 4) k_extend(DevScene S, Queues q, int in, int smem_nodes) {
   __shared__ uint4 snodes[kSmemNodes * 4];
-  extend_body<COUNT, VARIANT>(S, q, in, smem_nodes, snodes);
+  extend_body<COUNT, VARIANT>(S, oriented(q, in), in, smem_nodes, snodes);
 }
 
 template <bool COUNT, int VARIANT>
@@ -208,13 +227,13 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
   }
   uint32_t cnt[3] = {0u, 0u, 0u};
   if (VARIANT == 0) {
-    gridstride_trace<false, COUNT>(S, n, QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
+    gridstride_trace<false, COUNT>(S, n, QueueSrc{q.orig[0], q.dir[0]}, HitSink{q.hits}, snodes, ns, cnt,
                                    &q.counters[2]);
   } else {
     constexpr int kStep = VARIANT == 1 ? 1 : 2;
     constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
     persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, VARIANT != 7, VARIANT != 6, VARIANT == 7>(
-        S, n, &q.counters[4 + in], QueueSrc{q.orig[in], q.dir[in]}, HitSink{q.hits}, snodes, ns, cnt,
+        S, n, &q.counters[4 + in], QueueSrc{q.orig[0], q.dir[0]}, HitSink{q.hits}, snodes, ns, cnt,
         &q.counters[2]);
   }
   if (COUNT) {
@@ -428,7 +447,7 @@ template <bool NEE>
 __device__ __forceinline__ int shade_one(const DevScene &S, const RenderConst &rc, const Wave &w,
                                          const Queues &q, int in, uint32_t i, NewRay &r0, NewRay &r1,
                                          ShadowRay &sr, bool &has_sr) {
-  const float4 ro = q.orig[in][i], rd = q.dir[in][i], rb = q.beta[in][i], hh = q.hits[i];
+  const float4 ro = q.orig[0][i], rd = q.dir[0][i], rb = q.beta[0][i], hh = q.hits[i];
   const V3 o = ld3(ro), d = ld3(rd);
   V3 beta = ld3(rb);
   const uint32_t path = __float_as_uint(ro.w);
@@ -595,6 +614,20 @@ __device__ __forceinline__ uint32_t find_segment(const Segment *segs, uint32_t n
   return lo;
 }
 
+// Writes continuation ray r at position pos of the output queue (slot 1 of an
+// oriented q; a position past the capacity sets the queue error bit and
+// drops the ray).
+__device__ __forceinline__ void append_ray(const Queues &q, uint32_t pos, const NewRay &r,
+                                           uint32_t pathbits, uint32_t tag) {
+  if (pos >= q.capacity) {
+    atomicOr(&q.counters[2], kErrQueue);
+    return;
+  }
+  q.orig[1][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
+  q.dir[1][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
+  q.beta[1][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, __uint_as_float(tag));
+}
+
 // Shades queue entry i when `valid` and appends its continuation and shadow
 // rays (warp-aggregated: every lane of the warp calls this together).
 // BATCH: the ray's segment (beta.w) selects the job's scene, constants and
@@ -614,7 +647,7 @@ __device__ __forceinline__ void shade_item(const DevScene &S0, const RenderConst
   uint32_t tag = 0;
   if (valid) {
     if (BATCH) {
-      tag = __float_as_uint(q.beta[in][i].w);
+      tag = __float_as_uint(q.beta[0][i].w);
       const Segment sg = b.segs[tag];
       const JobDev &job = b.jobs[sg.job];
       Wave w = w0;
@@ -669,7 +702,7 @@ __device__ __forceinline__ void shade_item(const DevScene &S0, const RenderConst
     if (has_sr) {
       const uint32_t pos = sbase + (uint32_t)__popc(sm & ((1u << lane) - 1u));
       if (pos < q.capacity) {
-        q.sorig[pos] = make_float4(sr.o.x, sr.o.y, sr.o.z, q.orig[in][i].w);
+        q.sorig[pos] = make_float4(sr.o.x, sr.o.y, sr.o.z, q.orig[0][i].w);
         q.sdir[pos] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.tmax);
         q.scontrib[pos] = make_float4(sr.c.x, sr.c.y, sr.c.z, __uint_as_float(tag));
       } else {
@@ -677,26 +710,20 @@ __device__ __forceinline__ void shade_item(const DevScene &S0, const RenderConst
       }
     }
   }
-  // append to the output queue
-  uint32_t pos = wbase + (uint32_t)(incl - cnt);
-  const uint32_t pathbits = cnt ? __float_as_uint(q.orig[in][i].w) : 0u;
-  for (int k = 0; k < cnt; k++, pos++) {
-    const NewRay &r = k == 0 ? r0 : r1;
-    if (pos >= q.capacity) {
-      atomicOr(&q.counters[2], kErrQueue);
-      continue;
-    }
-    q.orig[out][pos] = make_float4(r.o.x, r.o.y, r.o.z, __uint_as_float(pathbits));
-    q.dir[out][pos] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(r.meta));
-    q.beta[out][pos] = make_float4(r.beta.x, r.beta.y, r.beta.z, __uint_as_float(tag));
-  }
+  // append to the output queue (each ray written by name, so neither needs an
+  // addressable copy in local memory)
+  const uint32_t pos = wbase + (uint32_t)(incl - cnt);
+  const uint32_t pathbits = cnt ? __float_as_uint(q.orig[0][i].w) : 0u;
+  if (cnt > 0) append_ray(q, pos, r0, pathbits, tag);
+  if (cnt > 1) append_ray(q, pos + 1u, r1, pathbits, tag);
 }
 
 // One path vertex for every queued ray (grid-stride; the loop bound is
 // uniform over the block, as BLK's barriers need).
 template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4, bool BLK = false>
-__global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues q, int in,
+__global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues qp, int in,
                                                             Batch b) {
+  const Queues q = oriented(qp, in);
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
@@ -716,7 +743,8 @@ __global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc
 // vertices and delta vertices.  The roulette is recomputed by the shade
 // kernel from the same Philox counter, so the path is unchanged.
 template <bool NEE>
-__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues q, int in) {
+__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues qp, int in) {
+  const Queues q = oriented(qp, in);
   __shared__ uint32_t wcount[2][8], wbase[2];  // per class: warp counts (then offsets), the block's base
   const uint32_t n = min(q.counters[in], q.capacity);
   const uint32_t lane = threadIdx.x & 31u;
@@ -725,12 +753,12 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
     int cls = -1;  // -1: done here (a miss), 0: front list, 1: back list
     if (i < n) {
       const uint32_t rec = __float_as_uint(q.hits[i].y);
-      const float4 rd = q.dir[in][i];
+      const float4 rd = q.dir[0][i];
       const uint32_t meta = __float_as_uint(rd.w);
       const uint32_t depth = meta & 0xFFFFu;
       if (rec == kMissRec) {
         if (!(rc.nee && depth > 0 && !(meta & kMetaSpec))) {
-          const float4 ro = q.orig[in][i], rb = q.beta[in][i];
+          const float4 ro = q.orig[0][i], rb = q.beta[0][i];
           add_radiance(q.pathL + __float_as_uint(ro.w), ld3(rb) * env_lookup(S, ld3(rd)));
         }
       } else if (NEE) {
@@ -744,7 +772,7 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
           lb = inf.layer_begin;
           lc = inf.layer_count;
         }
-        const uint32_t path = __float_as_uint(q.orig[in][i].w);
+        const uint32_t path = __float_as_uint(q.orig[0][i].w);
         const uint4 rn = philox(path_counter(w.g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo,
                                 rc.seed_hi);
         const MaterialDev &m = S.materials[S.layers[lb + pick_layer(S, lb, lc, u01(rn.x))].material];
@@ -784,8 +812,9 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
 // Sorted shade, second step: the entries of one list (back = 0: the front
 // list, light-sampling vertices; 1: the back list).
 template <bool NEE, int MINB = NEE ? 3 : 4>
-__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues q, int in,
+__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues qp, int in,
                                                           int back) {
+  const Queues q = oriented(qp, in);
   const uint32_t cap = q.capacity;
   const uint32_t n = min(q.counters[back ? 11 : 10], cap);
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -992,7 +1021,8 @@ __global__ void k_texture_sample(DevScene S, int tex, uint32_t n, const float *u
 
 // ---------------------------------------------------------------- batched form kernels
 
-__global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
+__global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues qp, int out) {
+  const Queues q = oriented(qp, out);  // the queue written is slot 0
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     q.counters[out] = num_paths;
@@ -1008,9 +1038,9 @@ __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues q, int out) {
   const uint32_t pix = (uint32_t)(pg % ((uint64_t)rc.W * rc.H));
   V3 o, d;
   camera_ray(rc, pix % rc.W, pix / rc.W, sub % rc.ss, sub / rc.ss, pix * rc.ss2 + sub, sg.pass_first, o, d);
-  q.orig[out][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
-  q.dir[out][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
-  q.beta[out][i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(si));
+  q.orig[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
+  q.dir[0][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
+  q.beta[0][i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(si));
   q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -1094,6 +1124,7 @@ struct BatchShadowSrc {
 
 template <bool COUNT, bool FN = true, bool HOIST = true>
 __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int in) {
+  const Queues qo = oriented(q, in);
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&q.stats[0], (unsigned long long)n);
@@ -1101,7 +1132,7 @@ __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int 
   }
   uint32_t cnt[3] = {0u, 0u, 0u};
   batch_trace<false, COUNT, BatchQueueSrc, HitSink, FN, HOIST>(
-      b, n, &q.counters[4 + in], BatchQueueSrc{q.orig[in], q.dir[in], q.beta[in]}, HitSink{q.hits}, cnt,
+      b, n, &q.counters[4 + in], BatchQueueSrc{qo.orig[0], qo.dir[0], qo.beta[0]}, HitSink{q.hits}, cnt,
       &q.counters[2]);
   if (COUNT) {
     unsigned long long c0 = cnt[0], c1 = cnt[1], c2 = cnt[2];

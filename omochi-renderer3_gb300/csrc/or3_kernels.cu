@@ -720,10 +720,12 @@ __device__ __forceinline__ void shade_item(const DevScene &S0, const RenderConst
 
 // One path vertex for every queued ray (grid-stride; the loop bound is
 // uniform over the block, as BLK's barriers need).
-template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4, bool BLK = false>
-__global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues qp, int in,
-                                                            Batch b) {
-  const Queues q = oriented(qp, in);
+// IN: the input queue as a template constant, so the oriented pointers come
+// straight from the parameter bank (no registers held across the loop).
+template <bool BATCH, bool NEE, int MINB = NEE ? 3 : 4, bool BLK = false, int IN = 0>
+__global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc0, Wave w0, Queues qp, Batch b) {
+  constexpr int in = IN;
+  const Queues q = oriented(qp, IN);
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
@@ -742,9 +744,10 @@ __global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc
 // by separate kernel instances, so no warp mixes misses, light-sampling
 // vertices and delta vertices.  The roulette is recomputed by the shade
 // kernel from the same Philox counter, so the path is unchanged.
-template <bool NEE>
-__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues qp, int in) {
-  const Queues q = oriented(qp, in);
+template <bool NEE, int IN>
+__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues qp) {
+  constexpr int in = IN;
+  const Queues q = oriented(qp, IN);
   __shared__ uint32_t wcount[2][8], wbase[2];  // per class: warp counts (then offsets), the block's base
   const uint32_t n = min(q.counters[in], q.capacity);
   const uint32_t lane = threadIdx.x & 31u;
@@ -811,10 +814,10 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
 
 // Sorted shade, second step: the entries of one list (back = 0: the front
 // list, light-sampling vertices; 1: the back list).
-template <bool NEE, int MINB = NEE ? 3 : 4>
-__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues qp, int in,
-                                                          int back) {
-  const Queues q = oriented(qp, in);
+template <bool NEE, int IN, int MINB = NEE ? 3 : 4>
+__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues qp, int back) {
+  constexpr int in = IN;
+  const Queues q = oriented(qp, IN);
   const uint32_t cap = q.capacity;
   const uint32_t n = min(q.counters[back ? 11 : 10], cap);
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -1217,31 +1220,45 @@ void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int blo
   }
 }
 
-void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
-                  int grid, int block, cudaStream_t st, bool nee4, bool blk) {
+template <int IN>
+static void launch_shade_in(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int grid,
+                            int block, cudaStream_t st, bool nee4, bool blk) {
   const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
   if (nee && nee4)
-    k_shade<false, true, 4><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+    k_shade<false, true, 4, false, IN><<<grid, block, 0, st>>>(S, rc, w, q, Batch{});
   else if (nee && blk)
-    k_shade<false, true, 3, true><<<grid, 256, 0, st>>>(S, rc, w, q, in, Batch{});
+    k_shade<false, true, 3, true, IN><<<grid, 256, 0, st>>>(S, rc, w, q, Batch{});
   else if (nee)
-    k_shade<false, true><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+    k_shade<false, true, 3, false, IN><<<grid, block, 0, st>>>(S, rc, w, q, Batch{});
   else if (blk)
-    k_shade<false, false, 4, true><<<grid, 256, 0, st>>>(S, rc, w, q, in, Batch{});
+    k_shade<false, false, 4, true, IN><<<grid, 256, 0, st>>>(S, rc, w, q, Batch{});
   else
-    k_shade<false, false><<<grid, block, 0, st>>>(S, rc, w, q, in, Batch{});
+    k_shade<false, false, 4, false, IN><<<grid, block, 0, st>>>(S, rc, w, q, Batch{});
+}
+
+void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
+                  int grid, int block, cudaStream_t st, bool nee4, bool blk) {
+  if (in) launch_shade_in<1>(S, rc, w, q, grid, block, st, nee4, blk);
+  else launch_shade_in<0>(S, rc, w, q, grid, block, st, nee4, blk);
+}
+
+template <int IN>
+static void launch_shade_sorted_in(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q,
+                                   int grid_classify, int grid_nee, int grid_plain, cudaStream_t st) {
+  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
+  if (nee) {
+    k_classify<true, IN><<<grid_classify, 256, 0, st>>>(S, rc, w, q);
+    k_shade_list<true, IN><<<grid_nee, 256, 0, st>>>(S, rc, w, q, 0);
+  } else {
+    k_classify<false, IN><<<grid_classify, 256, 0, st>>>(S, rc, w, q);
+  }
+  k_shade_list<false, IN><<<grid_plain, 256, 0, st>>>(S, rc, w, q, 1);
 }
 
 void launch_shade_sorted(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                          int grid_classify, int grid_nee, int grid_plain, cudaStream_t st) {
-  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
-  if (nee) {
-    k_classify<true><<<grid_classify, 256, 0, st>>>(S, rc, w, q, in);
-    k_shade_list<true><<<grid_nee, 256, 0, st>>>(S, rc, w, q, in, 0);
-  } else {
-    k_classify<false><<<grid_classify, 256, 0, st>>>(S, rc, w, q, in);
-  }
-  k_shade_list<false><<<grid_plain, 256, 0, st>>>(S, rc, w, q, in, 1);
+  if (in) launch_shade_sorted_in<1>(S, rc, w, q, grid_classify, grid_nee, grid_plain, st);
+  else launch_shade_sorted_in<0>(S, rc, w, q, grid_classify, grid_nee, grid_plain, st);
 }
 
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st) {
@@ -1319,8 +1336,8 @@ void launch_texture_sample(const DevScene &S, int tex, uint32_t n, const float *
 
 const void *kernel_extend_ptr() { return (const void *)k_extend<false, 0>; }
 const void *kernel_shade_ptr(bool batch, bool nee) {
-  if (batch) return nee ? (const void *)k_shade<true, true> : (const void *)k_shade<true, false>;
-  return nee ? (const void *)k_shade<false, true> : (const void *)k_shade<false, false>;
+  if (batch) return nee ? (const void *)k_shade<true, true, 3, false, 0> : (const void *)k_shade<true, false, 4, false, 0>;
+  return nee ? (const void *)k_shade<false, true, 3, false, 0> : (const void *)k_shade<false, false, 4, false, 0>;
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1346,8 +1363,13 @@ void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool
 }
 
 void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool nee, cudaStream_t st) {
-  if (nee) k_shade<true, true><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
-  else k_shade<true, false><<<grid, 256, 0, st>>>(DevScene{}, RenderConst{}, Wave{}, q, in, b);
+  const DevScene S{};
+  const RenderConst rc{};
+  const Wave w{};
+  if (nee && in) k_shade<true, true, 3, false, 1><<<grid, 256, 0, st>>>(S, rc, w, q, b);
+  else if (nee) k_shade<true, true, 3, false, 0><<<grid, 256, 0, st>>>(S, rc, w, q, b);
+  else if (in) k_shade<true, false, 4, false, 1><<<grid, 256, 0, st>>>(S, rc, w, q, b);
+  else k_shade<true, false, 4, false, 0><<<grid, 256, 0, st>>>(S, rc, w, q, b);
 }
 
 void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st) {

@@ -162,6 +162,8 @@ typedef struct or3_camera {
                                           (default: the 128-byte FP32-box nodes) */
 #define OR3_FLAG_RELOAD_SCENE 256u     /* batched form: read each ray's node array through its scene
                                           descriptor every step (default: copied to registers per ray) */
+#define OR3_FLAG_UNSORTED_SHADE 512u   /* batched form: one shade kernel for every hit and miss (default where
+                                          the batch samples lights: the material-sorted shade) */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */
@@ -368,6 +370,8 @@ typedef struct or3_server_params {
 
 #define OR3_SERVER_KEEP_MOMENTS 1u /* keep finished jobs' pixel sums on the host for or3_server_get_moments */
 #define OR3_SERVER_ONE_LANE 2u     /* each wave on one stream (default: split over three streams that overlap) */
+#define OR3_SERVER_UNSORTED_SHADE 4u /* one shade kernel for every hit and miss (default where jobs sample lights:
+                                        the material-sorted shade) */
 
 /* frame of job `job_id`: samples so far, frame in the job's output layout,
    final = 1 for the last one.  Called on the server thread. */

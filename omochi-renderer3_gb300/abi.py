@@ -32,6 +32,7 @@ OR3_FLAG_COUNT_TRAVERSAL = 32
 OR3_FLAG_ONE_LANE = 64
 OR3_FLAG_QUANTISED_NODES = 128
 OR3_FLAG_RELOAD_SCENE = 256
+OR3_FLAG_UNSORTED_SHADE = 512
 
 API_VERSION = 1
 OR3_API_VERSION = API_VERSION
@@ -154,6 +155,7 @@ JOB_FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c
 OR3_JOB_QUEUED, OR3_JOB_RUNNING, OR3_JOB_DONE, OR3_JOB_CANCELLED, OR3_JOB_FAILED = 0, 1, 2, 3, 4
 OR3_SERVER_KEEP_MOMENTS = 1
 OR3_SERVER_ONE_LANE = 2
+OR3_SERVER_UNSORTED_SHADE = 4
 OR3_TUNE_EXTEND_MASK = 0x7
 OR3_TUNE_SMEM_NODES = 0x10
 OR3_TUNE_SHADOW_UNSORTED = 0x20

@@ -267,12 +267,18 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   auto lane_batch = [&](int l) { return Batch{B.scenes, B.jobs, B.lanes[l].segs, B.lanes[l].info}; };
   // traversal variant: node layout and how a ray's node array is reached
   const int tvar = ((bp->flags & OR3_FLAG_QUANTISED_NODES) ? 1 : 0) | ((bp->flags & OR3_FLAG_RELOAD_SCENE) ? 2 : 0);
+  // material-sorted shade where the batch samples lights (as or3_render)
+  const bool sorted_shade = shadows && !(bp->flags & OR3_FLAG_UNSORTED_SHADE);
   auto launch_bounces = [&](int l) {
     const Batch b = lane_batch(l);
     for (int k = 0; k < unroll; k++) {
       const int in = k & 1;
       launch_extend_batch(b, ql[l], in, grid_ext, count, tvar, sl[l]);
-      launch_shade_batch(b, ql[l], in, grid_sh, shadows, sl[l]);
+      if (sorted_shade)
+        launch_shade_batch_sorted(b, ql[l], in, true, ctx->num_sms * 8, ctx->num_sms * ctx->occ_shade_nee,
+                                  ctx->num_sms * ctx->occ_shade, sl[l]);
+      else
+        launch_shade_batch(b, ql[l], in, grid_sh, shadows, sl[l]);
       if (shadows) launch_shadow_batch(b, ql[l], grid_ext, tvar, sl[l]);
       launch_reset_count(ql[l], in, sl[l]);
     }

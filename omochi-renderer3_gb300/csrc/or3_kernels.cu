@@ -744,8 +744,41 @@ __global__ void __launch_bounds__(256, MINB) k_shade(DevScene S0, RenderConst rc
 // by separate kernel instances, so no warp mixes misses, light-sampling
 // vertices and delta vertices.  The roulette is recomputed by the shade
 // kernel from the same Philox counter, so the path is unchanged.
-template <bool NEE, int IN>
-__global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wave w, Queues qp) {
+// The class of one queued ray (-1: a miss, shaded here; 0: a light-sampling
+// surface; 1: any other surface), for the ray's scene S, constants rc and
+// the wave's first path number g_first.
+template <bool NEE>
+__device__ __forceinline__ int classify_one(const DevScene &S, const RenderConst &rc, uint64_t g_first,
+                                            const Queues &q, uint32_t i, uint32_t rec, float4 rd) {
+  const uint32_t meta = __float_as_uint(rd.w);
+  const uint32_t depth = meta & 0xFFFFu;
+  if (rec == kMissRec) {
+    if (!(rc.nee && depth > 0 && !(meta & kMetaSpec))) {
+      const float4 ro = q.orig[0][i], rb = q.beta[0][i];
+      add_radiance(q.pathL + __float_as_uint(ro.w), ld3(rb) * env_lookup(S, ld3(rd)));
+    }
+    return -1;
+  }
+  if (!NEE) return 1;
+  uint32_t lb, lc;
+  if (rec & kPlaneBit) {
+    const PlaneRec &pl = S.planes[rec & ~kPlaneBit];
+    lb = pl.layer_begin;
+    lc = pl.layer_count;
+  } else {
+    const PrimInfo &inf = S.info[rec];
+    lb = inf.layer_begin;
+    lc = inf.layer_count;
+  }
+  const uint32_t path = __float_as_uint(q.orig[0][i].w);
+  const uint4 rn = philox(path_counter(g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo, rc.seed_hi);
+  const MaterialDev &m = S.materials[S.layers[lb + pick_layer(S, lb, lc, u01(rn.x))].material];
+  return ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG) ? 0 : 1;
+}
+
+// BATCH: each ray's segment (beta.w) names its job, scene and constants.
+template <bool NEE, int IN, bool BATCH = false>
+__global__ void __launch_bounds__(256) k_classify(DevScene S0, RenderConst rc0, Wave w0, Queues qp, Batch b) {
   constexpr int in = IN;
   const Queues q = oriented(qp, IN);
   __shared__ uint32_t wcount[2][8], wbase[2];  // per class: warp counts (then offsets), the block's base
@@ -757,31 +790,12 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
     if (i < n) {
       const uint32_t rec = __float_as_uint(q.hits[i].y);
       const float4 rd = q.dir[0][i];
-      const uint32_t meta = __float_as_uint(rd.w);
-      const uint32_t depth = meta & 0xFFFFu;
-      if (rec == kMissRec) {
-        if (!(rc.nee && depth > 0 && !(meta & kMetaSpec))) {
-          const float4 ro = q.orig[0][i], rb = q.beta[0][i];
-          add_radiance(q.pathL + __float_as_uint(ro.w), ld3(rb) * env_lookup(S, ld3(rd)));
-        }
-      } else if (NEE) {
-        uint32_t lb, lc;
-        if (rec & kPlaneBit) {
-          const PlaneRec &pl = S.planes[rec & ~kPlaneBit];
-          lb = pl.layer_begin;
-          lc = pl.layer_count;
-        } else {
-          const PrimInfo &inf = S.info[rec];
-          lb = inf.layer_begin;
-          lc = inf.layer_count;
-        }
-        const uint32_t path = __float_as_uint(q.orig[0][i].w);
-        const uint4 rn = philox(path_counter(w.g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo,
-                                rc.seed_hi);
-        const MaterialDev &m = S.materials[S.layers[lb + pick_layer(S, lb, lc, u01(rn.x))].material];
-        cls = ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG) ? 0 : 1;
+      if (BATCH) {
+        const Segment sg = b.segs[__float_as_uint(q.beta[0][i].w)];
+        const JobDev &job = b.jobs[sg.job];
+        cls = classify_one<NEE>(b.scenes[job.scene], job.rc, sg.g_first - sg.wave_first, q, i, rec, rd);
       } else {
-        cls = 1;
+        cls = classify_one<NEE>(S0, rc0, w0.g_first, q, i, rec, rd);
       }
     }
     // block-aggregated appends (one atomic per class and block iteration: the
@@ -814,8 +828,9 @@ __global__ void __launch_bounds__(256) k_classify(DevScene S, RenderConst rc, Wa
 
 // Sorted shade, second step: the entries of one list (back = 0: the front
 // list, light-sampling vertices; 1: the back list).
-template <bool NEE, int IN, int MINB = NEE ? 3 : 4>
-__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues qp, int back) {
+template <bool NEE, int IN, bool BATCH = false, int MINB = NEE ? 3 : 4>
+__global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderConst rc, Wave w, Queues qp, Batch b,
+                                                          int back) {
   constexpr int in = IN;
   const Queues q = oriented(qp, IN);
   const uint32_t cap = q.capacity;
@@ -824,7 +839,7 @@ __global__ void __launch_bounds__(256, MINB) k_shade_list(DevScene S, RenderCons
     const uint32_t k = base + threadIdx.x;
     const bool valid = k < n;
     const uint32_t i = valid ? q.slist[back ? cap - 1u - k : k] : 0u;
-    shade_item<false, NEE, true>(S, rc, w, q, in, Batch{}, valid, i);
+    shade_item<BATCH, NEE, true>(S, rc, w, q, in, b, valid, i);
   }
 }
 
@@ -1242,23 +1257,33 @@ void launch_shade(const DevScene &S, const RenderConst &rc, const Wave &w, const
   else launch_shade_in<0>(S, rc, w, q, grid, block, st, nee4, blk);
 }
 
-template <int IN>
+template <int IN, bool BATCH>
 static void launch_shade_sorted_in(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q,
-                                   int grid_classify, int grid_nee, int grid_plain, cudaStream_t st) {
-  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
+                                   const Batch &b, bool nee, int grid_classify, int grid_nee, int grid_plain,
+                                   cudaStream_t st) {
   if (nee) {
-    k_classify<true, IN><<<grid_classify, 256, 0, st>>>(S, rc, w, q);
-    k_shade_list<true, IN><<<grid_nee, 256, 0, st>>>(S, rc, w, q, 0);
+    k_classify<true, IN, BATCH><<<grid_classify, 256, 0, st>>>(S, rc, w, q, b);
+    k_shade_list<true, IN, BATCH><<<grid_nee, 256, 0, st>>>(S, rc, w, q, b, 0);
   } else {
-    k_classify<false, IN><<<grid_classify, 256, 0, st>>>(S, rc, w, q);
+    k_classify<false, IN, BATCH><<<grid_classify, 256, 0, st>>>(S, rc, w, q, b);
   }
-  k_shade_list<false, IN><<<grid_plain, 256, 0, st>>>(S, rc, w, q, 1);
+  k_shade_list<false, IN, BATCH><<<grid_plain, 256, 0, st>>>(S, rc, w, q, b, 1);
 }
 
 void launch_shade_sorted(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                          int grid_classify, int grid_nee, int grid_plain, cudaStream_t st) {
-  if (in) launch_shade_sorted_in<1>(S, rc, w, q, grid_classify, grid_nee, grid_plain, st);
-  else launch_shade_sorted_in<0>(S, rc, w, q, grid_classify, grid_nee, grid_plain, st);
+  const bool nee = rc.nee && (S.num_lights > 0 || S.env_light != 0);
+  if (in) launch_shade_sorted_in<1, false>(S, rc, w, q, Batch{}, nee, grid_classify, grid_nee, grid_plain, st);
+  else launch_shade_sorted_in<0, false>(S, rc, w, q, Batch{}, nee, grid_classify, grid_nee, grid_plain, st);
+}
+
+void launch_shade_batch_sorted(const Batch &b, const Queues &q, int in, bool nee, int grid_classify, int grid_nee,
+                               int grid_plain, cudaStream_t st) {
+  const DevScene S{};
+  const RenderConst rc{};
+  const Wave w{};
+  if (in) launch_shade_sorted_in<1, true>(S, rc, w, q, b, nee, grid_classify, grid_nee, grid_plain, st);
+  else launch_shade_sorted_in<0, true>(S, rc, w, q, b, nee, grid_classify, grid_nee, grid_plain, st);
 }
 
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st) {

@@ -142,6 +142,10 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st);
 // replaces launch_shade when chosen; 2 or 3 launches.
 void launch_shade_sorted(const DevScene &S, const RenderConst &rc, const Wave &w, const Queues &q, int in,
                          int grid_classify, int grid_nee, int grid_plain, cudaStream_t st);
+// The same for the batched and served forms (nee: the batch's light-sampling
+// instance, as launch_shade_batch picks it).
+void launch_shade_batch_sorted(const Batch &b, const Queues &q, int in, bool nee, int grid_classify, int grid_nee,
+                               int grid_plain, cudaStream_t st);
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st);

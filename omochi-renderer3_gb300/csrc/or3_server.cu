@@ -562,7 +562,12 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
     for (int k = 0; k < S->unroll; k++) {
       const int in = k & 1;
       launch_extend_batch(b, L.q, in, ctx->num_sms * ctx->occ_extend, false, 0, L.st);
-      launch_shade_batch(b, L.q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows, L.st);
+      if (shadows && !(S->p.flags & OR3_SERVER_UNSORTED_SHADE))  // material-sorted shade, as or3_render
+        launch_shade_batch_sorted(b, L.q, in, true, ctx->num_sms * 8, ctx->num_sms * ctx->occ_shade_nee,
+                                  ctx->num_sms * ctx->occ_shade, L.st);
+      else
+        launch_shade_batch(b, L.q, in, ctx->num_sms * (shadows ? ctx->occ_shade_nee : ctx->occ_shade), shadows,
+                           L.st);
       if (shadows) launch_shadow_batch(b, L.q, ctx->num_sms * ctx->occ_extend, 0, L.st);
       launch_reset_count(L.q, in, L.st);
     }

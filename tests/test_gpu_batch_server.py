@@ -16,7 +16,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _jobs(pkg, ctx):
+def _jobs(pkg, ctx, nee=False):
+    """Three jobs; nee: with next-event estimation (the Cornell box's area
+    light, the reference Cornell's SphereLight, the icosphere box's light quad)."""
     W = pkg.workloads
     a = W.cornell_box(40, 32)
     b = W.icosphere_in_box(48, 32, level=3)
@@ -30,6 +32,9 @@ def _jobs(pkg, ctx):
         (sids[2], c[1], dict(supersamples=1, min_samples=4, max_samples=8, step_samples=4, rr_min_depth=5,
                              max_depth=0, seed=7)),
     ]
+    if nee:
+        for _, _, st in jobs:
+            st["next_event_estimation"] = True
     return sids, jobs
 
 
@@ -40,12 +45,16 @@ def _plain(ctx, sid, cam, st):
     return s, q, n, img
 
 
-@pytest.mark.parametrize("wave_paths,flags", [(0, 0), (3000, 0), (3000, 64), (3000, 256)])
-def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags):
+@pytest.mark.parametrize("wave_paths,flags,nee", [(0, 0, False), (3000, 0, False), (3000, 64, False),
+                                                (3000, 256, False), (0, 0, True), (3000, 0, True),
+                                                (3000, 512, True)])
+def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags, nee):
     """flags 64 = OR3_FLAG_ONE_LANE (every wave on one stream; the default
     deals waves to three lanes); 256 = OR3_FLAG_RELOAD_SCENE (the node array
-    read through the scene descriptor every step: the same traversal)."""
-    sids, jobs = _jobs(pkg, ctx)
+    read through the scene descriptor every step: the same traversal); nee:
+    light sampling on, where the material-sorted shade is the default and 512
+    (OR3_FLAG_UNSORTED_SHADE) selects the single shade kernel."""
+    sids, jobs = _jobs(pkg, ctx, nee)
     try:
         alone = [_plain(ctx, *j) for j in jobs]
         stats, frames = ctx.render_batch(jobs, frames=True, wave_paths=wave_paths, flags=flags)
@@ -116,9 +125,9 @@ def test_batch_rejects_bad_jobs(pkg, ctx):
     ctx.release(sid)
 
 
-@pytest.mark.parametrize("one_lane", [False, True])
-def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx, one_lane):
-    sids, jobs = _jobs(pkg, ctx)
+@pytest.mark.parametrize("one_lane,nee", [(False, False), (True, False), (False, True)])
+def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx, one_lane, nee):
+    sids, jobs = _jobs(pkg, ctx, nee)
     alone = [_plain(ctx, *j) for j in jobs]
     frames = defaultdict(list)
     lock = threading.Lock()

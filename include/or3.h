@@ -205,6 +205,8 @@ typedef struct or3_render_params {
                                           without light sampling; with it, it is the default */
 #define OR3_TUNE_UNSORTED_SHADE 0x2000u /* or3_render: one shade kernel for every hit and miss even where
                                           vertices sample lights */
+#define OR3_TUNE_WIDE8 0x4000u         /* or3_render: extension and shadow rays traverse an 8-wide tree made
+                                          from the scene's 4-wide one on first use (kept with the scene) */
 #define OR3_TUNE_BLOCK_APPEND 0x1000u  /* or3_render: the shade kernel appends rays with one atomic per block
                                           instead of one per warp */
 

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libor3.so")
 CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["or3_kernels.cu", "or3_api.cu", "or3_batch.cu", "or3_server.cu", "or3_noalloc.cu", "bvh_build.cpp",
+SOURCES = ["or3_kernels.cu", "or3_api.cu", "or3_batch.cu", "or3_server.cu", "or3_noalloc.cu", "bvh_build.cpp", "bvh_wide8.cpp",
            "bvh_build_gpu.cu", "or3_image.cu", "hdr_io.cpp", "obj_ingest.cpp",
            "scene_file.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -36,6 +36,10 @@ bool build_wide_bvh(const std::vector<BuildPrim> &prims, int bins, int leaf_max,
 
 // FP32-box nodes (WideNodeF) from a built tree's topology and exact child boxes.
 void make_float_nodes(const WideBVH &bvh, std::vector<WideNodeF> &out);
+// The 8-wide tree of the 8-wide traversal variant from a 4-wide FP32-box tree
+// (bvh_wide8.cpp); false if a ray could need more than kStackSize8 stack
+// entries (*max_push: the bound found).
+bool make_wide8_nodes(const std::vector<WideNodeF> &n4, std::vector<WideNode8F> &out, int *max_push);
 
 // Decoded child box of a quantised node, exactly as the kernels compute it.
 void decode_child_box(const WideNode &n, int child, float lo[3], float hi[3]);

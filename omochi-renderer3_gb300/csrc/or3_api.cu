@@ -70,6 +70,25 @@ struct DeviceTemps {
   }
 };
 
+// The scene's 8-wide tree (WideNode8F) for OR3_TUNE_WIDE8, made on the host
+// from its 4-wide FP32-box nodes the first time it is asked for.
+int ensure_wide8(or3_context *ctx, SceneGPU *sg) {
+  if (sg->view.fnodes8 || sg->view.num_nodes == 0) return OR3_OK;
+  std::vector<WideNodeF> n4(sg->view.num_nodes);
+  OR3_CUDA(ctx, cudaMemcpy(n4.data(), sg->view.fnodes, n4.size() * sizeof(WideNodeF), cudaMemcpyDeviceToHost));
+  std::vector<WideNode8F> n8;
+  int pushes = 0;
+  if (!make_wide8_nodes(n4, n8, &pushes))
+    return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "8-wide tree: a ray could need %d stack entries (limit %d)", pushes,
+                kStackSize8);
+  void *d = nullptr;
+  OR3_CUDA(ctx, cudaMalloc(&d, n8.size() * sizeof(WideNode8F)));
+  sg->allocs.push_back(d);
+  OR3_CUDA(ctx, cudaMemcpy(d, n8.data(), n8.size() * sizeof(WideNode8F), cudaMemcpyHostToDevice));
+  sg->view.fnodes8 = static_cast<const float4 *>(d);
+  return OR3_OK;
+}
+
 void free_scene(SceneGPU *sg) {
   for (void *p : sg->allocs) cudaFree(p);
   delete sg;
@@ -1054,7 +1073,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const int grid_ext = ctx->num_sms * ctx->occ_extend;
   const int smem_nodes =
       (prm->tuning & OR3_TUNE_SMEM_NODES) ? (int)std::min<uint64_t>(256, sg->view.num_nodes) : 0;
-  const int variant = extend_variant(prm->tuning);
+  // the 8-wide traversal variant: its tree is made from the 4-wide one on first use
+  const bool wide8 = (prm->tuning & OR3_TUNE_WIDE8) != 0;
+  if (wide8) {
+    if (int r = ensure_wide8(ctx, sg)) return r;
+  }
+  const int variant = wide8 ? 8 : extend_variant(prm->tuning);
   // L2 persisting window over the BVH nodes (a context setting, restored below)
   const bool l2win = (prm->tuning & OR3_TUNE_L2_PERSIST) != 0;
   if (l2win) {
@@ -1205,7 +1229,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         }
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
         if (shadows)
-          launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl);
+          launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl,
+                        wide8);
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
         launch_reset_count(ql, in, sl);
         lr[l].in ^= 1;

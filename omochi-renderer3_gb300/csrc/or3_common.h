@@ -64,6 +64,21 @@ struct alignas(16) WideNodeF {
 };
 static_assert(sizeof(WideNodeF) == 128, "WideNodeF must be 128 bytes");
 
+// 8-wide node with FP32 child boxes (256 bytes), for the 8-wide traversal
+// variant: b[2a] / b[2a+1] the lower / upper bounds of the 8 children on axis
+// a (so float4 2p + h holds plane p of children 4h..4h+3), then the child
+// words (node index or first record), the counts (ntri | nsph << 4) and the
+// internal mask as in WideNodeF.
+struct alignas(16) WideNode8F {
+  float b[6][8];
+  uint32_t child[8];
+  uint8_t count[8];
+  uint32_t imask;
+  uint32_t pad[5];
+};
+static_assert(sizeof(WideNode8F) == 256, "WideNode8F must be 256 bytes");
+constexpr int kStackSize8 = 96;  // traversal stack entries per ray over 8-wide nodes
+
 // One child slab of a WideNodeF: the exact bound [lo, hi] widened by 2^-18
 // of the parent's extent on that axis and then two ulps, so that the
 // rounding of the slab distances cannot drop a ray that grazes a box face.

@@ -13,6 +13,7 @@ namespace or3 {
 struct DevScene {
   const uint4 *nodes;          // WideNode[num_nodes] as 4 x uint4
   const float4 *fnodes;        // WideNodeF[num_nodes] as 8 x float4 (optional FP32-box copy)
+  const float4 *fnodes8;       // WideNode8F as 16 x float4: the 8-wide traversal variant (made on first use)
   const float4 *prims;         // 3 x float4 per record
   const PrimInfo *info;        // per record
   const TriShade *tri_shade;   // per record (triangles)
@@ -579,6 +580,81 @@ __device__ __forceinline__ bool trav_step_inline(const SV &S, TravState &s, STK 
       }
     }
     s.entry = kid[0];
+    return false;
+  }
+  return !trav_pop_stk(s, stk);
+}
+
+// One step over the 8-wide FP32-box nodes (S.fnodes8): the node's hit leaf
+// children are tested in place, the nearest internal child is next and the
+// others go on the stack (popped entries pruned by their entry distance).
+// The stack holds kStackSize8 entries (bound checked when the tree is made).
+template <bool ANY, bool COUNT, class STK>
+__device__ __forceinline__ bool trav_step_w8(const DevScene &S, TravState &s, STK &stk, uint32_t *cnt) {
+  const uint32_t e = s.entry;
+  if (e == kNoEntry) return true;
+  if (COUNT) cnt[0]++;
+  const float4 *np = S.fnodes8 + 16 * (size_t)e;
+  const uint32_t sx = s.signs & 1u, sy = (s.signs >> 1) & 1u, sz = (s.signs >> 2) & 1u;
+  const uint4 c0 = __ldg(reinterpret_cast<const uint4 *>(np + 12));
+  const uint4 c1 = __ldg(reinterpret_cast<const uint4 *>(np + 13));
+  const uint4 mt = __ldg(reinterpret_cast<const uint4 *>(np + 14));
+  const float tlimit = s.tmax * 1.0000010f;
+  const float inf2 = kInf * 2.f;
+  float key[8];
+  uint32_t leafmask = 0;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const float4 bnx = __ldg(np + 2 * sx + h), bfx = __ldg(np + 2 * (sx ^ 1u) + h);
+    const float4 bny = __ldg(np + 4 + 2 * sy + h), bfy = __ldg(np + 4 + 2 * (sy ^ 1u) + h);
+    const float4 bnz = __ldg(np + 8 + 2 * sz + h), bfz = __ldg(np + 8 + 2 * (sz ^ 1u) + h);
+    const float nxa[4] = {bnx.x, bnx.y, bnx.z, bnx.w}, fxa[4] = {bfx.x, bfx.y, bfx.z, bfx.w};
+    const float nya[4] = {bny.x, bny.y, bny.z, bny.w}, fya[4] = {bfy.x, bfy.y, bfy.z, bfy.w};
+    const float nza[4] = {bnz.x, bnz.y, bnz.z, bnz.w}, fza[4] = {bfz.x, bfz.y, bfz.z, bfz.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int c = 4 * h + i;
+      const float tnx = fmaf(nxa[i], s.inv.x, s.oi.x), tfx = fmaf(fxa[i], s.inv.x, s.oi.x);
+      const float tny = fmaf(nya[i], s.inv.y, s.oi.y), tfy = fmaf(fya[i], s.inv.y, s.oi.y);
+      const float tnz = fmaf(nza[i], s.inv.z, s.oi.z), tfz = fmaf(fza[i], s.inv.z, s.oi.z);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+      const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * 1.0000010f, tlimit);
+      const bool internal = (mt.z >> c) & 1u;
+      const bool hitbox = tn <= tf;  // never for an empty slot
+      key[c] = (hitbox && internal) ? tn : inf2;
+      if (hitbox && !internal) leafmask |= 1u << c;
+    }
+  }
+  while (leafmask) {
+    const uint32_t i = __ffs(leafmask) - 1;
+    leafmask &= leafmask - 1;
+    const uint4 cw = i < 4 ? c0 : c1;
+    const uint32_t j = i & 3u;
+    const uint32_t first = j == 0 ? cw.x : j == 1 ? cw.y : j == 2 ? cw.z : cw.w;
+    trav_leaf<COUNT>(S, s, first, ((i < 4 ? mt.x : mt.y) >> (8 * j)) & 0xFFu, cnt);
+  }
+  if (ANY && s.rec != kMissRec) return true;
+  const uint32_t kids[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+  float kmin = key[0];
+  uint32_t next = kids[0];
+  int jmin = 0;
+#pragma unroll
+  for (int j = 1; j < 8; j++) {
+    if (key[j] < kmin) {
+      kmin = key[j];
+      next = kids[j];
+      jmin = j;
+    }
+  }
+  if (kmin < inf2 && kmin <= s.tmax * 1.0000010f) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (j != jmin && key[j] < inf2) {
+        stk.put(s.sp, kids[j], key[j]);
+        s.sp = min(s.sp + 1, kStackSize8 - 1);
+      }
+    }
+    s.entry = next;
     return false;
   }
   return !trav_pop_stk(s, stk);

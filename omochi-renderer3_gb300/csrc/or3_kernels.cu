@@ -112,13 +112,13 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // nearest-first child order (off only for any-hit queries).  FN: STEP 2 over
 // the FP32-box nodes (else the quantised ones).
 template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, bool FN = true,
-          bool NEAREST = false>
+          bool NEAREST = false, bool W8 = false>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
   uint32_t stk_e[kStackSize];
   float stk_t[kStackSize];
-  uint2 stk_p[kStackSize];
+  uint2 stk_p[W8 ? kStackSize8 : kStackSize];
   PairStack stk{stk_p};
   TravState st;
   uint32_t r = kNoEntry;
@@ -146,9 +146,10 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
       break;
     }
     if (r != kNoEntry) {
-      const bool done = STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                  : trav_step_inline<ANY, COUNT, SORT, PairStack, FN, DevScene, NEAREST>(
-                                        S, st, stk, snodes, ns, cnt, err);
+      const bool done = W8          ? trav_step_w8<ANY, COUNT>(S, st, stk, cnt)
+                        : STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
+                                    : trav_step_inline<ANY, COUNT, SORT, PairStack, FN, DevScene, NEAREST>(
+                                          S, st, stk, snodes, ns, cnt, err);
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;
@@ -203,7 +204,8 @@ __device__ __forceinline__ void gridstride_trace(const DevScene &S, uint32_t n, 
 // spheres each ray touched to stats[3..5] (the algorithmic byte count).
 // VARIANT 0: gridstride_trace; 1: persistent_trace STEP 1; 2, 4, 5: STEP 2
 // refilling at 16, 8 or 24 idle lanes; 6: STEP 2 over the quantised nodes;
-// 7: STEP 2, nearest internal child next and its siblings pushed unsorted.
+// 7: STEP 2, nearest internal child next and its siblings pushed unsorted;
+// 8: the 8-wide nodes (S.fnodes8), as 7.
 // 0, 1 and 6 read the quantised nodes (and may stage the top ones in shared
 // memory), 2, 4 and 5 the FP32-box nodes.
 template <bool COUNT, int VARIANT>
@@ -232,7 +234,8 @@ __device__ __forceinline__ void extend_body(const DevScene &S, const Queues &q, 
   } else {
     constexpr int kStep = VARIANT == 1 ? 1 : 2;
     constexpr int kRefill = VARIANT == 4 ? 8 : VARIANT == 5 ? 24 : 16;
-    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, VARIANT != 7, VARIANT != 6, VARIANT == 7>(
+    persistent_trace<false, COUNT, kStep, QueueSrc, HitSink, kRefill, VARIANT != 7, VARIANT != 6, VARIANT == 7,
+                     VARIANT == 8>(
         S, n, &q.counters[4 + in], QueueSrc{q.orig[0], q.dir[0]}, HitSink{q.hits}, snodes, ns, cnt,
         &q.counters[2]);
   }
@@ -887,11 +890,11 @@ struct ShadowSink {
 // Any-hit test of every queued shadow ray (persistent, lane-refilled).
 // SORT false: children in slot order (no distance sort).
 // FN: FP32-box nodes (else the quantised ones).
-template <bool SORT, bool FN>
+template <bool SORT, bool FN, bool W8 = false>
 __global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT, FN>(
+  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT, FN, false, W8>(
       S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir}, ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u,
       nullptr, &q.counters[2]);
 }
@@ -1219,6 +1222,11 @@ void launch_raygen(const RenderConst &rc, const Wave &w, const Queues &q, int ou
 void launch_extend(const DevScene &S, const Queues &q, int in, int grid, int block, int smem_nodes, bool count,
                    int variant, cudaStream_t st) {
   const int sn = smem_nodes > kSmemNodes ? kSmemNodes : smem_nodes;
+  if (variant == 8) {  // the 8-wide nodes
+    if (count) k_extend<true, 8><<<grid, block, 0, st>>>(S, q, in, 0);
+    else k_extend<false, 8><<<grid, block, 0, st>>>(S, q, in, 0);
+    return;
+  }
   switch ((count ? 8 : 0) | (variant & 7)) {
     case 1: k_extend<false, 1><<<grid, block, 0, st>>>(S, q, in, sn); break;
     case 2: k_extend<false, 2><<<grid, block, 0, st>>>(S, q, in, 0); break;
@@ -1295,8 +1303,10 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
   k_reset_count<<<1, 1, 0, st>>>(q.counters, which);
 }
 
-void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st) {
-  if (quantised) k_shadow<true, false><<<grid, 256, 0, st>>>(S, q);
+void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st,
+                   bool wide8) {
+  if (wide8) k_shadow<false, true, true><<<grid, 256, 0, st>>>(S, q);
+  else if (quantised) k_shadow<true, false><<<grid, 256, 0, st>>>(S, q);
   else if (unsorted) k_shadow<false, true><<<grid, 256, 0, st>>>(S, q);
   else k_shadow<true, true><<<grid, 256, 0, st>>>(S, q);
 }

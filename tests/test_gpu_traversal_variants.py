@@ -28,6 +28,7 @@ VARIANTS = {
     "sorted_shade": 0x800,
     "unsorted_shade": 0x2000,
     "block_append": 0x1000,
+    "wide8": 0x4000,
 }
 
 

@@ -773,9 +773,13 @@ __device__ __forceinline__ int classify_one(const DevScene &S, const RenderConst
     lb = inf.layer_begin;
     lc = inf.layer_count;
   }
-  const uint32_t path = __float_as_uint(q.orig[0][i].w);
-  const uint4 rn = philox(path_counter(g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo, rc.seed_hi);
-  const MaterialDev &m = S.materials[S.layers[lb + pick_layer(S, lb, lc, u01(rn.x))].material];
+  uint32_t sel = 0;  // a one-layer object needs no roulette draw
+  if (lc > 1) {
+    const uint32_t path = __float_as_uint(q.orig[0][i].w);
+    const uint4 rn = philox(path_counter(g_first + path, (meta >> 16) & 0xFFu, depth, 0u), rc.seed_lo, rc.seed_hi);
+    sel = pick_layer(S, lb, lc, u01(rn.x));
+  }
+  const MaterialDev &m = S.materials[S.layers[lb + sel].material];
   return ((m.type == OR3_LAMBERT && !m.emissive) || m.type == OR3_PHONG) ? 0 : 1;
 }
 

@@ -72,17 +72,12 @@ def workload(pkg, name):
     return sd, cam, st, desc
 
 
-def rmse_vs_16k(ctx, cam, name):
-    """Image RMSE of the last render against the workload's 16384-spp
-    reference (tests/golden/rmse_*.npz: tiles of an FP64 oracle render for the
-    mesh and terrain, the reference's own full image for the Cornell box),
-    with the RMSE the two renders' noise alone predicts.  None without one."""
-    fname = {"cornell": "rmse_cornell_cfg.npz", "mesh": "rmse_mesh.npz", "terrain": "rmse_terrain.npz"}[name]
-    path = os.path.join(ROOT, "tests", "golden", fname)
-    if not os.path.exists(path):
-        return None
-    g = np.load(path)
-    s, q, n = ctx.moments(cam.width, cam.height)
+def tile_rmse(s, q, n, fixture):
+    """RMSE of a render's pixel moments (sums s, sums of squares q over n
+    samples, rows top-down) against a 16384-spp reference fixture: tiles (rows
+    counted from the bottom, as camera rows) or a whole image; with the RMSE
+    the noise of both renders predicts."""
+    g = np.load(fixture)
     m = s / n
     se2 = np.maximum(q / n - m * m, 0.0) / n
     if "tiles" in g.files:
@@ -100,6 +95,19 @@ def rmse_vs_16k(ctx, cam, name):
     rmse = float(np.sqrt(np.mean(d2)))
     return {"value": rmse, "expected_from_noise": float(np.sqrt(np.mean(v))),
             "relative": rmse / float(np.mean(ref)), "spp": int(n), "reference": what}
+
+
+def rmse_vs_16k(ctx, cam, name):
+    """Image RMSE of the last render against the workload's 16384-spp
+    reference (tests/golden/rmse_*.npz: tiles of an FP64 oracle render for the
+    mesh and terrain, the reference's own full image for the Cornell box).
+    None without one."""
+    fname = {"cornell": "rmse_cornell_cfg.npz", "mesh": "rmse_mesh.npz", "terrain": "rmse_terrain.npz"}[name]
+    path = os.path.join(ROOT, "tests", "golden", fname)
+    if not os.path.exists(path):
+        return None
+    s, q, n = ctx.moments(cam.width, cam.height)
+    return tile_rmse(s, q, n, path)
 
 
 def load_peaks():
@@ -314,6 +322,14 @@ def run_batched(args, pkg):
         s, _ = ctx.render_batch(jobs, **best)
         batch_wall.append(time.perf_counter() - w0)
         batch_ms.append(s["render_ms"])
+    # image error of the first job in the last timed batch (the same paths as its plain render)
+    rmse = None
+    fix = os.path.join(ROOT, "tests", "golden", "rmse_batched_job0.npz")
+    if (args.mix == "config" and args.scale == 1.0 and os.path.exists(fix) and
+            jobs_sd[0][0].digest() == str(np.load(fix)["digest"])):
+        cam0 = jobs[0][1]
+        s0, q0, n0 = ctx.batch_moments(0, cam0.width, cam0.height)
+        rmse = dict(tile_rmse(s0, q0, n0, fix), job=0)
     # equal images: a batched job equals its plain render (same paths), checked on a few jobs
     maxdiff = 0.0
     for k in (0, 1, len(jobs) - 1):
@@ -336,7 +352,7 @@ def run_batched(args, pkg):
                            "what": "the same 64 renders, one or3_render call each, scenes resident"},
             "speedup_vs_plain": plain_ms / bms, "batch_wall_s": float(np.median(batch_wall)),
             "speedup_vs_plain_wall": plain_wall / float(np.median(batch_wall)),
-            "equal_images_max_rel_diff": maxdiff}
+            "equal_images_max_rel_diff": maxdiff, "rmse_vs_16k": rmse}
     print(json.dumps(line), flush=True)
     ctx.close()
 

@@ -14,10 +14,12 @@ committed and are all the GPU tests need.
                         PathTracer::Radiance estimator (float16), sample counts
   rmse_cornell_cfg.npz  (--rmse) 16384-spp reference render of the Cornell
                         workload, the RMSE target
-  rmse_mesh.npz, rmse_terrain.npz  (--only rmse_mesh / rmse_terrain) 16384-spp
+  rmse_mesh.npz, rmse_terrain.npz, rmse_batched_job0.npz
+                        (--only rmse_mesh / rmse_terrain / rmse_batched_job0) 16384-spp
                         FP64 oracle renders of five 32x32 tiles of the mesh and
-                        terrain workloads (their own sub-pixel grids), the RMSE
-                        targets of those workloads
+                        terrain workloads and of the batched workload's first job
+                        (their own sub-pixel grids), the RMSE targets of those
+                        workloads
   obj_ref.npz           the reference's Model::ReadFromObj + Transform of
                         tests/golden/obj/mesh.obj (with and without the v flip)
   image_codec.npz       the reference's 8-bit conversion (gamma on and off),
@@ -273,7 +275,9 @@ def make_rmse():
 # FP64 C oracle: the mesh's Phong lobe and the terrain's light sampling have
 # no counterpart in the reference, and the oracle is pinned to the reference
 # wherever they overlap.
-RMSE_CONFIGS = {"mesh": lambda: W.icosphere_in_box(), "terrain": lambda: W.terrain_ibl()}
+RMSE_CONFIGS = {"mesh": lambda: W.icosphere_in_box(), "terrain": lambda: W.terrain_ibl(),
+                # the batched workload's first job (1.31M-triangle icosphere in the box, NEE)
+                "batched_job0": lambda: W.batched_jobs(n=1)[0]}
 RMSE_SEED = 0x5EED16
 
 

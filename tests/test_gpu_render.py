@@ -127,18 +127,22 @@ def tile_rmse(fixture, m, se):
     return float(np.sqrt(np.mean(d2))), float(np.sqrt(np.mean(v)))
 
 
-@pytest.mark.parametrize("name", ["mesh", "terrain"])
+@pytest.mark.parametrize("name", ["mesh", "terrain", "batched_job0"])
 def test_rmse_of_benchmark_workloads_against_16k_oracle(pkg, ctx, name):
     # the full benchmark render (its resolution, sub-pixel grid, depth and
-    # light sampling) against the FP64 oracle's 16384-spp tiles
+    # light sampling) against the FP64 oracle's 16384-spp tiles; batched_job0
+    # is the batched workload's first job, rendered plainly (a batch renders
+    # the same paths)
     g = golden("rmse_%s.npz" % name)
-    sd, cam, st = pkg.workloads.icosphere_in_box() if name == "mesh" else pkg.workloads.terrain_ibl()
+    W = pkg.workloads
+    sd, cam, st = {"mesh": W.icosphere_in_box, "terrain": W.terrain_ibl,
+                   "batched_job0": lambda: W.batched_jobs(n=1)[0]}[name]()
     assert sd.digest() == str(g["digest"])
     assert (int(g["width"]), int(g["height"]), int(g["supersamples"])) == (cam.width, cam.height,
                                                                            st["supersamples"])
     sid = ctx.upload(sd)
     try:
-        ctx.render(sid, cam, seed=7, **st)
+        ctx.render(sid, cam, **dict(st, seed=7))
         s, q, n = ctx.moments(cam.width, cam.height)
     finally:
         ctx.release(sid)

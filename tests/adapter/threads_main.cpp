@@ -51,7 +51,7 @@ int main() {
   // a reader polling GetResult() while the renders run.  Double buffering
   // promises whole frames to a reader that is done before the next pass
   // completes (a pass takes 5 ms here); a read the scheduler stretched past
-  // 2 ms is not judged.
+  // 2 ms is not counted.
   std::atomic<bool> reading(true);
   std::atomic<long> reads(0), torn(0), slow(0);
   std::thread reader([&]() {
@@ -123,7 +123,7 @@ int main() {
   r2->RenderScene(scene);  // and it renders again
   CHECK(r2->GetCurrentSampleCount() == 10);
 
-  std::printf("reads %ld torn %ld (slow reads not judged %ld) stopped after %.1f ms, fails %d\n", reads.load(),
+  std::printf("reads %ld torn %ld (slow reads not counted %ld) stopped after %.1f ms, fails %d\n", reads.load(),
               torn.load(), slow.load(), ms, fails);
   return fails ? 1 : 0;
 }

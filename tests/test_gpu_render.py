@@ -286,7 +286,7 @@ def test_lanes_fall_back_when_device_memory_is_short(pkg, ctx):
             del filler
             torch.cuda.empty_cache()
             c2.release(sid)
-    # (the driver may find room for one extra lane by trimming its own pools)
+    # (the CUDA driver may find room for one extra lane by trimming its own pools)
     assert s["waves"] >= 4 and s["lanes"] < 3, s["lanes"]
     np.testing.assert_allclose(f2, f1, rtol=1e-5, atol=1e-7)
 

@@ -168,6 +168,7 @@ OR3_TUNE_SORTED_SHADE = 0x800
 OR3_TUNE_BLOCK_APPEND = 0x1000
 OR3_TUNE_UNSORTED_SHADE = 0x2000
 OR3_TUNE_WIDE8 = 0x4000
+OR3_TUNE_SHADOW_REFILL8 = 0x8000
 
 # name -> (restype, argtypes); every function declared in include/or3.h
 PROTOTYPES = {

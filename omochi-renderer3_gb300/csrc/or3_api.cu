@@ -1230,7 +1230,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[2], st));
         if (shadows)
           launch_shadow(sg->view, ql, grid_ext, (prm->tuning & OR3_TUNE_SHADOW_UNSORTED) != 0, variant == 6, sl,
-                        wide8);
+                        wide8, (prm->tuning & OR3_TUNE_SHADOW_REFILL8) != 0);
         if (timek) OR3_CUDA(ctx, cudaEventRecord(e4[3], st));
         launch_reset_count(ql, in, sl);
         lr[l].in ^= 1;

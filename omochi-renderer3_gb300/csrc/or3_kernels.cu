@@ -894,11 +894,12 @@ struct ShadowSink {
 // Any-hit test of every queued shadow ray (persistent, lane-refilled).
 // SORT false: children in slot order (no distance sort).
 // FN: FP32-box nodes (else the quantised ones).
-template <bool SORT, bool FN, bool W8 = false>
+// REFILL: a warp fetches new rays once this many lanes are idle.
+template <bool SORT, bool FN, bool W8 = false, int REFILL = 16>
 __global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, 16, SORT, FN, false, W8>(
+  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, REFILL, SORT, FN, false, W8>(
       S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir}, ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u,
       nullptr, &q.counters[2]);
 }
@@ -1308,8 +1309,9 @@ void launch_reset_count(const Queues &q, int which, cudaStream_t st) {
 }
 
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st,
-                   bool wide8) {
+                   bool wide8, bool refill8) {
   if (wide8) k_shadow<false, true, true><<<grid, 256, 0, st>>>(S, q);
+  else if (refill8) k_shadow<true, true, false, 8><<<grid, 256, 0, st>>>(S, q);
   else if (quantised) k_shadow<true, false><<<grid, 256, 0, st>>>(S, q);
   else if (unsorted) k_shadow<false, true><<<grid, 256, 0, st>>>(S, q);
   else k_shadow<true, true><<<grid, 256, 0, st>>>(S, q);

@@ -149,7 +149,7 @@ void launch_shade_batch_sorted(const Batch &b, const Queues &q, int in, bool nee
 void launch_merge_sums(size_t n, double *a, double *aq, double *b, double *bq, int max_grid, cudaStream_t st);
 // any-hit test of the shadow queue; unoccluded samples add to their path's radiance
 void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, bool quantised, cudaStream_t st,
-                   bool wide8 = false);
+                   bool wide8 = false, bool refill8 = false);
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, int variant, cudaStream_t st);
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st);

@@ -29,6 +29,7 @@ VARIANTS = {
     "unsorted_shade": 0x2000,
     "block_append": 0x1000,
     "wide8": 0x4000,
+    "shadow_refill8": 0x8000,
 }
 
 

@@ -164,6 +164,10 @@ typedef struct or3_camera {
                                           descriptor every step (default: copied to registers per ray) */
 #define OR3_FLAG_UNSORTED_SHADE 512u   /* batched form: one shade kernel for every hit and miss (default where
                                           the batch samples lights: the material-sorted shade) */
+#define OR3_FLAG_HOST_LOOP 1024u       /* batched form: the host hands out waves and replays each wave's
+                                          bounce graph (default: the device runs the whole batch, each lane
+                                          one graph launch whose while loop takes waves from a shared
+                                          device queue) */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */
@@ -335,8 +339,8 @@ typedef struct or3_batch_job {
 
 typedef struct or3_batch_params {
   uint64_t wave_paths;     /* camera paths per wave, 0 = automatic */
-  uint32_t flags;          /* OR3_FLAG_NO_GRAPH, OR3_FLAG_COUNT_TRAVERSAL, OR3_FLAG_ONE_LANE */
-  uint32_t graph_bounces;  /* bounce iterations per graph launch, 0 = 8 */
+  uint32_t flags;          /* OR3_FLAG_NO_GRAPH, OR3_FLAG_COUNT_TRAVERSAL, OR3_FLAG_ONE_LANE, OR3_FLAG_HOST_LOOP, ... */
+  uint32_t graph_bounces;  /* bounce iterations per loop iteration / graph replay, 0 = 8 */
   uint32_t blocks_per_sm;  /* persistent kernel blocks per SM, 0 = occupancy limit */
   uint32_t reserved;
 } or3_batch_params;

@@ -33,6 +33,7 @@ OR3_FLAG_ONE_LANE = 64
 OR3_FLAG_QUANTISED_NODES = 128
 OR3_FLAG_RELOAD_SCENE = 256
 OR3_FLAG_UNSORTED_SHADE = 512
+OR3_FLAG_HOST_LOOP = 1024
 
 API_VERSION = 1
 OR3_API_VERSION = API_VERSION

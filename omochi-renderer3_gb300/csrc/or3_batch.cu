@@ -8,9 +8,17 @@
 // and a planner packs segments of all jobs into waves of up to `wave_paths`
 // camera paths.  Rays carry their segment index, so the multi-job kernels
 // (raygen/extend/shade/accumulate *_batch) pick scene, camera, depth policy and
-// RNG numbering per ray.  The bounce loop of a wave is a captured CUDA graph of
-// `graph_bounces` extend/shade/reset iterations, replayed until the wave's
-// queue is empty (one host round trip per replay instead of per kernel).
+// RNG numbering per ray.
+//
+// By default the device runs the whole batch: all planned waves sit in one
+// device table, and each wave lane (stream and ray queues) is ONE launch of a
+// graph whose single node is a while loop.  Its body takes the next wave from
+// the shared head counter when the lane is idle, writes the wave's camera
+// rays, runs `graph_bounces` extend/shade/shadow iterations, accumulates a
+// wave whose queue ran empty, and ends the loop when the queue of waves is
+// empty, with no host round trip in between.  OR3_FLAG_HOST_LOOP keeps the
+// host-driven form: the host hands each wave to a free lane and replays the
+// wave's captured bounce graph until its queue is empty.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +54,12 @@ struct BatchBuffers {
   } lanes[3];
   double *frame_dev = nullptr, *frame_pinned = nullptr;
   size_t cap_frame = 0;
+  // the device loop: every wave's segments, the wave table, the loop state
+  Segment *segs_all = nullptr;
+  size_t cap_segs_all = 0;
+  WaveDesc *wdesc = nullptr;
+  size_t cap_wdesc = 0;
+  BatchLoop *loop = nullptr;
   struct JobOut {
     uint64_t pix_base;
     uint32_t W, H;
@@ -72,6 +86,9 @@ void destroy_batch_state(or3_context *ctx) {
   }
   cudaFree(b->frame_dev);
   cudaFreeHost(b->frame_pinned);
+  cudaFree(b->segs_all);
+  cudaFree(b->wdesc);
+  cudaFree(b->loop);
   delete b;
   ctx->batch = nullptr;
 }
@@ -291,7 +308,65 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     }
   } guard;
   const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
-  if (use_graph) {
+  const bool device_loop = use_graph && !(bp->flags & OR3_FLAG_HOST_LOOP);
+  struct LoopGraphs {
+    cudaGraph_t g[3] = {nullptr, nullptr, nullptr};
+    ~LoopGraphs() {
+      for (cudaGraph_t x : g)
+        if (x) cudaGraphDestroy(x);
+    }
+  } lg;
+  if (device_loop) {
+    // the wave queue: all planned waves' segments in one table, read by the
+    // lanes' loop heads as they take waves
+    std::vector<Segment> all;
+    std::vector<WaveDesc> wd(waves.size());
+    for (size_t w = 0; w < waves.size(); w++) {
+      wd[w] = WaveDesc{(uint32_t)all.size(), (uint32_t)waves[w].segs.size(), waves[w].ngroups, waves[w].num_paths};
+      all.insert(all.end(), waves[w].segs.begin(), waves[w].segs.end());
+    }
+    if ((rc = grow_dev(ctx, B.segs_all, B.cap_segs_all, all.size()))) return rc;
+    if ((rc = grow_dev(ctx, B.wdesc, B.cap_wdesc, wd.size()))) return rc;
+    if (!B.loop) OR3_CUDA(ctx, cudaMalloc(&B.loop, sizeof(BatchLoop)));
+    BatchLoop hl{};
+    hl.nwaves = (uint32_t)wd.size();
+    hl.max_iters = 1u << 16;  // per wave, as the host loop's replay bound
+    if (!all.empty())
+      OR3_CUDA(ctx, cudaMemcpyAsync(B.segs_all, all.data(), all.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
+    if (!wd.empty())
+      OR3_CUDA(ctx, cudaMemcpyAsync(B.wdesc, wd.data(), wd.size() * sizeof(WaveDesc), cudaMemcpyHostToDevice, st));
+    OR3_CUDA(ctx, cudaMemcpyAsync(B.loop, &hl, sizeof(hl), cudaMemcpyHostToDevice, st));
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    // per lane: a graph whose one node is a while loop; its body takes a wave
+    // when the lane is idle, runs `unroll` bounces, and completes the wave
+    // when its queue is empty
+    for (int l = 0; l < nl; l++) {
+      OR3_CUDA(ctx, cudaGraphCreate(&lg.g[l], 0));
+      cudaGraphConditionalHandle h{};
+      OR3_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, lg.g[l], 1u, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      OR3_CUDA(ctx, cudaGraphAddNode(&node, lg.g[l], nullptr, nullptr, 0, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      OR3_CUDA(ctx, cudaStreamBeginCaptureToGraph(sl[l], body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      BatchBuffers::Lane &L = B.lanes[l];
+      const Batch b = lane_batch(l);
+      launch_wave_take(B.loop, l, B.wdesc, B.segs_all, L.segs, L.info, ql[l].counters, h, sl[l]);
+      launch_raygen_batch_loop(b, ql[l], B.loop, l, ctx->num_sms * 8, sl[l]);
+      launch_bounces(l);
+      launch_accumulate_batch_loop(b, ql[l], B.loop, l, ctx->num_sms * 8, sl[l]);
+      launch_wave_finish(B.loop, l, L.info, ql[l].counters, sl[l]);
+      cudaGraph_t captured = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(sl[l], &captured);
+      if (ce != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "device loop capture: %s", cudaGetErrorString(ce));
+      const cudaError_t ie = cudaGraphInstantiate(&guard.g[l], lg.g[l], 0);
+      if (ie != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "device loop instantiate: %s", cudaGetErrorString(ie));
+    }
+  } else if (use_graph) {
     OR3_CUDA(ctx, cudaStreamSynchronize(st));
     for (int l = 0; l < nl; l++) {
       cudaGraph_t graph = nullptr;
@@ -337,9 +412,13 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     return replay(l);
   };
   int live = 0;
-  for (int l = 0; l < nl; l++) {
-    if ((rc = start(l))) return rc;
-    if (wave_of[l] >= 0) live++;
+  if (device_loop) {  // the lanes' loops run the whole batch
+    for (int l = 0; l < nl; l++) OR3_CUDA(ctx, cudaGraphLaunch(guard.g[l], sl[l]));
+  } else {
+    for (int l = 0; l < nl; l++) {
+      if ((rc = start(l))) return rc;
+      if (wave_of[l] >= 0) live++;
+    }
   }
   while (live > 0) {
     for (int l = 0; l < nl; l++) {
@@ -377,6 +456,25 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   stats.render_ms = ms;
+  if (device_loop) {
+    BatchLoop hl{};
+    OR3_CUDA(ctx, cudaMemcpy(&hl, B.loop, sizeof(hl), cudaMemcpyDeviceToHost));
+    uint32_t bits = 0;
+    for (int l = 0; l < nl; l++) {
+      uint32_t c[4];
+      OR3_CUDA(ctx, cudaMemcpy(c, ql[l].counters, sizeof(c), cudaMemcpyDeviceToHost));
+      bits |= c[2];
+    }
+    if (bits || (hl.abort & 2u)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x in a batch", bits);
+    if (hl.abort & 1u) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+    uint32_t done = 0;
+    for (int l = 0; l < nl; l++) {
+      done += hl.lane[l].waves;
+      stats.camera_paths += hl.lane[l].paths;
+    }
+    stats.waves = done;
+    if (done != hl.nwaves) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "device loop completed %u of %u waves", done, hl.nwaves);
+  }
 
   if (write_frames) {
     size_t need = 0;

@@ -1047,14 +1047,8 @@ __global__ void k_texture_sample(DevScene S, int tex, uint32_t n, const float *u
 
 // ---------------------------------------------------------------- batched form kernels
 
-__global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues qp, int out) {
-  const Queues q = oriented(qp, out);  // the queue written is slot 0
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
-    q.counters[out] = num_paths;
-    q.counters[4 + out] = 0;
-  }
-  if (i >= num_paths) return;
+// The camera ray of wave path i into queue slot 0 of q (oriented).
+__device__ __forceinline__ void raygen_batch_one(const Batch &b, const Queues &q, uint32_t i) {
   const uint32_t si = find_segment(b.segs, b.info->nseg, i);
   const Segment sg = b.segs[si];
   const RenderConst &rc = b.jobs[sg.job].rc;
@@ -1068,6 +1062,74 @@ __global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues qp, int out) 
   q.dir[0][i] = make_float4(d.x, d.y, d.z, __uint_as_float(0u));
   q.beta[0][i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(si));
   q.pathL[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_raygen_batch(Batch b, uint32_t num_paths, Queues qp, int out) {
+  const Queues q = oriented(qp, out);  // the queue written is slot 0
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    q.counters[out] = num_paths;
+    q.counters[4 + out] = 0;
+  }
+  if (i < num_paths) raygen_batch_one(b, q, i);
+}
+
+// Device loop: the camera rays of a wave taken in this iteration, into queue
+// 0 (a grid-stride loop: the grid is fixed when the loop is captured).
+__global__ void k_raygen_batch_loop(Batch b, Queues q, const BatchLoop *L, int lane) {
+  if (!L->lane[lane].fresh) return;
+  const uint32_t n = b.info->num_paths;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    q.counters[0] = n;
+    q.counters[4] = 0;
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    raygen_batch_one(b, q, i);
+}
+
+// Device loop head: an idle lane takes the next wave from the shared queue
+// and copies its segments into the lane's table; the lane's loop ends (its
+// conditional handle set to 0) when no wave is left or the batch aborts.
+// One block; thread 0 alone touches the loop state and the handle.
+__global__ void k_wave_take(BatchLoop *L, int lane, const WaveDesc *waves, const Segment *segs_all, Segment *segs,
+                            WaveInfo *info, const uint32_t *counters, cudaGraphConditionalHandle h) {
+  __shared__ int w;
+  if (threadIdx.x == 0) {
+    BatchLoop::Lane &me = L->lane[lane];
+    w = -1;
+    if (counters[2]) atomicOr(&L->abort, 2u);
+    if (me.active && ++me.iters > L->max_iters) atomicOr(&L->abort, 1u);
+    bool stop = atomicOr(&L->abort, 0u) != 0u;
+    if (!stop && !me.active) {
+      const uint32_t t = atomicAdd(&L->next_wave, 1u);
+      if (t < L->nwaves) {
+        w = (int)t;
+        me.active = 1u;
+        me.fresh = 1u;
+        me.iters = 0u;
+      } else {
+        stop = true;
+      }
+    }
+    if (stop) cudaGraphSetConditional(h, 0u);
+  }
+  __syncthreads();
+  if (w < 0) return;
+  const WaveDesc d = waves[w];
+  for (uint32_t k = threadIdx.x; k < d.nseg; k += blockDim.x) segs[k] = segs_all[d.seg_first + k];
+  if (threadIdx.x == 0) *info = WaveInfo{d.nseg, d.ngroups, d.num_paths, 0u};
+}
+
+// Device loop tail: the wave's camera rays are out; a wave whose queue ran
+// empty is complete (accumulated just before) and the lane takes the next.
+__global__ void k_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters) {
+  BatchLoop::Lane &me = L->lane[lane];
+  me.fresh = 0u;
+  if (me.active && counters[0] == 0u) {
+    me.active = 0u;
+    me.waves++;
+    me.paths += info->num_paths;
+  }
 }
 
 // persistent_trace (STEP 2) with the scene chosen per ray by its segment
@@ -1187,9 +1249,7 @@ __global__ void __launch_bounds__(256, 4) k_shadow_batch(Batch b, Queues q) {
 
 // One thread per pixel-sample group (ss2 consecutive paths of one pixel and
 // sample); FP32 partial sums added to the job's FP64 pixel sums.
-__global__ void k_accumulate_batch(Batch b, Queues q) {
-  const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= b.info->ngroups) return;
+__device__ __forceinline__ void accumulate_batch_one(const Batch &b, const Queues &q, uint32_t gi) {
   uint32_t lo = 0, hi = b.info->nseg;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -1213,6 +1273,19 @@ __global__ void k_accumulate_batch(Batch b, Queues q) {
   double *Q = job.sumsq + 3 * pix;
   atomicAdd(S, (double)s0); atomicAdd(S + 1, (double)s1); atomicAdd(S + 2, (double)s2);
   atomicAdd(Q, (double)q0); atomicAdd(Q + 1, (double)q1); atomicAdd(Q + 2, (double)q2);
+}
+
+__global__ void k_accumulate_batch(Batch b, Queues q) {
+  const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi < b.info->ngroups) accumulate_batch_one(b, q, gi);
+}
+
+// Device loop: accumulate the lane's wave once its queue 0 is empty.
+__global__ void k_accumulate_batch_loop(Batch b, Queues q, const BatchLoop *L, int lane) {
+  if (!L->lane[lane].active || q.counters[0] != 0u) return;
+  const uint32_t ng = b.info->ngroups;
+  for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x)
+    accumulate_batch_one(b, q, gi);
 }
 
 }  // namespace
@@ -1416,6 +1489,25 @@ void launch_shade_batch(const Batch &b, const Queues &q, int in, int grid, bool 
 void launch_accumulate_batch(const Batch &b, uint32_t max_groups, const Queues &q, cudaStream_t st) {
   const uint32_t g = (max_groups + 255) / 256;
   k_accumulate_batch<<<g > 0 ? g : 1, 256, 0, st>>>(b, q);
+}
+
+void launch_wave_take(BatchLoop *L, int lane, const WaveDesc *waves, const Segment *segs_all, Segment *segs,
+                      WaveInfo *info, const uint32_t *counters, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_wave_take<<<1, 256, 0, st>>>(L, lane, waves, segs_all, segs, info, counters, h);
+}
+
+void launch_raygen_batch_loop(const Batch &b, const Queues &q, const BatchLoop *L, int lane, int grid,
+                              cudaStream_t st) {
+  k_raygen_batch_loop<<<grid > 0 ? grid : 1, 256, 0, st>>>(b, q, L, lane);
+}
+
+void launch_accumulate_batch_loop(const Batch &b, const Queues &q, const BatchLoop *L, int lane, int grid,
+                                  cudaStream_t st) {
+  k_accumulate_batch_loop<<<grid > 0 ? grid : 1, 256, 0, st>>>(b, q, L, lane);
+}
+
+void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters, cudaStream_t st) {
+  k_wave_finish<<<1, 1, 0, st>>>(L, lane, info, counters);
 }
 
 }  // namespace or3

@@ -107,7 +107,42 @@ struct Batch {
   const WaveInfo *info;
 };
 
+// The device-driven batch loop: every planned wave of the batch sits in one
+// table, and the lanes' looping graphs take waves from a shared head counter
+// until none is left (no host round trip between waves or bounces).
+struct WaveDesc {
+  uint32_t seg_first;  // the wave's first entry in the batch's segment table
+  uint32_t nseg;
+  uint32_t ngroups;
+  uint32_t num_paths;
+};
+
+struct BatchLoop {
+  uint32_t next_wave;  // head of the shared wave queue
+  uint32_t nwaves;
+  uint32_t abort;      // bit 0: a wave's bounce loop passed max_iters; bit 1: a kernel set error bits
+  uint32_t max_iters;  // loop iterations one wave may take
+  struct Lane {
+    uint32_t active;   // the lane holds a wave
+    uint32_t fresh;    // the wave was taken in this iteration: camera rays pending
+    uint32_t iters;    // iterations of the current wave
+    uint32_t waves;    // waves completed
+    unsigned long long paths;  // camera paths completed
+  } lane[3];
+};
+
 void launch_raygen_batch(const Batch &b, uint32_t num_paths, const Queues &q, int out, cudaStream_t st);
+// One iteration of a lane's device loop around its bounces: take a wave when
+// idle (ending the loop through `h` when the queue is empty), then camera
+// rays for a fresh wave; after the bounces, accumulate a finished wave and
+// free the lane.  `segs` / `info` are the lane's (b.segs, b.info).
+void launch_wave_take(BatchLoop *L, int lane, const WaveDesc *waves, const Segment *segs_all, Segment *segs,
+                      WaveInfo *info, const uint32_t *counters, cudaGraphConditionalHandle h, cudaStream_t st);
+void launch_raygen_batch_loop(const Batch &b, const Queues &q, const BatchLoop *L, int lane, int grid,
+                              cudaStream_t st);
+void launch_accumulate_batch_loop(const Batch &b, const Queues &q, const BatchLoop *L, int lane, int grid,
+                                  cudaStream_t st);
+void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters, cudaStream_t st);
 void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, int variant,
                          cudaStream_t st);
 // nee: some job samples lights (the light-sampling instance of the kernel)

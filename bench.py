@@ -579,12 +579,18 @@ def main():
     img = np.zeros((cam.height, 2 * cam.width, 3), np.float64)  # the caller's frame buffer, reused per step
     img[:] = 1.0
     barrier(dist)
+    parts = np.zeros(4)  # wall seconds: upload, render, frame read-back, release
     e0 = time.perf_counter()
     for i in range(e2e_steps):
+        t0 = time.perf_counter()
         sid2 = ctx.upload(sd)
+        t1 = time.perf_counter()
         ctx.render(sid2, cam, seed=50 + i, **kw)
+        t2 = time.perf_counter()
         ctx.frame(cam.width, cam.height, out=img)
+        t3 = time.perf_counter()
         ctx.release(sid2)
+        parts += (t1 - t0, t2 - t1, t3 - t2, time.perf_counter() - t3)
     e2e_s = max_over_ranks(dist, time.perf_counter() - e0)
     e2e_paths = sum_over_ranks(dist, float(paths / args.steps * e2e_steps))
 
@@ -616,7 +622,9 @@ def main():
                                              for k in ("nodes_visited", "tris_tested", "spheres_tested")}},
             "e2e": {"value": e2e_paths / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": frame_bytes,
-                    "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step"},
+                    "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step",
+                    "ms_per_step": {k: float(v) * 1000.0 / e2e_steps
+                                    for k, v in zip(("upload", "render", "frame", "release"), parts)}},
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,

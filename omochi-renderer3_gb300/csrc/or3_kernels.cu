@@ -98,6 +98,13 @@ __global__ void k_raygen(RenderConst rc, Wave w, Queues qp, int out) {
 }
 
 constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
+// Node steps a lane takes between two warp votes of the persistent traversal
+// (persistent_trace): the vote, the refill test and the loop's branches are
+// paid once per pair (measured: extend -3% on the mesh, shadow -2% on the
+// terrain; 3 and 4 steps spill at 64 registers and are slower).  The batched
+// traversal keeps one step per vote: its extra scene registers made the pair
+// spill there (-1.5%).
+constexpr int kStepsPerVote = 2;
 
 // Persistent traversal over a ray source: every lane traces one ray at a time
 // and takes the next one the moment its ray is finished (warp-aggregated
@@ -106,8 +113,9 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // All 32 lanes of every warp must enter (blockDim is a multiple of 32).
 // STEP 1: one node or one leaf per step (leaves go through the stack), refill
 //         any idle lane every step;
-// STEP 2: one node per step with its hit leaves tested in place, refill only
-//         once at least half of the warp is idle (amortises the atomic).
+// STEP 2: one node per step with its hit leaves tested in place, up to
+//         kStepsPerVote steps per vote, refill only once at least half of
+//         the warp is idle (amortises the atomic).
 // REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
 // nearest-first child order (off only for any-hit queries).  FN: STEP 2 over
 // the FP32-box nodes (else the quantised ones).
@@ -146,10 +154,18 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
       break;
     }
     if (r != kNoEntry) {
-      const bool done = W8          ? trav_step_w8<ANY, COUNT>(S, st, stk, cnt)
-                        : STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
-                                    : trav_step_inline<ANY, COUNT, SORT, PairStack, FN, DevScene, NEAREST>(
-                                          S, st, stk, snodes, ns, cnt, err);
+      // STEP 2 takes up to kStepsPerVote node steps per vote (a lane whose ray
+      // ends after the first step sits out the second)
+      constexpr int kSteps = STEP == 2 && !W8 ? kStepsPerVote : 1;
+      bool done = false;
+#pragma unroll
+      for (int k = 0; k < kSteps; k++) {
+        if (done) break;
+        done = W8          ? trav_step_w8<ANY, COUNT>(S, st, stk, cnt)
+               : STEP == 1 ? trav_step<ANY, COUNT>(S, st, stk_e, stk_t, snodes, ns, cnt, err)
+                           : trav_step_inline<ANY, COUNT, SORT, PairStack, FN, DevScene, NEAREST>(
+                                 S, st, stk, snodes, ns, cnt, err);
+      }
       if (done) {
         sink.store(S, r, trav_finish<ANY>(S, st), st.o, st.d);
         r = kNoEntry;

@@ -611,7 +611,8 @@ def main():
             "config": {"workload": desc, "paths_per_step": paths // args.steps,
                        "extension_rays_per_step": ext_rays // args.steps, "triangles": int(info["num_primitives"]),
                        "wide_nodes": int(info["num_nodes"]), "scene_upload_ms": upload_s * 1000.0,
-                       "bvh_build_ms": info["build_ms"], "l2": "flushed between steps (256 MB write)",
+                       "bvh_build_ms": info["build_ms"], "flatten_ms": info["flatten_ms"],
+                       "records_env_upload_ms": info["upload_ms"], "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "wall_s_timed": wall_s, "shadow_rays_per_step": shadow_rays // args.steps,
                        "mrays_per_s": (ext_rays + shadow_rays) / (render_ms / 1000.0) / 1e6,

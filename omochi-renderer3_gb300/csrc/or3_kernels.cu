@@ -105,6 +105,8 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // traversal keeps one step per vote: its extra scene registers made the pair
 // spill there (-1.5%).
 constexpr int kStepsPerVote = 2;
+// The shadow kernel (fewer live registers: no hit record to keep) takes three.
+constexpr int kShadowStepsPerVote = 3;
 
 // Persistent traversal over a ray source: every lane traces one ray at a time
 // and takes the next one the moment its ray is finished (warp-aggregated
@@ -114,13 +116,13 @@ constexpr int kStepsPerVote = 2;
 // STEP 1: one node or one leaf per step (leaves go through the stack), refill
 //         any idle lane every step;
 // STEP 2: one node per step with its hit leaves tested in place, up to
-//         kStepsPerVote steps per vote, refill only once at least half of
+//         VOTE_STEPS steps per vote, refill only once at least half of
 //         the warp is idle (amortises the atomic).
 // REFILL (STEP 2): refill once at least this many lanes are idle.  SORT:
 // nearest-first child order (off only for any-hit queries).  FN: STEP 2 over
 // the FP32-box nodes (else the quantised ones).
 template <bool ANY, bool COUNT, int STEP, class Src, class Sink, int REFILL = 16, bool SORT = true, bool FN = true,
-          bool NEAREST = false, bool W8 = false>
+          bool NEAREST = false, bool W8 = false, int VOTE_STEPS = kStepsPerVote>
 __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, uint32_t *fetch, const Src &src,
                                                  const Sink &sink, const uint4 *snodes, uint32_t ns, uint32_t *cnt,
                                                  uint32_t *err) {
@@ -154,9 +156,9 @@ __device__ __forceinline__ void persistent_trace(const DevScene &S, uint32_t n, 
       break;
     }
     if (r != kNoEntry) {
-      // STEP 2 takes up to kStepsPerVote node steps per vote (a lane whose ray
-      // ends after the first step sits out the second)
-      constexpr int kSteps = STEP == 2 && !W8 ? kStepsPerVote : 1;
+      // STEP 2 takes up to VOTE_STEPS node steps per vote (a lane whose ray
+      // ends early sits out the rest)
+      constexpr int kSteps = STEP == 2 && !W8 ? VOTE_STEPS : 1;
       bool done = false;
 #pragma unroll
       for (int k = 0; k < kSteps; k++) {
@@ -915,7 +917,7 @@ template <bool SORT, bool FN, bool W8 = false, int REFILL = 16>
 __global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, REFILL, SORT, FN, false, W8>(
+  persistent_trace<true, false, 2, ShadowSrc, ShadowSink, REFILL, SORT, FN, false, W8, kShadowStepsPerVote>(
       S, n, &q.counters[6], ShadowSrc{q.sorig, q.sdir}, ShadowSink{q.sorig, q.scontrib, q.pathL}, nullptr, 0u,
       nullptr, &q.counters[2]);
 }

@@ -585,6 +585,9 @@ def main():
         t0 = time.perf_counter()
         sid2 = ctx.upload(sd)
         t1 = time.perf_counter()
+        info2 = ctx.scene_info(sid2)  # the upload's own split (a few microseconds, outside the parts)
+        e0 += time.perf_counter() - t1
+        t1 = time.perf_counter()
         ctx.render(sid2, cam, seed=50 + i, **kw)
         t2 = time.perf_counter()
         ctx.frame(cam.width, cam.height, out=img)
@@ -625,7 +628,9 @@ def main():
                     "d2h_bytes_per_step": frame_bytes,
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step",
                     "ms_per_step": {k: float(v) * 1000.0 / e2e_steps
-                                    for k, v in zip(("upload", "render", "frame", "release"), parts)}},
+                                    for k, v in zip(("upload", "render", "frame", "release"), parts)},
+                    "last_upload_ms": {"flatten": info2["flatten_ms"], "flatten_and_bvh": info2["build_ms"],
+                                       "records_env": info2["upload_ms"]}},
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,

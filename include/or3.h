@@ -212,7 +212,7 @@ typedef struct or3_render_params {
 #define OR3_TUNE_WIDE8 0x4000u         /* or3_render: extension and shadow rays traverse an 8-wide tree made
                                           from the scene's 4-wide one on first use (kept with the scene) */
 #define OR3_TUNE_SHADOW_REFILL8 0x8000u /* or3_render: shadow-ray warps fetch new rays once 8 lanes are idle
-                                          (default 16) */
+                                          (default 24) */
 #define OR3_TUNE_BLOCK_APPEND 0x1000u  /* or3_render: the shade kernel appends rays with one atomic per block
                                           instead of one per warp */
 

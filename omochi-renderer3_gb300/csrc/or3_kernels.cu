@@ -912,8 +912,10 @@ struct ShadowSink {
 // Any-hit test of every queued shadow ray (persistent, lane-refilled).
 // SORT false: children in slot order (no distance sort).
 // FN: FP32-box nodes (else the quantised ones).
-// REFILL: a warp fetches new rays once this many lanes are idle.
-template <bool SORT, bool FN, bool W8 = false, int REFILL = 16>
+// REFILL: a warp fetches new rays once this many lanes are idle (24 at
+// three steps per vote: terrain shadow time 267 ms at 16, 265 ms at 24,
+// 295 ms at 8 per step).
+template <bool SORT, bool FN, bool W8 = false, int REFILL = 24>
 __global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);

@@ -53,7 +53,7 @@ METRIC = "Mpaths/s on 1 GB300 at fixed RMSE vs host-CPU ref; p50/p99 latency whe
 NCU_EXTEND = {
     "mesh": {"dram_bytes_per_ray": 48.3, "issue_active": (0.755, 0.646),
              "source": "ncu --set full, k_extend launches 1-2, mesh scene at 512x384, 8x8 sub-pixel grid"},
-    "terrain": {"dram_bytes_per_ray": 49.8, "issue_active": (0.748, 0.755),
+    "terrain": {"dram_bytes_per_ray": 49.7, "issue_active": (0.747, 0.748),
                 "source": "ncu --set full, k_extend launches 1-2, terrain scene at 480x270, 8x8 sub-pixel grid"},
 }
 

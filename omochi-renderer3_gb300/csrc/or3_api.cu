@@ -30,8 +30,8 @@ int dev_upload(or3_context *ctx, SceneGPU *sg, const std::vector<T> &v, const T 
   *out = nullptr;
   if (v.empty()) return OR3_OK;
   void *p = nullptr;
-  OR3_CUDA(ctx, cudaMalloc(&p, v.size() * sizeof(T)));
-  sg->allocs.push_back(p);
+  OR3_CUDA(ctx, cudaMallocFromPoolAsync(&p, v.size() * sizeof(T), ctx->scene_pool, ctx->stream));
+  sg->pool_allocs.push_back(p);
   OR3_CUDA(ctx, cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
   sg->info.device_bytes += v.size() * sizeof(T);
   *out = static_cast<const T *>(p);
@@ -42,8 +42,8 @@ template <class T>
 int dev_alloc(or3_context *ctx, SceneGPU *sg, T **out, size_t n) {
   *out = nullptr;
   void *p = nullptr;
-  OR3_CUDA(ctx, cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
-  sg->allocs.push_back(p);
+  OR3_CUDA(ctx, cudaMallocFromPoolAsync(&p, std::max<size_t>(n, 1) * sizeof(T), ctx->scene_pool, ctx->stream));
+  sg->pool_allocs.push_back(p);
   sg->info.device_bytes += n * sizeof(T);
   *out = static_cast<T *>(p);
   return OR3_OK;
@@ -89,7 +89,10 @@ int ensure_wide8(or3_context *ctx, SceneGPU *sg) {
   return OR3_OK;
 }
 
+// Callers make sure no kernel still reads the scene (the pool's memory is
+// handed out again in the stream's order).
 void free_scene(SceneGPU *sg) {
+  for (void *p : sg->pool_allocs) cudaFreeAsync(p, sg->stream);
   for (void *p : sg->allocs) cudaFree(p);
   delete sg;
 }
@@ -217,6 +220,14 @@ void build_light_tables(const or3_scene_desc *d, const float *geom, LightTables 
 
 namespace or3 {
 
+// The ray queues are large: memory the pools keep from released scenes and
+// finished uploads goes back to the device before they grow.
+static void trim_pools(or3_context *ctx) {
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->tmp_pool) cudaMemPoolTrimTo(ctx->tmp_pool, 0);
+  if (ctx->scene_pool) cudaMemPoolTrimTo(ctx->scene_pool, 0);
+}
+
 int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   if (paths <= ctx->cap_paths && rays <= ctx->cap_rays) return OR3_OK;
   for (int k = 0; k < 2; k++) {
@@ -234,6 +245,7 @@ int ensure_queues(or3_context *ctx, size_t paths, size_t rays) {
   ctx->hits = ctx->pathL = ctx->sorig = ctx->sdir = ctx->scontrib = nullptr;
   ctx->slist = nullptr;
   ctx->cap_paths = ctx->cap_rays = 0;
+  trim_pools(ctx);
   for (int k = 0; k < 2; k++) {
     OR3_CUDA(ctx, cudaMalloc(&ctx->qorig[k], rays * sizeof(float4)));
     OR3_CUDA(ctx, cudaMalloc(&ctx->qdir[k], rays * sizeof(float4)));
@@ -314,6 +326,7 @@ int ensure_lane(or3_context *ctx, int k, size_t paths, size_t rays, size_t pixel
     cudaFree(L.slist);
     L.slist = nullptr;
     L.cap_paths = L.cap_rays = 0;
+    trim_pools(ctx);
     for (int k = 0; k < 2; k++) {
       OR3_CUDA(ctx, cudaMalloc(&L.qorig[k], rays * sizeof(float4)));
       OR3_CUDA(ctx, cudaMalloc(&L.qdir[k], rays * sizeof(float4)));
@@ -481,6 +494,11 @@ int or3_context_create(int device, or3_context **out) {
     if (cudaMemPoolCreate(&ctx->tmp_pool, &pp) != cudaSuccess) return bail(OR3_ERR_CUDA);
     uint64_t keep = uint64_t(1) << 30;
     cudaMemPoolSetAttribute(ctx->tmp_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (cudaMemPoolCreate(&ctx->scene_pool, &pp) != cudaSuccess) {
+      cudaMemPoolDestroy(ctx->tmp_pool);
+      return bail(OR3_ERR_CUDA);
+    }
+    cudaMemPoolSetAttribute(ctx->scene_pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   if (cudaMalloc(&ctx->counters, 16 * sizeof(uint32_t)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
   if (cudaMalloc(&ctx->dstats, 8 * sizeof(unsigned long long)) != cudaSuccess) return bail(OR3_ERR_OUT_OF_MEMORY);
@@ -544,6 +562,7 @@ int or3_context_destroy(or3_context *ctx) {
     if (e) cudaEventDestroy(e);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->tmp_pool) cudaMemPoolDestroy(ctx->tmp_pool);
+  if (ctx->scene_pool) cudaMemPoolDestroy(ctx->scene_pool);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return OR3_OK;
@@ -674,6 +693,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
 
   auto t0 = std::chrono::steady_clock::now();
   SceneGPU *sg = new SceneGPU();
+  sg->stream = ctx->stream;
   const uint32_t nt = d->num_triangles, nsph = d->num_spheres, np = nt + nsph;
 
   // ---- primitives and their bounds (in the FP32 geometry the kernels test),
@@ -682,7 +702,14 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
                          (d->build == OR3_BUILD_DEVICE ||
                           (d->build == OR3_BUILD_AUTO && np >= OR3_BUILD_DEVICE_MIN_PRIMS));
   FlatPrims fp;
-  const size_t stage_need = kFlatBytes * (size_t)np + 4 * 64;
+  // the sky's bytes go through the same pinned staging (copied on the
+  // flattening threads) instead of a pageable copy
+  const size_t env_bytes = d->env_rgb    ? 3 * sizeof(float) * (size_t)d->env_width * d->env_height
+                           : d->env_rgbe ? 4 * (size_t)d->env_width * d->env_height
+                                         : 0;
+  const void *env_src = d->env_rgb ? (const void *)d->env_rgb : (const void *)d->env_rgbe;
+  char *env_stage = nullptr;
+  const size_t stage_need = kFlatBytes * (size_t)np + env_bytes + 5 * 64;
   if (dev_build && stage_need <= kStageMax) {
     if (ctx->stage_bytes < stage_need) {
       cudaStreamSynchronize(ctx->stream);
@@ -705,6 +732,7 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     fp.bp = reinterpret_cast<BuildPrim *>(carve(sizeof(BuildPrim) * (size_t)np));
     fp.info = reinterpret_cast<PrimInfo *>(carve(sizeof(PrimInfo) * (size_t)np));
     fp.shade = reinterpret_cast<TriShade *>(carve(sizeof(TriShade) * (size_t)np));
+    if (env_bytes) env_stage = carve(env_bytes);
   } else {
     fp.vgeom.resize(12 * (size_t)np);
     fp.vbp.resize(np);
@@ -726,6 +754,10 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
       const uint32_t r = flatten_range(d, a, b, fp, &bb);
       first_bad[t] = r < b ? r : np;
       bad_bounds[t] = bb;
+      if (env_stage) {
+        const size_t e0 = env_bytes * t / nth, e1 = env_bytes * (t + 1) / nth;
+        std::memcpy(env_stage + e0, static_cast<const char *>(env_src) + e0, e1 - e0);
+      }
     };
     std::vector<std::thread> pool;
     for (uint32_t t = 1; t < nth; t++) pool.emplace_back(work, t);
@@ -928,12 +960,14 @@ int or3_scene_upload(or3_context *ctx, const or3_scene_desc *d, int32_t *scene_o
     }
     cudaError_t ce;
     if (d->env_rgb) {
-      ce = cudaMemcpyAsync(env_d, d->env_rgb, 3 * texels * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+      ce = cudaMemcpyAsync(env_d, env_stage ? (const void *)env_stage : (const void *)d->env_rgb,
+                           3 * texels * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
     } else {
       // RGBE bytes (a third of the float map's size) decoded on the device
       uint8_t *rgbe_d = nullptr;
       if ((rc = tmp.alloc(ctx, &rgbe_d, 4 * texels))) { free_scene(sg); return rc; }
-      ce = cudaMemcpyAsync(rgbe_d, d->env_rgbe, 4 * texels, cudaMemcpyHostToDevice, ctx->stream);
+      ce = cudaMemcpyAsync(rgbe_d, env_stage ? (const void *)env_stage : (const void *)d->env_rgbe, 4 * texels,
+                           cudaMemcpyHostToDevice, ctx->stream);
       if (ce == cudaSuccess) launch_decode_rgbe(rgbe_d, texels, env_d, ctx->stream);
     }
     if (ce != cudaSuccess) {
@@ -999,7 +1033,9 @@ int or3_scene_release(or3_context *ctx, int32_t scene) {
   auto it = ctx->scenes.find(scene);
   if (it == ctx->scenes.end()) return fail(ctx, OR3_ERR_NOT_FOUND, "scene %d not found", scene);
   cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
+  // every stream of the device (wave lanes, a running server) is past the
+  // scene's last use before its memory goes back to the pool
+  cudaDeviceSynchronize();
   free_scene(it->second);
   ctx->scenes.erase(it);
   return OR3_OK;

@@ -20,7 +20,9 @@ namespace or3 {
 
 struct SceneGPU {
   DevScene view{};
-  std::vector<void *> allocs;
+  std::vector<void *> allocs;       // cudaMalloc'd (the device BVH build's nodes, the 8-wide tree)
+  std::vector<void *> pool_allocs;  // from the context's scene pool, freed on `stream`
+  cudaStream_t stream = nullptr;
   or3_scene_info info{};
   bool has_split = false;  // a refractive layer exists: paths can split at depth <= 2
 };
@@ -83,6 +85,9 @@ struct or3_context {
   // stream-ordered pool for the temporaries of a scene upload (keeps up to
   // 1 GiB cached between uploads)
   cudaMemPool_t tmp_pool = nullptr;
+  // a scene's records, materials, sky and light tables: kept by the pool when
+  // a scene is released, so the next upload maps no new memory
+  cudaMemPool_t scene_pool = nullptr;
 
   // or3_render's extra wave lanes (two by default): waves are dealt round robin to lane 0
   // (the buffers above) and these, each on its own stream with its own

@@ -474,7 +474,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="triangle-count scale of batched/served scenes")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
-    ap.add_argument("--wave-paths", type=int, default=0, help="batched form: camera paths per wave (0 = library default)")
+    ap.add_argument("--wave-paths", type=int, default=0,
+                    help="camera paths per wave, plain and batched forms (0 = library default)")
     ap.add_argument("--one-lane", action="store_true", help="batched form: every wave on one stream")
     ap.add_argument("--batch-flags", type=int, default=0,
                     help="batched form: extra or3_batch_params.flags (OR3_FLAG_QUANTISED_NODES 128, "
@@ -518,6 +519,9 @@ def main():
               next_event_estimation=st.get("next_event_estimation", False), tuning=args.tuning)
     if args.tuning:
         desc += "_tuning%d" % args.tuning
+    if args.wave_paths:  # smaller waves hold smaller ray queues (profiling captures)
+        kw["wave_paths"] = args.wave_paths
+        desc += "_wave%d" % args.wave_paths
     if args.leaf_max or args.trav_cost:
         sd.leaf_max, sd.traversal_cost = args.leaf_max, args.trav_cost
         desc += "_leaf%d_ct%g" % (args.leaf_max, args.trav_cost)
@@ -580,6 +584,7 @@ def main():
     img[:] = 1.0
     barrier(dist)
     parts = np.zeros(4)  # wall seconds: upload, render, frame read-back, release
+    render_dev_ms = 0.0  # the renders' own device time (CUDA events)
     e0 = time.perf_counter()
     for i in range(e2e_steps):
         t0 = time.perf_counter()
@@ -588,8 +593,9 @@ def main():
         info2 = ctx.scene_info(sid2)  # the upload's own split (a few microseconds, outside the parts)
         e0 += time.perf_counter() - t1
         t1 = time.perf_counter()
-        ctx.render(sid2, cam, seed=50 + i, **kw)
+        r2 = ctx.render(sid2, cam, seed=50 + i, **kw)
         t2 = time.perf_counter()
+        render_dev_ms += r2["render_ms"]
         ctx.frame(cam.width, cam.height, out=img)
         t3 = time.perf_counter()
         ctx.release(sid2)
@@ -629,6 +635,7 @@ def main():
                     "what": "or3_scene_upload (flatten, BVH build, H2D) + or3_render + or3_get_frame per step",
                     "ms_per_step": {k: float(v) * 1000.0 / e2e_steps
                                     for k, v in zip(("upload", "render", "frame", "release"), parts)},
+                    "render_device_ms_per_step": render_dev_ms / e2e_steps,
                     "last_upload_ms": {"flatten": info2["flatten_ms"], "flatten_and_bvh": info2["build_ms"],
                                        "records_env": info2["upload_ms"]}},
             "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,

@@ -1158,7 +1158,7 @@ __global__ void k_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, cons
 // step's node fetch does not wait on a reload of the scene descriptor.
 // FN: the FP32-box nodes (else the 64-byte quantised ones).  HOIST false:
 // every step reads the node array through the scene descriptor instead.
-template <bool ANY, bool COUNT, class Src, class Sink, bool FN = true, bool HOIST = true>
+template <bool ANY, bool COUNT, class Src, class Sink, bool FN = true, bool HOIST = true, int VOTE_STEPS = 1>
 __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t *fetch, const Src &src,
                                             const Sink &sink, uint32_t *cnt, uint32_t *err) {
   uint2 stk_p[kStackSize];
@@ -1197,12 +1197,16 @@ __device__ __forceinline__ void batch_trace(const Batch &b, uint32_t n, uint32_t
       break;
     }
     if (r != kNoEntry) {
-      bool done;
-      if (HOIST) {
-        const TravView tv{fnodes, nodes, sp->prims};
-        done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(tv, st, stk, nullptr, 0u, cnt, err);
-      } else {
-        done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(*sp, st, stk, nullptr, 0u, cnt, err);
+      bool done = false;
+#pragma unroll
+      for (int k = 0; k < VOTE_STEPS; k++) {
+        if (done) break;
+        if (HOIST) {
+          const TravView tv{fnodes, nodes, sp->prims};
+          done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(tv, st, stk, nullptr, 0u, cnt, err);
+        } else {
+          done = trav_step_inline<ANY, COUNT, true, PairStack, FN>(*sp, st, stk, nullptr, 0u, cnt, err);
+        }
       }
       if (done) {
         sink.store(*sp, r, trav_finish<ANY>(*sp, st), st.o, st.d);
@@ -1262,7 +1266,7 @@ template <bool FN = true, bool HOIST = true>
 __global__ void __launch_bounds__(256, 4) k_shadow_batch(Batch b, Queues q) {
   const uint32_t n = min(q.counters[3], q.capacity);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
-  batch_trace<true, false, BatchShadowSrc, ShadowSink, FN, HOIST>(
+  batch_trace<true, false, BatchShadowSrc, ShadowSink, FN, HOIST, kShadowStepsPerVote>(
       b, n, &q.counters[6], BatchShadowSrc{q.sorig, q.sdir, q.scontrib}, ShadowSink{q.sorig, q.scontrib, q.pathL},
       nullptr, &q.counters[2]);
 }

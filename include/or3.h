@@ -245,7 +245,7 @@ typedef struct or3_render_stats {
   double shadow_ms;
   uint64_t shadow_launches;
   uint32_t lanes;          /* wave lanes (streams) the render used */
-  uint32_t reserved;
+  uint32_t waves_rerun;    /* waves whose ray queue a glass split overflowed, rendered again in sub-waves */
   uint64_t kernel_launches; /* kernels this call launched (every kind, counted at each launch) */
 } or3_render_stats;
 

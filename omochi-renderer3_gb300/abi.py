@@ -93,7 +93,7 @@ class RenderStatsC(ctypes.Structure):
                 ("extend_launches", ctypes.c_uint64), ("shade_launches", ctypes.c_uint64),
                 ("nodes_visited", ctypes.c_uint64), ("tris_tested", ctypes.c_uint64),
                 ("spheres_tested", ctypes.c_uint64), ("shadow_ms", ctypes.c_double),
-                ("shadow_launches", ctypes.c_uint64), ("lanes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("shadow_launches", ctypes.c_uint64), ("lanes", ctypes.c_uint32), ("waves_rerun", ctypes.c_uint32),
                 ("kernel_launches", ctypes.c_uint64)]
 
 

@@ -537,6 +537,7 @@ int or3_context_destroy(or3_context *ctx) {
   cudaFree(ctx->pix_sum);
   cudaFree(ctx->pix_sumsq);
   cudaFree(ctx->frame_dev);
+  cudaFree(ctx->wave_fail);
   cudaFreeHost(ctx->frame_pinned);
   cudaFreeHost(ctx->frame_front);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1077,9 +1078,17 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // queues need 8x capacity).  Fewer, larger waves mean fewer bounce
   // iterations and kernel tails (measured on the mesh workload: 4M-path waves
   // 1007 Mpaths/s, 32M-path waves 1285).
-  uint64_t wave = prm->wave_paths ? prm->wave_paths : (sg->has_split ? (1ull << 23) : (1ull << 25));
+  // Where glass can split paths the queues hold kSplitQueueFactor rays per
+  // path, and a wave that overflows them is rendered again in sub-waves (see
+  // the end of the pass).  OR3_FLAG_KEEP_PATHS reads the last wave's per-path
+  // radiance, so it keeps queues no split can overflow (8 rays per path) and
+  // 2^23-path waves.
+  const bool keep_paths = (prm->flags & OR3_FLAG_KEEP_PATHS) != 0;
+  const uint64_t qfactor = !sg->has_split ? 1 : keep_paths ? 8 : kSplitQueueFactor;
+  const bool optimistic = sg->has_split && qfactor < 8;  // a wave's queue can overflow: re-render it
+  uint64_t wave = prm->wave_paths ? prm->wave_paths : (sg->has_split && keep_paths ? (1ull << 23) : (1ull << 25));
   wave = std::max<uint64_t>(wave, ss2);
-  wave = std::min<uint64_t>(wave, 1ull << 30);
+  wave = std::min<uint64_t>(wave, (1ull << 31) / qfactor);  // queue capacities stay 32-bit
   // Waves: whole samples of the full image when one fits, else row chunks of one sample.
   uint64_t ns_per_wave = 1, npix_per_wave = npix;
   if (paths_per_sample <= wave) {
@@ -1088,11 +1097,26 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
     npix_per_wave = std::max<uint64_t>(1, wave / ss2);
   }
   const uint64_t max_wave_paths = ns_per_wave * npix_per_wave * ss2;
-  const uint64_t rays = max_wave_paths * (sg->has_split ? 8 : 1);
+  // a split scene's queues hold at least 8 rays per path of one pixel, so a
+  // one-pixel sub-wave always fits
+  const uint64_t rays = std::max<uint64_t>(max_wave_paths * qfactor, sg->has_split ? 8 * (uint64_t)ss2 : 1);
+  // sub-waves of an overflowed wave: whole pixels, at most rays / 8 paths
+  const uint64_t safe_pix = std::max<uint64_t>(1, rays / 8 / ss2);
+  // the overflow list holds every wave of a pass
+  const uint64_t max_pass_waves =
+      (((uint64_t)prm->max_samples + ns_per_wave - 1) / ns_per_wave) * ((npix + npix_per_wave - 1) / npix_per_wave);
   int rc = ensure_queues(ctx, max_wave_paths, rays);
   if (rc) return rc;
   const size_t frame_doubles = (prm->output_layout == OR3_LAYOUT_REFERENCE ? 2 : 1) * npix * 3;
   if ((rc = ensure_pixels(ctx, npix, frame_doubles))) return rc;
+  if (max_pass_waves + 1 > ctx->cap_wave_fail) {
+    cudaFree(ctx->wave_fail);
+    ctx->wave_fail = nullptr;
+    ctx->cap_wave_fail = 0;
+    OR3_CUDA(ctx, cudaMalloc(&ctx->wave_fail, (max_pass_waves + 1) * sizeof(uint32_t)));
+    ctx->cap_wave_fail = max_pass_waves + 1;
+  }
+  const uint32_t fail_cap = (uint32_t)std::min<uint64_t>(ctx->cap_wave_fail - 1, UINT32_MAX);
 
   RenderConst rcst{};
   fill_render_const(cam, prm, rcst);
@@ -1103,8 +1127,12 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   OR3_CUDA(ctx, cudaMemsetAsync(ctx->frame_dev, 0, frame_doubles * sizeof(double), st));
   OR3_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, 16 * sizeof(uint32_t), st));
   OR3_CUDA(ctx, cudaMemsetAsync(ctx->dstats, 0, 8 * sizeof(unsigned long long), st));
+  OR3_CUDA(ctx, cudaMemsetAsync(ctx->wave_fail, 0, sizeof(uint32_t), st));
 
-  const Queues q = make_queues(ctx);
+  // the render's own capacity, not the allocation's (which earlier, larger
+  // renders may have grown): whether a wave overflows depends on the wave only
+  Queues q = make_queues(ctx);
+  q.capacity = (uint32_t)std::min<uint64_t>(q.capacity, rays);
   const int block = 256;
   const int grid_ext = ctx->num_sms * ctx->occ_extend;
   const int smem_nodes =
@@ -1181,6 +1209,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       break;
     }
     qx[k] = lane_queues(L);
+    qx[k].capacity = (uint32_t)std::min<uint64_t>(qx[k].capacity, rays);
     OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sum, 0, npix * 3 * sizeof(double), st));
     OR3_CUDA(ctx, cudaMemsetAsync(L.pix_sumsq, 0, npix * 3 * sizeof(double), st));
     OR3_CUDA(ctx, cudaMemsetAsync(L.counters, 0, 16 * sizeof(uint32_t), st));
@@ -1290,6 +1319,10 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       launch_accumulate(lane_q(l), w, ss2, lsum, lsq, (int)std::min<uint64_t>((np + 7) / 8, (uint64_t)ctx->num_sms * 64),
                         block, lane_st(l));
       stats.kernel_launches++;
+      if (optimistic) {
+        launch_wave_check(lane_q(l), ctx->wave_fail, fail_cap, (uint32_t)lr[l].wave, lane_st(l));
+        stats.kernel_launches++;
+      }
       stats.waves++;
       stats.camera_paths += w.num_paths;
       ctx->last_wave_paths = w.num_paths;
@@ -1337,7 +1370,8 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
           if (lr[l].wave < 0) continue;
           OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev_poll[l]));
           const uint32_t *hc = lane_hc(l);
-          if (hc[2]) dev_error = true;
+          // a queue overflow only spoils its own wave (re-rendered at the end of the pass)
+          if (hc[2] & (optimistic ? ~kErrQueue : ~0u)) dev_error = true;
           if (!dev_error && hc[lr[l].in] != 0 && lr[l].chunks < 100000) {
             if (int r = enqueue_chunk(l)) return r;
             continue;
@@ -1358,6 +1392,59 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
       stats.kernel_launches++;
       OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters + 8 + 4 * k, L.counters, 4 * sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, st));
+    }
+    // Waves whose ray queue overflowed (glass splits beyond kSplitQueueFactor
+    // rays per path) were not accumulated: each is rendered again, on lane 0,
+    // in sub-waves of whole pixels and one sample that cannot overflow.  The
+    // paths and their random numbers are the same, so is the image.
+    if (optimistic && !stopped) {
+      uint32_t *hf = ctx->host_counters + 28;
+      OR3_CUDA(ctx, cudaMemcpyAsync(hf, ctx->wave_fail, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      OR3_CUDA(ctx, cudaStreamSynchronize(st));
+      const uint32_t nf = *hf;
+      if (nf > fail_cap) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "overflow list full (%u waves)", nf);
+      if (nf) {
+        std::vector<uint32_t> ids(nf);
+        OR3_CUDA(ctx, cudaMemcpy(ids.data(), ctx->wave_fail + 1, nf * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        OR3_CUDA(ctx, cudaMemsetAsync(ctx->wave_fail, 0, sizeof(uint32_t), st));
+        const size_t first_sub = pw.size();
+        for (uint32_t id : ids) {
+          const Wave w = pw[id];
+          stats.camera_paths -= w.num_paths;
+          stats.waves--;
+          stats.waves_rerun++;
+          const uint64_t s0 = w.g_first / (npix * ss2);
+          for (uint32_t j = 0; j < w.ns; j++) {
+            for (uint64_t a = w.pix0; a < (uint64_t)w.pix0 + w.npix; a += safe_pix) {
+              Wave sw = w;
+              sw.ns = 1;
+              sw.pix0 = (uint32_t)a;
+              sw.npix = (uint32_t)std::min<uint64_t>(safe_pix, (uint64_t)w.pix0 + w.npix - a);
+              sw.g_first = ((s0 + j) * npix + a) * ss2;
+              sw.num_paths = sw.npix * ss2;
+              pw.push_back(sw);
+            }
+          }
+        }
+        for (size_t k = first_sub; k < pw.size(); k++) {
+          lr[0].wave = (int)k;
+          lr[0].in = 0;
+          lr[0].chunks = 0;
+          launch_raygen(rcst, pw[k], q, 0, 0, block, st);
+          stats.kernel_launches++;
+          for (;;) {
+            if (int r = enqueue_chunk(0)) return r;
+            if (whole) break;
+            OR3_CUDA(ctx, cudaEventSynchronize(ctx->ev_poll[0]));
+            const uint32_t *hc = lane_hc(0);
+            if (hc[2] || hc[lr[0].in] == 0 || lr[0].chunks >= 100000) break;  // other errors: reported below
+          }
+          finish_wave(0);
+        }
+        OR3_CUDA(ctx, cudaMemcpyAsync(hf, ctx->wave_fail, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        OR3_CUDA(ctx, cudaStreamSynchronize(st));
+        if (*hf) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "ray queue capacity exceeded by a sub-wave");
+      }
     }
     // error bits of the pass (queue capacity, traversal stack)
     OR3_CUDA(ctx, cudaMemcpyAsync(ctx->host_counters, ctx->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost,

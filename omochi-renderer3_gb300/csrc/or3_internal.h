@@ -60,6 +60,8 @@ struct or3_context {
   double *pix_sum = nullptr, *pix_sumsq = nullptr;
   size_t cap_frame = 0;
   double *frame_dev = nullptr;
+  uint32_t *wave_fail = nullptr;  // waves of a pass whose queue overflowed: [0] count, then indices
+  size_t cap_wave_fail = 0;
   // pinned host frames: the pass's copy lands in the back buffer, which then
   // becomes the front (last completed frame, Renderer::GetResult) by a
   // pointer swap under frame_mu

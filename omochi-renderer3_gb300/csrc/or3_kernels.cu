@@ -924,9 +924,23 @@ __global__ void __launch_bounds__(256, 4) k_shadow(DevScene S, Queues q) {
       nullptr, &q.counters[2]);
 }
 
+// After a wave's accumulation: a queue overflow is filed in fail ([0] the
+// count, then wave indices; cap entries) and its bit cleared, so the lane's
+// next wave is judged on its own.
+__global__ void k_wave_check(uint32_t *counters, uint32_t *fail, uint32_t cap, uint32_t wave) {
+  if (!(counters[2] & kErrQueue)) return;
+  const uint32_t k = atomicAdd(fail, 1u);
+  if (k < cap) fail[1 + k] = wave;
+  counters[2] &= ~kErrQueue;
+}
+
 // Per-pixel sums of the wave's path radiance: one warp per pixel, lanes over
 // the pixel's samples (coalesced), FP32 partials added into FP64 sums.
+// A wave whose ray queue overflowed (a glass split past the queue's
+// capacity: the error bit kErrQueue) is not accumulated; k_wave_check files
+// it for a re-render.
 __global__ void k_accumulate(Queues q, Wave w, uint32_t ss2, double *sum, double *sumsq) {
+  if (q.counters[2] & kErrQueue) return;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -1426,6 +1440,10 @@ void launch_shadow_batch(const Batch &b, const Queues &q, int grid, int variant,
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st) {
   k_accumulate<<<grid, block, 0, st>>>(q, w, ss2, sum, sumsq);
+}
+
+void launch_wave_check(const Queues &q, uint32_t *fail, uint32_t cap, uint32_t wave, cudaStream_t st) {
+  k_wave_check<<<1, 1, 0, st>>>(q.counters, fail, cap, wave);
 }
 
 void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,

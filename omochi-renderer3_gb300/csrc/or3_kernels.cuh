@@ -68,6 +68,11 @@ constexpr uint32_t kMetaSpec = 1u << 24;
 
 constexpr uint32_t kErrStack = 1u;
 constexpr uint32_t kErrQueue = 2u;
+// Ray queue capacity per camera path of a wave where glass can split paths.
+// A split (depth <= 2) can make up to 8 rays of one path; a wave whose queue
+// overflows is rendered again in sub-waves of capacity / 8 paths, which
+// cannot overflow, and the same paths give the same image.
+constexpr uint32_t kSplitQueueFactor = 2;
 
 // ---- batched form: one wave holds path ranges ("segments") of many jobs.
 // A job is one render (scene, camera, sample budget); its camera paths keep
@@ -188,6 +193,9 @@ void launch_shadow(const DevScene &S, const Queues &q, int grid, bool unsorted, 
 void launch_shadow_batch(const Batch &b, const Queues &q, int grid, int variant, cudaStream_t st);
 void launch_accumulate(const Queues &q, const Wave &w, uint32_t ss2, double *sum, double *sumsq, int grid,
                        int block, cudaStream_t st);
+// After launch_accumulate: files the wave in fail when its queue overflowed
+// (and clears the bit); fail[0] counts, fail[1..cap] hold wave indices.
+void launch_wave_check(const Queues &q, uint32_t *fail, uint32_t cap, uint32_t wave, cudaStream_t st);
 void launch_frame(const double *sum, uint32_t W, uint32_t H, int layout, double scale, double *out,
                   cudaStream_t st);
 void launch_moments(const double *sum, const double *sumsq, uint32_t W, uint32_t H, double *sum_out,

@@ -261,6 +261,41 @@ def test_wave_lanes_match_one(pkg, ctx, nee, tuning, depth):
     assert f1.sum() > 0
 
 
+@pytest.mark.parametrize("depth", [8, 0])
+def test_split_overflow_renders_waves_again(pkg, ctx, depth):
+    """Where glass can split paths the ray queues hold two rays per camera
+    path of a wave.  Here a glass sphere in front of the camera fills the
+    view: every camera ray splits on entry (depth 0), its refracted ray on
+    the far side (depth 1) and the internal reflection again (depth 2), so
+    the depth-3 bounce holds three rays per path.  Those waves are not
+    accumulated and are rendered again in sub-waves that cannot overflow.
+    The image equals a render whose queues no split can overflow
+    (OR3_FLAG_KEEP_PATHS keeps eight rays per path), up to the order of
+    float additions."""
+    A = pkg.abi
+    sd, cam, _ = pkg.workloads.cornell_box(48, 36)
+    glass = sd.material(A.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    sd.add_sphere((50.0, 50.0, 150.0), 60.0, sd.layers(glass))  # the camera is at z = 250, 100 from its centre
+    sid = ctx.upload(sd)
+    kw = dict(supersamples=2, min_samples=1, max_samples=3, step_samples=1, seed=3, rr_min_depth=3,
+              max_depth=depth, wave_paths=2048)
+    try:
+        s_opt = ctx.render(sid, cam, **kw)
+        f_opt, n_opt = ctx.frame(cam.width, cam.height)
+        m_opt = ctx.moments(cam.width, cam.height)
+        s_safe = ctx.render(sid, cam, flags=A.OR3_FLAG_KEEP_PATHS, **kw)
+        f_safe, n_safe = ctx.frame(cam.width, cam.height)
+        m_safe = ctx.moments(cam.width, cam.height)
+    finally:
+        ctx.release(sid)
+    assert s_opt["waves_rerun"] > 0 and s_safe["waves_rerun"] == 0
+    assert n_opt == n_safe == 3 and s_opt["camera_paths"] == s_safe["camera_paths"]
+    np.testing.assert_allclose(m_opt[0], m_safe[0], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(m_opt[1], m_safe[1], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(f_opt, f_safe, rtol=1e-5, atol=1e-7)
+    assert f_opt.sum() > 0
+
+
 def test_lanes_fall_back_when_device_memory_is_short(pkg, ctx):
     """When another lane's queues do not fit, the render uses the lanes that do
     (same image) instead of failing."""

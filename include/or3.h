@@ -167,7 +167,8 @@ typedef struct or3_camera {
 #define OR3_FLAG_HOST_LOOP 1024u       /* batched form: the host hands out waves and replays each wave's
                                           bounce graph (default: the device runs the whole batch, each lane
                                           one graph launch whose while loop takes waves from a shared
-                                          device queue) */
+                                          device queue); with glass it keeps queues of 8 rays per path
+                                          and 2^23-path waves */
 
 typedef struct or3_render_params {
   int32_t min_samples;   /* PathTracer m_min_samples */

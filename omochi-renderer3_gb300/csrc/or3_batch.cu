@@ -59,6 +59,8 @@ struct BatchBuffers {
   size_t cap_segs_all = 0;
   WaveDesc *wdesc = nullptr;
   size_t cap_wdesc = 0;
+  uint32_t *fail = nullptr;  // waves a glass split overflowed
+  size_t cap_fail = 0;
   BatchLoop *loop = nullptr;
   struct JobOut {
     uint64_t pix_base;
@@ -88,6 +90,7 @@ void destroy_batch_state(or3_context *ctx) {
   cudaFreeHost(b->frame_pinned);
   cudaFree(b->segs_all);
   cudaFree(b->wdesc);
+  cudaFree(b->fail);
   cudaFree(b->loop);
   delete b;
   ctx->batch = nullptr;
@@ -170,6 +173,45 @@ void plan_waves(const std::vector<JobPlan> &jp, uint64_t cap, std::vector<Planne
   flush();
 }
 
+// The segments of the waves `ids` of `src` cut into waves of at most `cap`
+// paths (whole pixel-samples of each job; cap >= every job's ss2), for a
+// re-render of waves whose ray queue a glass split overflowed.
+void replan_waves(const std::vector<PlannedWave> &src, const std::vector<uint32_t> &ids,
+                  const std::vector<JobPlan> &jp, uint64_t cap, std::vector<PlannedWave> &out) {
+  out.clear();
+  PlannedWave cur;
+  auto flush = [&]() {
+    if (cur.num_paths) out.push_back(cur);
+    cur = PlannedWave();
+  };
+  for (uint32_t id : ids) {
+    for (const Segment &s : src[id].segs) {
+      const uint32_t ss2 = jp[s.job].ss2;
+      uint64_t g = s.g_first;
+      const uint64_t end = s.g_first + s.count;
+      while (g < end) {
+        const uint64_t take = std::min<uint64_t>(end - g, cap - cur.num_paths) / ss2 * ss2;
+        if (take == 0) {
+          flush();
+          continue;
+        }
+        Segment t{};
+        t.g_first = g;
+        t.job = s.job;
+        t.wave_first = cur.num_paths;
+        t.count = (uint32_t)take;
+        t.pass_first = s.pass_first;
+        t.group_first = cur.ngroups;
+        cur.segs.push_back(t);
+        cur.num_paths += (uint32_t)take;
+        cur.ngroups += (uint32_t)(take / ss2);
+        g += take;
+      }
+    }
+  }
+  flush();
+}
+
 int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_batch_params *bp,
               or3_render_stats *out, bool write_frames) {
   if (!ctx || (n && !jobs)) return fail(ctx, OR3_ERR_INVALID_ARGUMENT, "null argument");
@@ -218,17 +260,25 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     total_paths += (uint64_t)p.samples * p.per_sample;
     max_ss2 = std::max<uint64_t>(max_ss2, p.ss2);
   }
-  uint64_t cap = bp->wave_paths ? bp->wave_paths : (split ? (1ull << 23) : (1ull << 25));
+  const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
+  const bool device_loop = use_graph && !(bp->flags & OR3_FLAG_HOST_LOOP);
+  // Glass (a split makes up to 8 rays of a path): the device loop's queues
+  // hold kSplitQueueFactor rays per path and a wave that overflows them is
+  // rendered again in smaller waves after the loop; the host loop keeps 8.
+  const uint64_t qfactor = !split ? 1 : device_loop ? kSplitQueueFactor : 8;
+  uint64_t cap = bp->wave_paths ? bp->wave_paths : (split && !device_loop ? (1ull << 23) : (1ull << 25));
   cap = std::max<uint64_t>(cap, max_ss2);
-  cap = std::min<uint64_t>(cap, 1ull << 30);
+  cap = std::min<uint64_t>(cap, (1ull << 31) / qfactor);  // queue capacities stay 32-bit
   cap = std::min<uint64_t>(cap, std::max<uint64_t>(total_paths, max_ss2));
+  const uint64_t rays = std::max<uint64_t>(cap * qfactor, split ? 8 * max_ss2 : 1);
+  const uint64_t safe_cap = std::max<uint64_t>(max_ss2, rays / 8);  // a wave this size cannot overflow
   std::vector<PlannedWave> waves;
   plan_waves(jp, cap, waves);
   size_t max_segs = 1;
   for (const PlannedWave &w : waves) max_segs = std::max(max_segs, w.segs.size());
 
   // device state
-  int rc = ensure_queues(ctx, cap, cap * (split ? 8 : 1));
+  int rc = ensure_queues(ctx, cap, rays);
   if (rc) return rc;
   if ((rc = grow_dev(ctx, B.sum, B.cap_pixels, 3 * pixels))) return rc;
   if ((rc = grow_dev(ctx, B.sumsq, B.cap_sumsq, 3 * pixels))) return rc;
@@ -245,10 +295,11 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
       ql[0] = make_queues(ctx);
       sl[0] = ctx->stream;
     } else {
-      if ((rc = ensure_lane(ctx, l - 1, cap, cap * (split ? 8 : 1), 1))) return rc;
+      if ((rc = ensure_lane(ctx, l - 1, cap, rays, 1))) return rc;
       ql[l] = lane_queues(ctx->xl[l - 1]);
       sl[l] = ctx->xl[l - 1].stream;
     }
+    ql[l].capacity = (uint32_t)std::min<uint64_t>(ql[l].capacity, rays);  // this batch's sizing
     if ((rc = grow_dev(ctx, L.segs, L.cap_segs, max_segs))) return rc;
     if ((rc = grow_pinned(ctx, L.segs_host, L.cap_segs_host, max_segs))) return rc;
     if (!L.info) OR3_CUDA(ctx, cudaMalloc(&L.info, sizeof(WaveInfo)));
@@ -307,8 +358,6 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
         if (x) cudaGraphExecDestroy(x);
     }
   } guard;
-  const bool use_graph = !(bp->flags & OR3_FLAG_NO_GRAPH);
-  const bool device_loop = use_graph && !(bp->flags & OR3_FLAG_HOST_LOOP);
   struct LoopGraphs {
     cudaGraph_t g[3] = {nullptr, nullptr, nullptr};
     ~LoopGraphs() {
@@ -316,31 +365,44 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
         if (x) cudaGraphDestroy(x);
     }
   } lg;
-  if (device_loop) {
-    // the wave queue: all planned waves' segments in one table, read by the
-    // lanes' loop heads as they take waves
+  or3_render_stats stats{};
+  // Device loop, one round over a wave list: the waves' segments go to the
+  // device in one table, read by the lanes' loop heads as they take waves;
+  // per lane a graph whose one node is a while loop, whose body takes a wave
+  // when the lane is idle, runs `unroll` bounces and completes the wave when
+  // its queue is empty.  (Re)captured per round: a round's tables may have
+  // moved.
+  auto prepare_round = [&](const std::vector<PlannedWave> &wv) -> int {
     std::vector<Segment> all;
-    std::vector<WaveDesc> wd(waves.size());
-    for (size_t w = 0; w < waves.size(); w++) {
-      wd[w] = WaveDesc{(uint32_t)all.size(), (uint32_t)waves[w].segs.size(), waves[w].ngroups, waves[w].num_paths};
-      all.insert(all.end(), waves[w].segs.begin(), waves[w].segs.end());
+    std::vector<WaveDesc> wd(wv.size());
+    size_t msegs = 1;
+    for (size_t w = 0; w < wv.size(); w++) {
+      wd[w] = WaveDesc{(uint32_t)all.size(), (uint32_t)wv[w].segs.size(), wv[w].ngroups, wv[w].num_paths};
+      all.insert(all.end(), wv[w].segs.begin(), wv[w].segs.end());
+      msegs = std::max(msegs, wv[w].segs.size());
     }
-    if ((rc = grow_dev(ctx, B.segs_all, B.cap_segs_all, all.size()))) return rc;
-    if ((rc = grow_dev(ctx, B.wdesc, B.cap_wdesc, wd.size()))) return rc;
+    int r = OR3_OK;
+    if ((r = grow_dev(ctx, B.segs_all, B.cap_segs_all, all.size()))) return r;
+    if ((r = grow_dev(ctx, B.wdesc, B.cap_wdesc, wd.size()))) return r;
+    if ((r = grow_dev(ctx, B.fail, B.cap_fail, wd.size()))) return r;
+    for (int l = 0; l < nl; l++)
+      if ((r = grow_dev(ctx, B.lanes[l].segs, B.lanes[l].cap_segs, msegs))) return r;
     if (!B.loop) OR3_CUDA(ctx, cudaMalloc(&B.loop, sizeof(BatchLoop)));
     BatchLoop hl{};
     hl.nwaves = (uint32_t)wd.size();
     hl.max_iters = 1u << 16;  // per wave, as the host loop's replay bound
+    hl.fail_cap = (uint32_t)wd.size();
     if (!all.empty())
       OR3_CUDA(ctx, cudaMemcpyAsync(B.segs_all, all.data(), all.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
     if (!wd.empty())
       OR3_CUDA(ctx, cudaMemcpyAsync(B.wdesc, wd.data(), wd.size() * sizeof(WaveDesc), cudaMemcpyHostToDevice, st));
     OR3_CUDA(ctx, cudaMemcpyAsync(B.loop, &hl, sizeof(hl), cudaMemcpyHostToDevice, st));
     OR3_CUDA(ctx, cudaStreamSynchronize(st));
-    // per lane: a graph whose one node is a while loop; its body takes a wave
-    // when the lane is idle, runs `unroll` bounces, and completes the wave
-    // when its queue is empty
     for (int l = 0; l < nl; l++) {
+      if (guard.g[l]) cudaGraphExecDestroy(guard.g[l]);
+      guard.g[l] = nullptr;
+      if (lg.g[l]) cudaGraphDestroy(lg.g[l]);
+      lg.g[l] = nullptr;
       OR3_CUDA(ctx, cudaGraphCreate(&lg.g[l], 0));
       cudaGraphConditionalHandle h{};
       OR3_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, lg.g[l], 1u, cudaGraphCondAssignDefault));
@@ -359,13 +421,55 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
       launch_raygen_batch_loop(b, ql[l], B.loop, l, ctx->num_sms * 8, sl[l]);
       launch_bounces(l);
       launch_accumulate_batch_loop(b, ql[l], B.loop, l, ctx->num_sms * 8, sl[l]);
-      launch_wave_finish(B.loop, l, L.info, ql[l].counters, sl[l]);
+      launch_wave_finish(B.loop, l, L.info, ql[l].counters, B.fail, sl[l]);
       cudaGraph_t captured = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(sl[l], &captured);
       if (ce != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "device loop capture: %s", cudaGetErrorString(ce));
       const cudaError_t ie = cudaGraphInstantiate(&guard.g[l], lg.g[l], 0);
       if (ie != cudaSuccess) return fail(ctx, OR3_ERR_CUDA, "device loop instantiate: %s", cudaGetErrorString(ie));
     }
+    return OR3_OK;
+  };
+  // Runs a prepared round to its end; adds its completed waves and paths to
+  // the stats and returns the waves a glass split overflowed in `failed`.
+  auto run_round = [&](std::vector<uint32_t> &failed) -> int {
+    if (nl > 1) {
+      OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+      for (int l = 1; l < nl; l++) OR3_CUDA(ctx, cudaStreamWaitEvent(sl[l], ctx->ev_fork, 0));
+    }
+    for (int l = 0; l < nl; l++) OR3_CUDA(ctx, cudaGraphLaunch(guard.g[l], sl[l]));
+    for (int l = 1; l < nl; l++) {
+      OR3_CUDA(ctx, cudaEventRecord(B.lanes[l].ev, sl[l]));
+      OR3_CUDA(ctx, cudaStreamWaitEvent(st, B.lanes[l].ev, 0));
+    }
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    BatchLoop hl{};
+    OR3_CUDA(ctx, cudaMemcpy(&hl, B.loop, sizeof(hl), cudaMemcpyDeviceToHost));
+    uint32_t bits = 0;
+    for (int l = 0; l < nl; l++) {
+      uint32_t c[4];
+      OR3_CUDA(ctx, cudaMemcpy(c, ql[l].counters, sizeof(c), cudaMemcpyDeviceToHost));
+      bits |= c[2];
+    }
+    if (bits || (hl.abort & 2u)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x in a batch", bits);
+    if (hl.abort & 1u) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+    if (hl.nfail > hl.fail_cap) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "overflow list full (%u waves)", hl.nfail);
+    uint32_t done = 0;
+    for (int l = 0; l < nl; l++) {
+      done += hl.lane[l].waves;
+      stats.camera_paths += hl.lane[l].paths;
+    }
+    stats.waves += done;
+    if (done + hl.nfail != hl.nwaves)
+      return fail(ctx, OR3_ERR_DEVICE_REPORTED, "device loop completed %u of %u waves", done + hl.nfail, hl.nwaves);
+    failed.resize(hl.nfail);
+    if (hl.nfail)
+      OR3_CUDA(ctx, cudaMemcpy(failed.data(), B.fail, hl.nfail * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return OR3_OK;
+  };
+  if (device_loop) {
+    OR3_CUDA(ctx, cudaStreamSynchronize(st));
+    if ((rc = prepare_round(waves))) return rc;
   } else if (use_graph) {
     OR3_CUDA(ctx, cudaStreamSynchronize(st));
     for (int l = 0; l < nl; l++) {
@@ -379,9 +483,8 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
     }
   }
 
-  or3_render_stats stats{};
   OR3_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-  if (nl > 1) {  // the extra lanes start after the tables and sums above
+  if (nl > 1 && !device_loop) {  // the extra lanes start after the tables and sums above
     OR3_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     for (int l = 1; l < nl; l++) OR3_CUDA(ctx, cudaStreamWaitEvent(sl[l], ctx->ev_fork, 0));
   }
@@ -413,7 +516,18 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   };
   int live = 0;
   if (device_loop) {  // the lanes' loops run the whole batch
-    for (int l = 0; l < nl; l++) OR3_CUDA(ctx, cudaGraphLaunch(guard.g[l], sl[l]));
+    std::vector<uint32_t> failed;
+    if ((rc = run_round(failed))) return rc;
+    if (!failed.empty()) {
+      // waves a glass split overflowed were not accumulated: their paths
+      // again, in waves that cannot overflow (the same paths, the same image)
+      stats.waves_rerun = (uint32_t)failed.size();
+      std::vector<PlannedWave> sub;
+      replan_waves(waves, failed, jp, safe_cap, sub);
+      if ((rc = prepare_round(sub))) return rc;
+      if ((rc = run_round(failed))) return rc;
+      if (!failed.empty()) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "ray queue capacity exceeded by a sub-wave");
+    }
   } else {
     for (int l = 0; l < nl; l++) {
       if ((rc = start(l))) return rc;
@@ -456,26 +570,6 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   stats.render_ms = ms;
-  if (device_loop) {
-    BatchLoop hl{};
-    OR3_CUDA(ctx, cudaMemcpy(&hl, B.loop, sizeof(hl), cudaMemcpyDeviceToHost));
-    uint32_t bits = 0;
-    for (int l = 0; l < nl; l++) {
-      uint32_t c[4];
-      OR3_CUDA(ctx, cudaMemcpy(c, ql[l].counters, sizeof(c), cudaMemcpyDeviceToHost));
-      bits |= c[2];
-    }
-    if (bits || (hl.abort & 2u)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel reported error bits 0x%x in a batch", bits);
-    if (hl.abort & 1u) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
-    uint32_t done = 0;
-    for (int l = 0; l < nl; l++) {
-      done += hl.lane[l].waves;
-      stats.camera_paths += hl.lane[l].paths;
-    }
-    stats.waves = done;
-    if (done != hl.nwaves) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "device loop completed %u of %u waves", done, hl.nwaves);
-  }
-
   if (write_frames) {
     size_t need = 0;
     for (size_t j = 0; j < n; j++)

@@ -1131,13 +1131,14 @@ __global__ void k_wave_take(BatchLoop *L, int lane, const WaveDesc *waves, const
   if (threadIdx.x == 0) {
     BatchLoop::Lane &me = L->lane[lane];
     w = -1;
-    if (counters[2]) atomicOr(&L->abort, 2u);
+    if (counters[2] & ~kErrQueue) atomicOr(&L->abort, 2u);  // an overflow spoils only its own wave
     if (me.active && ++me.iters > L->max_iters) atomicOr(&L->abort, 1u);
     bool stop = atomicOr(&L->abort, 0u) != 0u;
     if (!stop && !me.active) {
       const uint32_t t = atomicAdd(&L->next_wave, 1u);
       if (t < L->nwaves) {
         w = (int)t;
+        me.wave = t;
         me.active = 1u;
         me.fresh = 1u;
         me.iters = 0u;
@@ -1156,13 +1157,19 @@ __global__ void k_wave_take(BatchLoop *L, int lane, const WaveDesc *waves, const
 
 // Device loop tail: the wave's camera rays are out; a wave whose queue ran
 // empty is complete (accumulated just before) and the lane takes the next.
-__global__ void k_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters) {
+__global__ void k_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, uint32_t *counters, uint32_t *fail) {
   BatchLoop::Lane &me = L->lane[lane];
   me.fresh = 0u;
   if (me.active && counters[0] == 0u) {
     me.active = 0u;
-    me.waves++;
-    me.paths += info->num_paths;
+    if (counters[2] & kErrQueue) {  // not accumulated: filed for a re-render in smaller waves
+      const uint32_t k = atomicAdd(&L->nfail, 1u);
+      if (k < L->fail_cap) fail[k] = me.wave;
+      counters[2] &= ~kErrQueue;
+    } else {
+      me.waves++;
+      me.paths += info->num_paths;
+    }
   }
 }
 
@@ -1320,7 +1327,7 @@ __global__ void k_accumulate_batch(Batch b, Queues q) {
 
 // Device loop: accumulate the lane's wave once its queue 0 is empty.
 __global__ void k_accumulate_batch_loop(Batch b, Queues q, const BatchLoop *L, int lane) {
-  if (!L->lane[lane].active || q.counters[0] != 0u) return;
+  if (!L->lane[lane].active || q.counters[0] != 0u || (q.counters[2] & kErrQueue)) return;
   const uint32_t ng = b.info->ngroups;
   for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x)
     accumulate_batch_one(b, q, gi);
@@ -1548,8 +1555,9 @@ void launch_accumulate_batch_loop(const Batch &b, const Queues &q, const BatchLo
   k_accumulate_batch_loop<<<grid > 0 ? grid : 1, 256, 0, st>>>(b, q, L, lane);
 }
 
-void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters, cudaStream_t st) {
-  k_wave_finish<<<1, 1, 0, st>>>(L, lane, info, counters);
+void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, uint32_t *counters, uint32_t *fail,
+                        cudaStream_t st) {
+  k_wave_finish<<<1, 1, 0, st>>>(L, lane, info, counters, fail);
 }
 
 }  // namespace or3

@@ -127,12 +127,16 @@ struct BatchLoop {
   uint32_t nwaves;
   uint32_t abort;      // bit 0: a wave's bounce loop passed max_iters; bit 1: a kernel set error bits
   uint32_t max_iters;  // loop iterations one wave may take
+  uint32_t nfail;      // waves whose ray queue a glass split overflowed (their indices in the fail list)
+  uint32_t fail_cap;
   struct Lane {
     uint32_t active;   // the lane holds a wave
     uint32_t fresh;    // the wave was taken in this iteration: camera rays pending
     uint32_t iters;    // iterations of the current wave
     uint32_t waves;    // waves completed
     unsigned long long paths;  // camera paths completed
+    uint32_t wave;     // the wave the lane holds
+    uint32_t pad;
   } lane[3];
 };
 
@@ -147,7 +151,10 @@ void launch_raygen_batch_loop(const Batch &b, const Queues &q, const BatchLoop *
                               cudaStream_t st);
 void launch_accumulate_batch_loop(const Batch &b, const Queues &q, const BatchLoop *L, int lane, int grid,
                                   cudaStream_t st);
-void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, const uint32_t *counters, cudaStream_t st);
+// fail: the overflowed waves' indices (L->fail_cap entries); their queue
+// error bit is cleared and they count as neither done nor accumulated.
+void launch_wave_finish(BatchLoop *L, int lane, const WaveInfo *info, uint32_t *counters, uint32_t *fail,
+                        cudaStream_t st);
 void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool count, int variant,
                          cudaStream_t st);
 // nee: some job samples lights (the light-sampling instance of the kernel)

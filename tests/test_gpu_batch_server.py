@@ -79,6 +79,40 @@ def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags, nee):
             ctx.release(s)
 
 
+@pytest.mark.parametrize("flags", [0, 64])
+def test_batch_split_overflow_renders_waves_again(pkg, ctx, flags):
+    """Glass: the device loop's queues hold two rays per camera path.  A job
+    whose camera sees only a glass sphere makes three rays per path at depth
+    3, so its waves overflow; they are not accumulated and are rendered again
+    after the loop in waves that cannot overflow.  Every job still equals its
+    plain render (64 = one lane)."""
+    A = pkg.abi
+    sids, jobs = _jobs(pkg, ctx)
+    sd, cam, _ = pkg.workloads.cornell_box(40, 30)
+    glass = sd.material(A.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    sd.add_sphere((50.0, 50.0, 150.0), 60.0, sd.layers(glass))  # fills the view of the camera at z = 250
+    sids.append(ctx.upload(sd))
+    jobs.append((sids[-1], cam, dict(supersamples=2, min_samples=1, max_samples=2, step_samples=1,
+                                     rr_min_depth=3, max_depth=8, seed=11)))
+    try:
+        alone = [_plain(ctx, *j) for j in jobs]
+        stats, frames = ctx.render_batch(jobs, frames=True, wave_paths=3000, flags=flags)
+        assert stats["waves_rerun"] > 0
+        for k, (sid, cam_k, st) in enumerate(jobs):
+            s, q, n = ctx.batch_moments(k, cam_k.width, cam_k.height)
+            s0, q0, n0, img0 = alone[k]
+            assert n == n0
+            np.testing.assert_allclose(s, s0, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(q, q0, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(frames[k], img0, rtol=1e-5, atol=1e-7)
+        assert stats["camera_paths"] == sum(c.width * c.height * st["supersamples"] ** 2 *
+                                            (st["min_samples"] + (st["max_samples"] - st["min_samples"]) //
+                                             st["step_samples"] * st["step_samples"]) for _, c, st in jobs)
+    finally:
+        for s_ in sids:
+            ctx.release(s_)
+
+
 @pytest.mark.parametrize("flags", [128, 128 | 256])
 def test_batch_over_quantised_nodes(pkg, ctx, flags):
     """OR3_FLAG_QUANTISED_NODES: the 64-byte nodes bound the same leaves more

@@ -479,7 +479,7 @@ def main():
     ap.add_argument("--one-lane", action="store_true", help="batched form: every wave on one stream")
     ap.add_argument("--batch-flags", type=int, default=0,
                     help="batched form: extra or3_batch_params.flags (OR3_FLAG_QUANTISED_NODES 128, "
-                         "OR3_FLAG_RELOAD_SCENE 256)")
+                         "OR3_FLAG_HOIST_NODES 256)")
     ap.add_argument("--batch-only", action="store_true", help="batched form only, no plain renders (profiling)")
     ap.add_argument("--mix", default="config", choices=["config", "small"],
                     help="batched jobs: the stated mix, or small jobs (64-256 px, 16-64 spp)")

@@ -160,8 +160,10 @@ typedef struct or3_camera {
 #define OR3_FLAG_ONE_LANE 64u          /* batched form: every wave on one stream (default: three that overlap) */
 #define OR3_FLAG_QUANTISED_NODES 128u  /* batched form: traverse the 64-byte nodes with 8-bit child boxes
                                           (default: the 128-byte FP32-box nodes) */
-#define OR3_FLAG_RELOAD_SCENE 256u     /* batched form: read each ray's node array through its scene
-                                          descriptor every step (default: copied to registers per ray) */
+#define OR3_FLAG_HOIST_NODES 256u      /* batched form: copy each ray's node array into registers when a
+                                          lane takes the ray (default: read it through the ray's scene
+                                          descriptor every step, which frees the registers for two node
+                                          steps per warp vote) */
 #define OR3_FLAG_UNSORTED_SHADE 512u   /* batched form: one shade kernel for every hit and miss (default where
                                           the batch samples lights: the material-sorted shade) */
 #define OR3_FLAG_HOST_LOOP 1024u       /* batched form: the host hands out waves and replays each wave's

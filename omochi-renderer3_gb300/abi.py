@@ -31,7 +31,7 @@ OR3_FLAG_TIME_KERNELS = 16
 OR3_FLAG_COUNT_TRAVERSAL = 32
 OR3_FLAG_ONE_LANE = 64
 OR3_FLAG_QUANTISED_NODES = 128
-OR3_FLAG_RELOAD_SCENE = 256
+OR3_FLAG_HOIST_NODES = 256
 OR3_FLAG_UNSORTED_SHADE = 512
 OR3_FLAG_HOST_LOOP = 1024
 

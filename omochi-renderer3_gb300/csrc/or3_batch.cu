@@ -334,7 +334,7 @@ int run_batch(or3_context *ctx, const or3_batch_job *jobs, size_t n, const or3_b
   // the bounce loop, captured once per call and lane
   auto lane_batch = [&](int l) { return Batch{B.scenes, B.jobs, B.lanes[l].segs, B.lanes[l].info}; };
   // traversal variant: node layout and how a ray's node array is reached
-  const int tvar = ((bp->flags & OR3_FLAG_QUANTISED_NODES) ? 1 : 0) | ((bp->flags & OR3_FLAG_RELOAD_SCENE) ? 2 : 0);
+  const int tvar = ((bp->flags & OR3_FLAG_QUANTISED_NODES) ? 1 : 0) | ((bp->flags & OR3_FLAG_HOIST_NODES) ? 0 : 2);
   // material-sorted shade where the batch samples lights (as or3_render)
   const bool sorted_shade = shadows && !(bp->flags & OR3_FLAG_UNSORTED_SHADE);
   auto launch_bounces = [&](int l) {

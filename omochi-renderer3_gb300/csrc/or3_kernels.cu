@@ -102,8 +102,9 @@ constexpr int kSmemNodes = 256;  // top nodes staged in shared memory (16 KB)
 // (persistent_trace): the vote, the refill test and the loop's branches are
 // paid once per pair (measured: extend -3% on the mesh, shadow -2% on the
 // terrain; 3 and 4 steps spill at 64 registers and are slower).  The batched
-// traversal keeps one step per vote: its extra scene registers made the pair
-// spill there (-1.5%).
+// extend takes two where it reads each step's node array through the ray's
+// scene descriptor (its default); with the array held in registers the pair
+// spills (-1.5%) and it takes one.
 constexpr int kStepsPerVote = 2;
 // The shadow kernel (fewer live registers: no hit record to keep) takes three.
 constexpr int kShadowStepsPerVote = 3;
@@ -1255,7 +1256,7 @@ struct BatchShadowSrc {
   }
 };
 
-template <bool COUNT, bool FN = true, bool HOIST = true>
+template <bool COUNT, bool FN = true, bool HOIST = true, int VS = 1>
 __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int in) {
   const Queues qo = oriented(q, in);
   const uint32_t n = min(q.counters[in], q.capacity);  // an overflowed queue (error bit set) is read to capacity only
@@ -1264,7 +1265,7 @@ __global__ void __launch_bounds__(256, 4) k_extend_batch(Batch b, Queues q, int 
     if (n) atomicAdd(&q.stats[2], 1ull);
   }
   uint32_t cnt[3] = {0u, 0u, 0u};
-  batch_trace<false, COUNT, BatchQueueSrc, HitSink, FN, HOIST>(
+  batch_trace<false, COUNT, BatchQueueSrc, HitSink, FN, HOIST, VS>(
       b, n, &q.counters[4 + in], BatchQueueSrc{qo.orig[0], qo.dir[0], qo.beta[0]}, HitSink{q.hits}, cnt,
       &q.counters[2]);
   if (COUNT) {
@@ -1519,7 +1520,7 @@ void launch_extend_batch(const Batch &b, const Queues &q, int in, int grid, bool
   }
   switch (variant & 3) {
     case 1: k_extend_batch<false, false, true><<<grid, 256, 0, st>>>(b, q, in); break;
-    case 2: k_extend_batch<false, true, false><<<grid, 256, 0, st>>>(b, q, in); break;
+    case 2: k_extend_batch<false, true, false, 2><<<grid, 256, 0, st>>>(b, q, in); break;
     case 3: k_extend_batch<false, false, false><<<grid, 256, 0, st>>>(b, q, in); break;
     default: k_extend_batch<false, true, true><<<grid, 256, 0, st>>>(b, q, in); break;
   }

@@ -51,8 +51,9 @@ def _plain(ctx, sid, cam, st):
                                                 (3000, 1024 | 64, False), (0, 1024, True), (3000, 1024, True)])
 def test_batch_jobs_equal_their_plain_renders(pkg, ctx, wave_paths, flags, nee):
     """flags 64 = OR3_FLAG_ONE_LANE (every wave on one stream; the default
-    deals waves to three lanes); 256 = OR3_FLAG_RELOAD_SCENE (the node array
-    read through the scene descriptor every step: the same traversal); nee:
+    deals waves to three lanes); 256 = OR3_FLAG_HOIST_NODES (the node array
+    copied to registers per ray instead of read through the scene descriptor
+    every step: the same traversal); nee:
     light sampling on, where the material-sorted shade is the default and 512
     (OR3_FLAG_UNSORTED_SHADE) selects the single shade kernel.  By default each
     lane is one graph launch that takes waves from a device queue until none

@@ -1074,10 +1074,10 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   const uint32_t W = cam->width, H = cam->height, ss = (uint32_t)prm->supersamples, ss2 = ss * ss;
   const uint64_t npix = (uint64_t)W * H;
   const uint64_t paths_per_sample = npix * ss2;
-  // Default waves: 2^25 camera paths (2^23 when glass can split paths, whose
-  // queues need 8x capacity).  Fewer, larger waves mean fewer bounce
+  // Default waves: 2^25 camera paths.  Fewer, larger waves mean fewer bounce
   // iterations and kernel tails (measured on the mesh workload: 4M-path waves
-  // 1007 Mpaths/s, 32M-path waves 1285).
+  // 1007 Mpaths/s, 32M-path waves 1285; the terrain 2440 / 2659 / 2774 / 2829
+  // at 2^22 / 2^23 / 2^24 / 2^25).
   // Where glass can split paths the queues hold kSplitQueueFactor rays per
   // path, and a wave that overflows them is rendered again in sub-waves (see
   // the end of the pass).  OR3_FLAG_KEEP_PATHS reads the last wave's per-path

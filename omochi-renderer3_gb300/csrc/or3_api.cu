@@ -1078,15 +1078,17 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   // iterations and kernel tails (measured on the mesh workload: 4M-path waves
   // 1007 Mpaths/s, 32M-path waves 1285; the terrain 2440 / 2659 / 2774 / 2829
   // at 2^22 / 2^23 / 2^24 / 2^25).
-  // Where glass can split paths the queues hold kSplitQueueFactor rays per
-  // path, and a wave that overflows them is rendered again in sub-waves (see
-  // the end of the pass).  OR3_FLAG_KEEP_PATHS reads the last wave's per-path
-  // radiance, so it keeps queues no split can overflow (8 rays per path) and
-  // 2^23-path waves.
+  // Where glass can split paths the queues hold the scene's split_factor
+  // rays per path (kSplitQueueFactor at first), and a wave that overflows
+  // them is rendered again in sub-waves (see the end of the pass); after such
+  // a render the scene's factor doubles, up to 8, and its default waves
+  // shrink to keep the queues' size (2^26 rays).  OR3_FLAG_KEEP_PATHS reads
+  // the last wave's per-path radiance, so it keeps queues no split can
+  // overflow (8 rays per path) and 2^23-path waves.
   const bool keep_paths = (prm->flags & OR3_FLAG_KEEP_PATHS) != 0;
-  const uint64_t qfactor = !sg->has_split ? 1 : keep_paths ? 8 : kSplitQueueFactor;
+  const uint64_t qfactor = !sg->has_split ? 1 : keep_paths ? 8 : std::min<uint32_t>(sg->split_factor, 8u);
   const bool optimistic = sg->has_split && qfactor < 8;  // a wave's queue can overflow: re-render it
-  uint64_t wave = prm->wave_paths ? prm->wave_paths : (sg->has_split && keep_paths ? (1ull << 23) : (1ull << 25));
+  uint64_t wave = prm->wave_paths ? prm->wave_paths : std::min<uint64_t>(1ull << 25, (1ull << 26) / qfactor);
   wave = std::max<uint64_t>(wave, ss2);
   wave = std::min<uint64_t>(wave, (1ull << 31) / qfactor);  // queue capacities stay 32-bit
   // Waves: whole samples of the full image when one fits, else row chunks of one sample.
@@ -1521,6 +1523,7 @@ int or3_render(or3_context *ctx, int32_t scene, const or3_camera *cam, const or3
   stats.tris_tested = hs[4];
   stats.spheres_tested = hs[5];
   stats.samples = prev;
+  if (stats.waves_rerun && sg->split_factor < 8u) sg->split_factor *= 2u;  // the scene's next renders
   stats.passes = passes;
   stats.upload_ms = sg->info.build_ms + sg->info.upload_ms;
   ctx->last = stats;

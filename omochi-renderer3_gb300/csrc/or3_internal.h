@@ -25,6 +25,9 @@ struct SceneGPU {
   cudaStream_t stream = nullptr;
   or3_scene_info info{};
   bool has_split = false;  // a refractive layer exists: paths can split at depth <= 2
+  // ray queue capacity per camera path for or3_render where paths can split:
+  // kSplitQueueFactor, doubled (up to 8) after a render whose waves overflowed
+  uint32_t split_factor = kSplitQueueFactor;
 };
 
 struct BatchBuffers;  // or3_batch.cu

@@ -271,7 +271,8 @@ def test_split_overflow_renders_waves_again(pkg, ctx, depth):
     accumulated and are rendered again in sub-waves that cannot overflow.
     The image equals a render whose queues no split can overflow
     (OR3_FLAG_KEEP_PATHS keeps eight rays per path), up to the order of
-    float additions."""
+    float additions, and the scene's next render, with its queue factor
+    doubled, overflows no wave."""
     A = pkg.abi
     sd, cam, _ = pkg.workloads.cornell_box(48, 36)
     glass = sd.material(A.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
@@ -286,9 +287,13 @@ def test_split_overflow_renders_waves_again(pkg, ctx, depth):
         s_safe = ctx.render(sid, cam, flags=A.OR3_FLAG_KEEP_PATHS, **kw)
         f_safe, n_safe = ctx.frame(cam.width, cam.height)
         m_safe = ctx.moments(cam.width, cam.height)
+        # the overflow doubled the scene's queue factor: its next render fits
+        s_again = ctx.render(sid, cam, **kw)
+        m_again = ctx.moments(cam.width, cam.height)
     finally:
         ctx.release(sid)
-    assert s_opt["waves_rerun"] > 0 and s_safe["waves_rerun"] == 0
+    assert s_opt["waves_rerun"] > 0 and s_safe["waves_rerun"] == 0 and s_again["waves_rerun"] == 0
+    np.testing.assert_allclose(m_again[0], m_safe[0], rtol=1e-5, atol=1e-7)
     assert n_opt == n_safe == 3 and s_opt["camera_paths"] == s_safe["camera_paths"]
     np.testing.assert_allclose(m_opt[0], m_safe[0], rtol=1e-5, atol=1e-7)
     np.testing.assert_allclose(m_opt[1], m_safe[1], rtol=1e-5, atol=1e-7)

@@ -208,10 +208,11 @@ int run_wave(or3_context *ctx, Server &S, std::vector<SJob *> &act) {
     d.sum = j.sum;
     d.sumsq = j.sumsq;
   }
-  // Segments, lane by lane: each lane takes up to cap / lanes paths, fair
-  // shares of the active jobs first, then leftover room.
+  // Segments, lane by lane: each lane takes up to cap paths (its queues are
+  // sized for a whole wave: larger waves make every kernel cheaper per ray),
+  // fair shares of the active jobs first, then leftover room.
   const size_t nl = S.lanes.size();
-  const uint64_t cap_l = std::max<uint64_t>(S.cap / nl, 1);
+  const uint64_t cap_l = std::max<uint64_t>(S.cap, 1);
   std::vector<uint64_t> taken(na, 0);
   uint64_t used_all = 0;
   for (size_t l = 0; l < nl; l++) {

@@ -415,6 +415,7 @@ typedef struct or3_server_stats {
   double first_frame_p50_s;
   uint64_t peak_active_jobs;
   uint64_t peak_budget_bytes;
+  uint64_t waves_rerun;    /* waves with a lane a glass split overflowed (rendered again in pieces) */
 } or3_server_stats;
 
 int or3_server_start(or3_context *ctx, const or3_server_params *params, or3_job_frame_callback cb, void *user);

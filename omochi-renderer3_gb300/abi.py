@@ -134,7 +134,8 @@ class ServerStatsC(ctypes.Structure):
                 ("busy_s", ctypes.c_double), ("device_ms", ctypes.c_double), ("latency_p50_s", ctypes.c_double),
                 ("latency_p99_s", ctypes.c_double), ("queue_p50_s", ctypes.c_double),
                 ("queue_p99_s", ctypes.c_double), ("first_frame_p50_s", ctypes.c_double),
-                ("peak_active_jobs", ctypes.c_uint64), ("peak_budget_bytes", ctypes.c_uint64)]
+                ("peak_active_jobs", ctypes.c_uint64), ("peak_budget_bytes", ctypes.c_uint64),
+                ("waves_rerun", ctypes.c_uint64)]
 
 
 class MeshC(ctypes.Structure):

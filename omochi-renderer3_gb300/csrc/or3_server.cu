@@ -70,8 +70,9 @@ struct Server {
   Clock::time_point t0;
   uint64_t cap = 0;
   bool split = false;
+  uint64_t rays = 0;  // a lane's queue capacity (kSplitQueueFactor rays per path where glass can split)
   // stats
-  uint64_t paths = 0, waves = 0, submitted = 0, finished = 0, cancelled = 0;
+  uint64_t paths = 0, waves = 0, submitted = 0, finished = 0, cancelled = 0, waves_rerun = 0;
   double device_ms = 0, busy_s = 0;
   int error = OR3_OK;
   std::string error_msg;
@@ -278,16 +279,22 @@ int run_wave(or3_context *ctx, Server &S, std::vector<SJob *> &act) {
   }
   // replay each lane's bounce loop until its queue is empty, visiting the
   // lanes in turn (the others keep running meanwhile)
+  std::vector<Segment> redo;  // segments of lanes whose queue overflowed
   for (int rep = 0; live > 0; rep++) {
     if (rep > (1 << 18)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
     for (size_t l = 0; l < nl; l++) {
       Server::Lane &L = S.lanes[l];
       if (!L.live) continue;
       OR3_CUDA(ctx, cudaEventSynchronize(L.ev));
-      if (L.hc[2]) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel error bits 0x%x", L.hc[2]);
+      if (L.hc[2] & ~kErrQueue) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel error bits 0x%x", L.hc[2]);
       if (L.hc[0] == 0) {
         const Batch b{S.scenes_dev, S.jobs_dev, L.segs_dev, L.info_dev};
-        launch_accumulate_batch(b, (uint32_t)L.groups, L.q, L.st);
+        if (L.hc[2] & kErrQueue) {  // a glass split overflowed the queue: rendered again below
+          redo.insert(redo.end(), L.segs.begin(), L.segs.end());
+          OR3_CUDA(ctx, cudaMemsetAsync(L.q.counters + 2, 0, sizeof(uint32_t), L.st));
+        } else {
+          launch_accumulate_batch(b, (uint32_t)L.groups, L.q, L.st);
+        }
         if (l) {
           OR3_CUDA(ctx, cudaEventRecord(L.ev, L.st));
           OR3_CUDA(ctx, cudaStreamWaitEvent(st, L.ev, 0));
@@ -300,6 +307,40 @@ int run_wave(or3_context *ctx, Server &S, std::vector<SJob *> &act) {
       OR3_CUDA(ctx, cudaMemcpyAsync(L.hc, L.q.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, L.st));
       OR3_CUDA(ctx, cudaEventRecord(L.ev, L.st));
     }
+  }
+  // Overflowed lanes: their segments again, on lane 0, in pieces of at most
+  // a queue's capacity / 8 paths, one piece per sub-wave (the same paths).
+  if (!redo.empty()) {
+    Server::Lane &L = S.lanes[0];
+    const Batch b{S.scenes_dev, S.jobs_dev, L.segs_dev, L.info_dev};
+    for (const Segment &sg : redo) {
+      const uint64_t ss2 = act[sg.job]->ss2;
+      const uint64_t piece = std::max<uint64_t>(ss2, S.rays / 8 / ss2 * ss2);
+      for (uint64_t off = 0; off < sg.count; off += piece) {
+        Segment t = sg;
+        t.g_first = sg.g_first + off;
+        t.count = (uint32_t)std::min<uint64_t>(piece, sg.count - off);
+        t.wave_first = 0;
+        t.group_first = 0;
+        L.segs_host[0] = t;
+        L.info_host->nseg = 1;
+        L.info_host->ngroups = (uint32_t)(t.count / ss2);
+        L.info_host->num_paths = t.count;
+        OR3_CUDA(ctx, cudaMemcpyAsync(L.segs_dev, L.segs_host, sizeof(Segment), cudaMemcpyHostToDevice, L.st));
+        OR3_CUDA(ctx, cudaMemcpyAsync(L.info_dev, L.info_host, sizeof(WaveInfo), cudaMemcpyHostToDevice, L.st));
+        launch_raygen_batch(b, t.count, L.q, 0, L.st);
+        for (int rep = 0;; rep++) {
+          if (rep > (1 << 18)) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "bounce loop did not end");
+          OR3_CUDA(ctx, cudaGraphLaunch(L.graph, L.st));
+          OR3_CUDA(ctx, cudaMemcpyAsync(L.hc, L.q.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, L.st));
+          OR3_CUDA(ctx, cudaStreamSynchronize(L.st));
+          if (L.hc[2]) return fail(ctx, OR3_ERR_DEVICE_REPORTED, "kernel error bits 0x%x in a re-rendered piece", L.hc[2]);
+          if (L.hc[0] == 0) break;
+        }
+        launch_accumulate_batch(b, t.count / (uint32_t)ss2, L.q, L.st);
+      }
+    }
+    S.waves_rerun++;
   }
   OR3_CUDA(ctx, cudaEventRecord(S.e1, st));
   OR3_CUDA(ctx, cudaEventSynchronize(S.e1));
@@ -508,14 +549,19 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
     shadows = shadows || kv.second->view.num_lights > 0 || kv.second->view.env_light != 0;
   }
   if (scenes.empty()) return bail(fail(ctx, OR3_ERR_NOT_FOUND, "upload scenes before starting the server"));
-  S->cap = S->p.wave_paths ? S->p.wave_paths : (S->split ? (1ull << 23) : (1ull << 24));
+  // Glass: the queues hold kSplitQueueFactor rays per path, and a lane whose
+  // wave a split overflows is rendered again in pieces that cannot overflow
+  // (run_wave), so waves need not shrink to 1/8 of the queues.
+  const uint64_t qfactor = S->split ? kSplitQueueFactor : 1;
+  S->cap = S->p.wave_paths ? S->p.wave_paths : (S->split ? (1ull << 25) : (1ull << 24));
   S->cap = std::max<uint64_t>(S->cap, 1u << 16);
-  S->cap = std::min<uint64_t>(S->cap, 1ull << 30);
+  S->cap = std::min<uint64_t>(S->cap, (1ull << 31) / qfactor);
+  S->rays = S->cap * qfactor;
   const uint32_t maxa = S->p.max_active_jobs ? S->p.max_active_jobs : 64;
   S->cap_segs = 4 * maxa + 64;
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
-  int rc = ensure_queues(ctx, S->cap, S->cap * (S->split ? 8 : 1));
+  int rc = ensure_queues(ctx, S->cap, S->rays);
   if (rc) return bail(rc);
   S->budget = S->p.hbm_budget_bytes ? S->p.hbm_budget_bytes : free_b / 2;
   if (cudaMalloc(&S->scenes_dev, scenes.size() * sizeof(DevScene)) != cudaSuccess ||
@@ -533,10 +579,11 @@ static int server_start(or3_context *ctx, const or3_server_params *params, or3_j
       L.st = ctx->stream;
       L.q = make_queues(ctx);
     } else {
-      if ((rc = ensure_lane(ctx, l - 1, S->cap, S->cap * (S->split ? 8 : 1), 1))) return bail(rc);
+      if ((rc = ensure_lane(ctx, l - 1, S->cap, S->rays, 1))) return bail(rc);
       L.st = ctx->xl[l - 1].stream;
       L.q = lane_queues(ctx->xl[l - 1]);
     }
+    L.q.capacity = (uint32_t)std::min<uint64_t>(L.q.capacity, S->rays);  // the server's sizing
     if (cudaMalloc(&L.segs_dev, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
         cudaMallocHost(&L.segs_host, S->cap_segs * sizeof(Segment)) != cudaSuccess ||
         cudaMalloc(&L.info_dev, sizeof(WaveInfo)) != cudaSuccess ||
@@ -686,6 +733,7 @@ int or3_server_get_stats(or3_context *ctx, or3_server_stats *out) {
   out->jobs_cancelled = S->cancelled;
   out->camera_paths = S->paths;
   out->waves = S->waves;
+  out->waves_rerun = S->waves_rerun;
   out->busy_s = S->busy_s;
   out->device_ms = S->device_ms;
   out->latency_p50_s = percentile(lat, 0.5);

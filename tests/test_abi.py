@@ -61,6 +61,7 @@ int main(void) {
   S(or3_render_params) O(or3_render_params, seed) O(or3_render_params, flags)
   S(or3_render_stats) O(or3_render_stats, render_ms) O(or3_render_stats, passes) O(or3_render_stats, lanes) O(or3_render_stats, kernel_launches)
   S(or3_scene_info) O(or3_scene_info, build_ms) O(or3_scene_info, tree_depth) O(or3_scene_info, flatten_ms)
+  S(or3_server_stats) O(or3_server_stats, latency_p50_s) O(or3_server_stats, waves_rerun)
   return 0;
 }
 """
@@ -75,7 +76,8 @@ def test_ctypes_layouts_match_the_header(pkg):
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
     a = pkg.abi
     py = {"or3_material": a.Material, "or3_scene_desc": a.SceneDescC, "or3_camera": a.CameraC,
-          "or3_render_params": a.RenderParamsC, "or3_render_stats": a.RenderStatsC, "or3_scene_info": a.SceneInfoC}
+          "or3_render_params": a.RenderParamsC, "or3_render_stats": a.RenderStatsC, "or3_scene_info": a.SceneInfoC,
+          "or3_server_stats": a.ServerStatsC}
     for line in out.strip().splitlines():
         key, val = line.split()
         if "." in key:

@@ -205,6 +205,44 @@ def test_server_continuous_batching_same_alone_and_in_mix(pkg, ctx, one_lane, ne
             ctx.release(s)
 
 
+def test_server_split_overflow_renders_pieces_again(pkg, ctx):
+    """Glass: the server's queues hold two rays per camera path.  A job whose
+    camera sees only a glass sphere overflows its lanes' queues (three rays
+    per path at depth 3); those lanes are not accumulated and their segments
+    are rendered again in pieces that cannot overflow: every job still
+    equals its plain render."""
+    A = pkg.abi
+    sids, jobs = _jobs(pkg, ctx)
+    # 153,600 paths: once the small jobs are done it fills whole lanes
+    # (65,536 paths each, queues of 131,072 rays)
+    sd, cam, _ = pkg.workloads.cornell_box(160, 120)
+    glass = sd.material(A.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
+    sd.add_sphere((50.0, 50.0, 150.0), 60.0, sd.layers(glass))  # fills the view of the camera at z = 250
+    sids.append(ctx.upload(sd))
+    jobs.append((sids[-1], cam, dict(supersamples=2, min_samples=1, max_samples=2, step_samples=1,
+                                     rr_min_depth=3, max_depth=8, seed=11)))
+    alone = [_plain(ctx, *j) for j in jobs]
+    ctx.server_start(keep_moments=True, frame_every_samples=1, wave_paths=1 << 16)
+    try:
+        ids = [ctx.server_submit(j[0], j[1], **j[2]) for j in jobs]
+        ctx.server_drain(120.0)
+        stats = ctx.server_stats()
+        assert stats["waves_rerun"] > 0
+        for k, jid in enumerate(ids):
+            cam_k = jobs[k][1]
+            assert ctx.server_poll(jid)["state"] == A.OR3_JOB_DONE
+            s, q, n = ctx.server_moments(jid, cam_k.width, cam_k.height)
+            s0, q0, n0, _ = alone[k]
+            assert n == n0
+            np.testing.assert_allclose(s, s0, rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(q, q0, rtol=1e-5, atol=1e-6)
+        assert stats["jobs_done"] == len(jobs)
+    finally:
+        ctx.server_stop()
+        for s_ in sids:
+            ctx.release(s_)
+
+
 def test_server_budget_admission_and_cancel(pkg, ctx):
     sids, jobs = _jobs(pkg, ctx)
     big = pkg.workloads.cornell_box(64, 64)

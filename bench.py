@@ -413,7 +413,7 @@ def run_served(args, pkg):
             if t > secs:
                 break
             reqs.append((t,) + tuple(W.served_request(rng, len(sids), lambda k: eyes[k])))
-        ctx.server_start(frame_every_samples=1)
+        ctx.server_start(frame_every_samples=1, wave_paths=args.wave_paths)
         tstart = time.perf_counter()
         for t_arr, s, cam, st in reqs:
             time.sleep(max(0.0, tstart + t_arr - time.perf_counter()))

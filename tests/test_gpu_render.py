@@ -261,8 +261,8 @@ def test_wave_lanes_match_one(pkg, ctx, nee, tuning, depth):
     assert f1.sum() > 0
 
 
-@pytest.mark.parametrize("depth", [8, 0])
-def test_split_overflow_renders_waves_again(pkg, ctx, depth):
+@pytest.mark.parametrize("depth,wave", [(8, 2048), (0, 2048), (8, 32768)])
+def test_split_overflow_renders_waves_again(pkg, ctx, depth, wave):
     """Where glass can split paths the ray queues hold two rays per camera
     path of a wave.  Here a glass sphere in front of the camera fills the
     view: every camera ray splits on entry (depth 0), its refracted ray on
@@ -278,8 +278,10 @@ def test_split_overflow_renders_waves_again(pkg, ctx, depth):
     glass = sd.material(A.OR3_REFRACTION, (0.99, 0.99, 0.99), ior=1.5)
     sd.add_sphere((50.0, 50.0, 150.0), 60.0, sd.layers(glass))  # the camera is at z = 250, 100 from its centre
     sid = ctx.upload(sd)
-    kw = dict(supersamples=2, min_samples=1, max_samples=3, step_samples=1, seed=3, rr_min_depth=3,
-              max_depth=depth, wave_paths=2048)
+    # wave 2048: passes of one sample in row chunks; 32768: one pass of three
+    # samples in one wave (re-rendered one sample at a time)
+    kw = dict(supersamples=2, min_samples=1 if wave == 2048 else 3, max_samples=3, step_samples=1, seed=3,
+              rr_min_depth=3, max_depth=depth, wave_paths=wave)
     try:
         s_opt = ctx.render(sid, cam, **kw)
         f_opt, n_opt = ctx.frame(cam.width, cam.height)
